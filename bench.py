@@ -1,0 +1,418 @@
+#!/usr/bin/env python
+"""Benchmark of the group-then-align hot path on one GB300 (or N replicas).
+
+Workload (one step): the device hot path over 200,000 synthetic DNA
+sequences from 20,000 families (uniform roots 200-3000 nt, GC 0.45, members
+with 1-10 % substitutions and 1 % indels of mean length 2, seed 2) at
+identity 95 with 64 bands:
+  sketch (64 minhash signatures per sequence) -> bucket (rep rows of 64
+  bands) -> candidate pairs of all bands, deduplicated -> banded bit-parallel
+  LCS of every distinct pair -> sorted unique edge list.
+The packed database is resident in HBM before timing; L2 is flushed (256 MiB
+write) before every timed step.  Leiden and the result file (host, unchanged
+from the reference) are not part of the step.
+
+metric  seqs clustered/s = sequences / step time (whole job, all ranks).
+e2e     the same through ngia_ctx_run_host on pinned host buffers: H2D of the
+        packed planes, offsets and lengths, the device path, D2H of the edges.
+--impl reference   times the reference's own CPU implementation of the same
+        path (makedb pack+sketch+group, buildGraph candidates+align+emit;
+        the reference code built as a host OpenMP program) on a bounded
+        sample of the workload with all host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+IDENTITY = 95
+BANDS = 64
+N_SEQS, N_FAMILIES, SEED = 200_000, 20_000, 2
+WORKLOAD = "dna_200k_seqs_20k_families_id95_64bands"
+DATA = ("synthetic: seeded DNA families (uniform roots 200-3000 nt, GC 0.45, 1-10% subs, "
+        "1% indels mean 2), 10 members per family")
+ALIGN_OPS_PER_WORD_STEP = 5  # AND, add with carry in, carry out, and-not, or
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--n-seqs", type=int, default=N_SEQS)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--ref-families", type=int, default=0,
+                   help="families in the reference arm's sample (default: sized to ~10 s)")
+    return p.parse_args()
+
+
+# ---- distributed bookkeeping (replicas: every rank runs the whole workload) --------
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def max_over_ranks(pg, value: float) -> float:
+    if pg is None:
+        return value
+    import torch
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+# ---- workload ---------------------------------------------------------------------
+def make_database(n_seqs: int, n_families: int, seed: int, workdir: Path):
+    import ngia2_gb300 as ng
+    from ngia2_gb300 import synth
+    t0 = time.time()
+    s = synth.dna_families(n_seqs, n_families, seed)
+    fasta = workdir / "workload.fa"
+    s.write_fasta(fasta)
+    packed = workdir / "workload.packed"
+    ng.makedb(fasta, packed)
+    db = ng.read_packed(packed)
+    log(f"workload: {db['n']} sequences, {int(db['lens'].sum())} residues "
+        f"({time.time() - t0:.1f} s to generate + makedb)")
+    return db, fasta, packed
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in self.path.read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for k, name in enumerate(names):
+                    if f[5 + k].lower().startswith("active"):
+                        reasons.add(name)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+# ---- the reference's CPU implementation --------------------------------------------
+class StdoutToStderr:
+    """The reference code prints progress on stdout; keep stdout for the one
+    JSON line by pointing file descriptor 1 at stderr meanwhile."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        os.dup2(2, 1)
+        return self
+
+    def __exit__(self, *exc):
+        import ctypes
+        ctypes.CDLL(None).fflush(None)
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+
+
+def reference_step(fasta: Path, workdir: Path) -> tuple[float, dict]:
+    """One pass of the reference's own code (host build): makedb + buildGraph."""
+    import oracle
+    packed = workdir / "ref.packed"
+    with StdoutToStderr():
+        t0 = time.perf_counter()
+        rc = oracle.ref_makedb(fasta, packed)
+        t1 = time.perf_counter()
+        if rc != 0:
+            raise RuntimeError(f"reference makedb failed ({rc})")
+        r, _, _ = oracle.ref_build_graph(packed, IDENTITY, BANDS, 1 << 22)
+        t2 = time.perf_counter()
+    return t2 - t0, {"makedb_s": t1 - t0, "build_graph_s": t2 - t1, "edges": int(len(r))}
+
+
+def port_step(db) -> tuple[float, dict]:
+    """One pass of the C oracle (single thread): sketch, bucket, graph."""
+    import numpy as np
+
+    import oracle
+    t0 = time.perf_counter()
+    sigs = oracle.sketch_all(db["packed"], db["offsets"], db["lens"])
+    rep = np.stack([oracle.bucket_band(sigs[b]) for b in range(BANDS)])
+    e, _ = oracle.graph_edges(db["packed"], db["offsets"], db["lens"], rep, IDENTITY, BANDS)
+    return time.perf_counter() - t0, {"edges": int(len(e))}
+
+
+def cpu_sample(n_families: int, workdir: Path):
+    """A bounded sample of the workload: fewer families, same generator (so the
+    per-sequence work distribution is the workload's)."""
+    import ngia2_gb300 as ng
+    from ngia2_gb300 import synth
+    s = synth.dna_families(n_families * (N_SEQS // N_FAMILIES), n_families, SEED + 1000)
+    fasta = workdir / "sample.fa"
+    s.write_fasta(fasta)
+    return fasta, len(s)
+
+
+def run_cpu_baseline(workdir: Path, steps: int, warmup: int, families: int) -> dict:
+    import oracle
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    fasta, n = cpu_sample(families, workdir)
+    if oracle.ref_available():
+        kind, cores = "reference", int(os.environ["OMP_NUM_THREADS"])
+        fn = lambda: reference_step(fasta, workdir)  # noqa: E731
+    else:
+        import ngia2_gb300 as ng
+        kind, cores = "port", 1
+        ng.makedb(fasta, workdir / "sample.packed")
+        db = ng.read_packed(workdir / "sample.packed")
+        fn = lambda: port_step(db)  # noqa: E731
+    for _ in range(warmup):
+        fn()
+    times, info = [], {}
+    for _ in range(steps):
+        t, info = fn()
+        times.append(t)
+    mean = sum(times) / len(times)
+    return {"value": n / mean, "unit": "seqs/s", "cores": cores, "kind": kind,
+            "sample": f"{n} sequences ({families} families) of the same generator, "
+                      f"identity {IDENTITY}, {BANDS} bands; mean of {steps} passes",
+            "seconds_per_pass": mean, "detail": info}
+
+
+# ---- our arm -----------------------------------------------------------------------
+def run_ours(args, world, rank, local, pg):
+    import numpy as np
+    import torch
+
+    import ngia2_gb300 as ng
+    torch.cuda.set_device(local)
+    workdir = Path(tempfile.mkdtemp(prefix="ngia_bench_"))
+    n_fam = max(1, args.n_seqs // (N_SEQS // N_FAMILIES))
+    db, fasta, _ = make_database(args.n_seqs, n_fam, SEED, workdir)
+    n = db["n"]
+    stream = torch.cuda.Stream()
+    ctx = ng.Context(stream.cuda_stream)
+    ctx.load(db["packed"], db["offsets"], db["lens"])
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b), out
+
+    step = lambda: ctx.group_align(IDENTITY, BANDS)  # noqa: E731
+    for _ in range(args.warmup):
+        step()
+    barrier(pg)
+    torch.cuda.synchronize()
+    launches0 = ng.kernel_launches()
+    ms, stats = [], []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t, (m, st) = timed(step)
+            ms.append(t)
+            stats.append(st)
+    launches = ng.kernel_launches() - launches0
+    torch.cuda.synchronize()
+    barrier(pg)
+    mean_ms = sum(ms) / len(ms)
+    mean_ms_max = max_over_ranks(pg, mean_ms)
+    st = stats[-1]
+    cells = st["aligned_cells"]
+    align_ms = statistics.mean(s["ms_align"] for s in stats)
+
+    # e2e through the C ABI on pinned host buffers
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        v = t.numpy().view(a.dtype)
+        v[:] = a.reshape(-1)
+        return t, v
+    _, h_packed = pinned(np.ascontiguousarray(db["packed"]))
+    _, h_offs = pinned(np.ascontiguousarray(db["offsets"]))
+    _, h_lens = pinned(np.ascontiguousarray(db["lens"]))
+    edge_cap = max(1, int(st["unique_pairs"]))
+    t_edges = torch.empty(edge_cap * ng.EDGE_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+    h_edges = t_edges.numpy().view(ng.EDGE_DTYPE)
+    e2e_step = lambda: ctx.run_host(h_packed, h_offs, h_lens, IDENTITY, BANDS, h_edges)  # noqa
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_ms = []
+    m_e2e = 0
+    for _ in range(args.steps):
+        t, (m_e2e, _) = timed(e2e_step)
+        e2e_ms.append(t)
+    e2e_mean = max_over_ranks(pg, sum(e2e_ms) / len(e2e_ms))
+    h2d = h_packed.nbytes + h_offs.nbytes + h_lens.nbytes
+    d2h = m_e2e * ng.EDGE_DTYPE.itemsize + 8
+
+    if rank != 0:
+        ctx.close()
+        return None
+    int_peak = ng.int32_peak(stream.cuda_stream)
+    align_ops = cells / 32 * ALIGN_OPS_PER_WORD_STEP
+    achieved = align_ops / (align_ms * 1e-3)
+    traffic = None
+    tfile = ROOT / "profiles" / "align_traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get("bytes_per_cell")
+            traffic = traffic * cells if traffic else None
+        except ValueError:
+            traffic = None
+    line = {
+        "metric": "seqs clustered/s", "value": world * n / (mean_ms_max * 1e-3),
+        "unit": "seqs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mean_ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": DATA,
+        "config": {"workload": WORKLOAD, "n_seqs": n, "families": n_fam, "identity": IDENTITY,
+                   "bands": BANDS, "stages": "sketch+bucket+candidates+align+emit",
+                   "l2": "flushed before every timed step (256 MiB write)",
+                   "parallelism": f"replicas x{world}"},
+        "aligned_cells_per_s": cells / (mean_ms_max * 1e-3),
+        "align_cells_per_s_kernel": cells / (align_ms * 1e-3),
+        "stages_ms": {k: statistics.mean(s[k] for s in stats)
+                      for k in ("ms_sketch", "ms_bucket", "ms_pairs", "ms_align", "ms_emit")},
+        "work": {"candidate_pairs": st["candidate_pairs"], "unique_pairs": st["unique_pairs"],
+                 "aligned_cells": cells, "edges": st["edges"]},
+        "roofline": {"bound": "int32_alu", "kernel": "align (width-class kernels, one phase)",
+                     "achieved": achieved / 1e12, "peak": int_peak / 1e12,
+                     "unit": "Tops/s (32-bit lane ops)", "frac": achieved / int_peak,
+                     "ops_per_32_cells": ALIGN_OPS_PER_WORD_STEP,
+                     "peak_source": "measured: ngia_int32_peak (lop3 chains, all SMs)",
+                     "traffic": traffic},
+        "e2e": {"value": world * n / (e2e_mean * 1e-3), "unit": "seqs/s",
+                "ms_per_step": e2e_mean, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches // max(1, args.steps) * args.steps,
+        "clocks": clk.summary(),
+        "hbm_peak_gbs": peaks().get("hbm_gbs"),
+    }
+    ctx.close()
+    if world == 1 and not args.no_cpu_baseline:
+        try:
+            fam = args.ref_families or 400
+            line["cpu_baseline"] = run_cpu_baseline(workdir, 1, 0, fam)
+        except Exception as e:  # reported, never silently dropped
+            line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+    return line
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    workdir = Path(tempfile.mkdtemp(prefix="ngia_ref_"))
+    fam = args.ref_families or 1000
+    base = run_cpu_baseline(workdir, args.steps, args.warmup, fam)
+    return {
+        "metric": "seqs clustered/s", "value": base["value"], "unit": "seqs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": base["seconds_per_pass"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": DATA,
+        "config": {"workload": WORKLOAD, "identity": IDENTITY, "bands": BANDS,
+                   "stages": "makedb (pack+sketch+group) + buildGraph (candidates+align+emit)",
+                   "sample": base["sample"]},
+        "impl": "reference",
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": base["value"], "unit": "seqs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "detail": base.get("detail"),
+    }
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        line = run_reference(args, world, rank)
+    else:
+        line = run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+    if line is not None and rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

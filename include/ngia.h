@@ -1,0 +1,216 @@
+/*
+ * ngia.h -- C ABI of the GB300 group-then-align library (libngia.so).
+ *
+ * Drop-in for nGIA2's hot path: minhash sketching, band bucketing, banded
+ * bit-parallel LCS alignment and identity-threshold edge emission.  All
+ * arithmetic is integer (plus the reference's float threshold tests) and is
+ * bit-exact with the reference.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: NGIA_OK (0) or a negative
+ *    NGIA_ERR_* code.  Nothing throws across the ABI and nothing prints.
+ *  - Pointers named d_* are device pointers owned by the caller; h_* are host
+ *    pointers.  `stream` is a cudaStream_t passed as void* (NULL = legacy
+ *    default stream).  Calls are asynchronous on `stream` unless documented.
+ *  - Entry points that need scratch memory take it from the CUDA stream-ordered
+ *    allocator (cudaMallocAsync) on `stream` and release it before returning
+ *    control of the stream.
+ *  - One host thread per ngia_ctx.  Contexts on different threads are
+ *    independent.
+ *
+ * Data layouts (the reference's packed file, src/makedb.hpp:1-21)
+ *  - packed region: records {u32 len; u32 planes[4*ceil(len/32)]}; bit r of
+ *    plane e of block b is bit e of the 4-bit code of residue 32*b + r.
+ *  - rec_offsets: u64 word offset of each record inside the packed region
+ *    (the reference's packedOffsets after src/buildGraph.hpp:172-177).
+ *  - signatures / rep rows: band-major u32 [bands][n]; row b of the rep area
+ *    is rep[b][i] = largest j < i with sig[b][j] == sig[b][i], else i.
+ *  - jobs: u32 triples (rep, tar, score) as kernel_dynamic uses them.
+ */
+#ifndef NGIA_H
+#define NGIA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NGIA_BANDS 64        /* GROUP_BANDS, src/makedb.hpp:45 */
+#define NGIA_MAX_READ 65534u /* reads of length >= 0xFFFF are dropped, src/makedb.hpp:118 */
+
+enum {
+  NGIA_OK = 0,
+  NGIA_ERR_ARG = -1,     /* invalid argument (size, identity, bands, NULL) */
+  NGIA_ERR_CUDA = -2,    /* a CUDA runtime call or kernel launch failed */
+  NGIA_ERR_NOMEM = -3,   /* device or host allocation failed */
+  NGIA_ERR_IO = -4,      /* file could not be read or written completely */
+  NGIA_ERR_FORMAT = -5,  /* malformed FASTA or packed file */
+  NGIA_ERR_STATE = -6    /* call out of order (e.g. no database loaded) */
+};
+
+/* One emitted edge: the reference's tuple<int,int,float>(rep, tar, score/100)
+ * (src/buildGraph.hpp:344-347). */
+typedef struct ngia_edge {
+  int32_t rep;
+  int32_t tar;
+  float weight;
+} ngia_edge;
+
+/* Band-bound rounding of ceil(L - Lt*t) (src/buildGraph.hpp:208-210):
+ * NGIA_ROUND_FMA rounds the fused multiply-add once, as a GPU build with
+ * multiply-add contraction does; NGIA_ROUND_SPLIT rounds the product first. */
+#define NGIA_ROUND_SPLIT 0
+#define NGIA_ROUND_FMA 1
+
+const char *ngia_status_string(int status);
+/* The cudaError_t of the last NGIA_ERR_CUDA on this thread (0 if none). */
+int ngia_last_cuda_error(void);
+/* Library version string. */
+const char *ngia_version(void);
+/* Kernels this process has launched through the library so far. */
+unsigned long long ngia_kernel_launches(void);
+
+/* Rounding mode used by the alignment entry points (process-wide; default
+ * NGIA_ROUND_FMA).  Returns the previous mode. */
+int ngia_set_round_mode(int mode);
+
+/* ---- stage (a): sketch --------------------------------------------------------
+ * 64 minhash signatures per record, written band-major: d_sigs[b*n + i].
+ * Replaces the signing half of MakeDB::packData (src/makedb.hpp:224-248).
+ * No scratch memory. */
+int ngia_sketch(const uint32_t *d_packed, const uint64_t *d_rec_offsets,
+                uint32_t n, uint32_t *d_sigs, void *stream);
+
+/* ---- stage (b): bucket --------------------------------------------------------
+ * Rep rows from band-major signatures: d_rep[b*n + i] for b < bands.
+ * Replaces MakeDB::groupSignatures (src/makedb.hpp:289-364): a stable radix
+ * sort of (sig, idx) per band and the predecessor chain.  Scratch: about
+ * 16 * bands * n bytes from the stream-ordered allocator. */
+int ngia_bucket(const uint32_t *d_sigs, uint32_t n, uint32_t bands,
+                uint32_t *d_rep, void *stream);
+
+/* ---- stage (c): align ---------------------------------------------------------
+ * Drop-in for BuildGraph::kernel_dynamic (src/buildGraph.hpp:192-253, launch
+ * at :323; same kernel at src/fastClustering.hpp:183-244, launch at :313):
+ * for every job, jobs[3j+2] = identity score of (rep = jobs[3j], tar =
+ * jobs[3j+1]); pairs failing the length filter keep their score word.
+ * identity in 1..99.  One launch.  No scratch memory. */
+int ngia_align_pairs(const uint32_t *d_packed, const uint64_t *d_rec_offsets,
+                     uint32_t *d_jobs, uint32_t count, uint32_t identity,
+                     void *stream);
+
+/* ---- stage (d): emit ------------------------------------------------------------
+ * Edge emission of one job batch (src/buildGraph.hpp:339-349): every job with
+ * score > 0 becomes ngia_edge{rep, tar, score/100.0f}, in job order.
+ * d_edges needs room for count edges; *d_n_edges (device u32) receives the
+ * number written.  Scratch: 4*ceil(count/1024) bytes. */
+int ngia_emit_edges(const uint32_t *d_jobs, uint32_t count,
+                    ngia_edge *d_edges, uint32_t *d_n_edges, void *stream);
+
+/* Sort + unique of an edge list by (rep, tar, weight), in place on the device
+ * (src/buildGraph.hpp:357-358).  *h_n is the count in, the unique count out.
+ * Synchronises `stream`.  n_nodes bounds the indices. */
+int ngia_sort_unique_edges(ngia_edge *d_edges, uint32_t *h_n, uint32_t n_nodes,
+                           void *stream);
+
+/* ---- whole graph build on a resident database -----------------------------------
+ * ngia_ctx keeps the packed database, its rep rows and all scratch resident
+ * on the device.  Inputs are copied once; every later call reuses them. */
+typedef struct ngia_ctx ngia_ctx;
+
+typedef struct ngia_stats {
+  uint64_t candidate_pairs; /* pairs over all bands, duplicates included (the
+                               reference's "compare pairs", buildGraph.hpp:353) */
+  uint64_t unique_pairs;    /* distinct (rep, tar) pairs aligned */
+  uint64_t aligned_cells;   /* 1024 x 32x32 blocks visited over unique pairs */
+  uint64_t edges;           /* emitted edges (sorted, unique) */
+  double ms_sketch, ms_bucket, ms_pairs, ms_align, ms_emit; /* device time */
+} ngia_stats;
+
+int ngia_ctx_create(ngia_ctx **ctx, void *stream);
+void ngia_ctx_destroy(ngia_ctx *ctx);
+
+/* Load a database from host arrays: the packed region (words), record
+ * offsets, read lengths (index order) and optionally `bands` rep rows
+ * (band-major; NULL = compute them on the device with sketch + bucket). */
+int ngia_ctx_load(ngia_ctx *ctx, const uint32_t *h_packed, uint64_t packed_words,
+                  const uint64_t *h_rec_offsets, const uint32_t *h_lens,
+                  uint32_t n, const uint32_t *h_rep, uint32_t bands);
+
+/* Same from a packed file written by makedb (reference format). */
+int ngia_ctx_load_packed_file(ngia_ctx *ctx, const char *path, uint32_t bands,
+                              int use_file_rep_rows);
+
+/* Recompute sketches and rep rows on the device from the loaded planes. */
+int ngia_ctx_sketch_bucket(ngia_ctx *ctx, uint32_t bands);
+
+/* buildGraph: candidates of bands 0..bands-1, deduplicated, aligned
+ * (length-binned batched kernels), emitted, sorted and uniqued on the device.
+ * Result stays on the device; *h_n_edges receives the count.  Synchronises. */
+int ngia_ctx_build_graph(ngia_ctx *ctx, uint32_t identity, uint32_t bands,
+                         uint64_t *h_n_edges, ngia_stats *stats);
+
+/* The whole device hot path on the resident planes: sketch + bucket of
+ * `bands` rep rows, then ngia_ctx_build_graph.  Fills every stats field.
+ * Synchronises. */
+int ngia_ctx_group_align(ngia_ctx *ctx, uint32_t identity, uint32_t bands,
+                         uint64_t *h_n_edges, ngia_stats *stats);
+
+/* Copy the last graph's edges to the host (cap entries at most). */
+int ngia_ctx_edges(ngia_ctx *ctx, ngia_edge *h_edges, uint64_t cap);
+
+/* Fast greedy clustering (src/fastClustering.hpp:249-352): per band, targets
+ * not yet assigned are aligned against their rep and assigned on a hit;
+ * h_cluster[i] = root index.  Synchronises. */
+int ngia_ctx_fast_cluster(ngia_ctx *ctx, uint32_t identity, uint32_t bands,
+                          uint32_t *h_cluster, ngia_stats *stats);
+
+/* Copy the device rep rows (bands x n) to the host. */
+int ngia_ctx_rep_rows(ngia_ctx *ctx, uint32_t *h_rep, uint32_t bands);
+
+/* End-to-end call on host buffers: copy the database in, sketch + bucket,
+ * build the graph, copy the edges out (the reference's makedb grouping plus
+ * buildGraph in one call).  Device buffers of the context are reused across
+ * calls.  Synchronises. */
+int ngia_ctx_run_host(ngia_ctx *ctx, const uint32_t *h_packed,
+                      uint64_t packed_words, const uint64_t *h_rec_offsets,
+                      const uint32_t *h_lens, uint32_t n, uint32_t identity,
+                      uint32_t bands, ngia_edge *h_edges, uint64_t cap,
+                      uint64_t *h_n_edges, ngia_stats *stats);
+
+/* Measured throughput of 32-bit three-input logic ops (lop3) over the whole
+ * device, in lane-operations per second: the integer-ALU ceiling used as the
+ * roofline of the integer-bound kernels.  Synchronises. */
+int ngia_int32_peak(void *stream, double *ops_per_s);
+
+/* ---- host side of the drop-in (C++ host code in the same library) -------------- */
+
+/* makedb (src/main.cu:54-83): FASTA -> packed file.  Index, length filter and
+ * stable length-descending order on the host, pack on the host, sketch and
+ * bucket on the device.  Returns the number of sequences in *n_out. */
+int ngia_makedb(const char *fasta_path, const char *packed_path, uint32_t *n_out);
+
+/* LeidenOmp::cluster (src/leidenParallel.hpp:265-322) on the host. */
+int ngia_leiden(const ngia_edge *h_edges, uint64_t m, uint32_t n,
+                float resolution, uint32_t seed, int iterations,
+                uint32_t *h_cluster);
+
+/* The resolution main() derives from the identity (src/main.cu:114-116). */
+float ngia_leiden_resolution(uint32_t identity);
+
+/* SaveResult::save (src/saveResult.hpp:31-83). */
+int ngia_save_result(const uint32_t *h_cluster, uint32_t n,
+                     const char *packed_path, const char *result_path);
+
+/* The whole `-m clustering` / `-m fast` mode on a packed file
+ * (src/main.cu:86-156).  fast != 0 selects fast mode. */
+int ngia_cluster_file(const char *packed_path, const char *result_path,
+                      uint32_t identity, uint32_t bands, int fast,
+                      ngia_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,135 @@
+// align.cu -- alignment kernels: the drop-in job-triple kernel and the
+// length-binned batched kernels.
+#include "align.cuh"
+#include "kernels.cuh"
+
+namespace ngia {
+
+// One thread per job, in job order: the drop-in for the reference's
+// one-launch-per-band kernel_dynamic<<<ceil(count/64), 64>>> (launch at
+// src/buildGraph.hpp:323).  The window width is picked per pair at run time.
+__device__ __forceinline__ uint32_t lcs_any(const uint32_t *rep, const uint32_t *tar,
+                                            const Band &b, uint32_t *lines) {
+  if (b.width <= 4) return lcs_window<4>(rep, tar, b);
+  if (b.width <= 8) return lcs_window<8>(rep, tar, b);
+  if (b.width <= 16) return lcs_window<16>(rep, tar, b);
+  return lcs_general(rep, tar, b, lines);
+}
+
+__global__ void __launch_bounds__(128)
+align_jobs_kernel(const uint32_t *__restrict__ packed,
+                  const uint64_t *__restrict__ offs, uint32_t *__restrict__ jobs,
+                  uint32_t count, float t, int fma_mode) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= count) return;
+  const uint32_t *rep = packed + offs[jobs[3 * j]];
+  const uint32_t *tar = packed + offs[jobs[3 * j + 1]];
+  const uint32_t lr = __ldg(rep), lt = __ldg(tar);
+  const Band b = make_band(lr, lt, t, fma_mode);
+  if (!b.pass) return;  // the reference leaves the score word as it was
+  uint32_t lines[kMaxRowBlocks];
+  const uint32_t lcs = lcs_any(rep, tar, b, lines);
+  jobs[3 * j + 2] = identity_score(lcs, lr, lt, t);
+}
+
+// Same over a job list whose length lives in device memory (graph-capturable
+// per-band rounds of fast mode).  Grid-stride.
+__global__ void __launch_bounds__(128)
+align_jobs_dev_count_kernel(const uint32_t *__restrict__ packed,
+                            const uint64_t *__restrict__ offs,
+                            uint32_t *__restrict__ jobs,
+                            const uint32_t *__restrict__ d_count, float t,
+                            int fma_mode) {
+  const uint32_t count = *d_count;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count;
+       j += gridDim.x * blockDim.x) {
+    const uint32_t *rep = packed + offs[jobs[3 * j]];
+    const uint32_t *tar = packed + offs[jobs[3 * j + 1]];
+    const uint32_t lr = __ldg(rep), lt = __ldg(tar);
+    const Band b = make_band(lr, lt, t, fma_mode);
+    if (!b.pass) continue;
+    uint32_t lines[kMaxRowBlocks];
+    const uint32_t lcs = lcs_any(rep, tar, b, lines);
+    jobs[3 * j + 2] = identity_score(lcs, lr, lt, t);
+  }
+}
+
+// Batched form: pairs of one width class, listed in `order[begin, end)`.
+template <int W>
+__global__ void __launch_bounds__(128)
+align_class_kernel(const uint32_t *__restrict__ packed,
+                   const uint64_t *__restrict__ offs, const uint2 *__restrict__ pairs,
+                   const uint32_t *__restrict__ order, uint32_t begin, uint32_t end,
+                   uint32_t *__restrict__ scores, float t, int fma_mode) {
+  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= end) return;
+  const uint32_t p = order[k];
+  const uint2 pr = pairs[p];
+  const uint32_t *rep = packed + offs[pr.x];
+  const uint32_t *tar = packed + offs[pr.y];
+  const uint32_t lr = __ldg(rep), lt = __ldg(tar);
+  const Band b = make_band(lr, lt, t, fma_mode);
+  uint32_t lcs;
+  if constexpr (W > 0) {
+    lcs = lcs_window<W>(rep, tar, b);
+  } else {
+    uint32_t lines[kMaxRowBlocks];
+    lcs = lcs_general(rep, tar, b, lines);
+  }
+  scores[p] = identity_score(lcs, lr, lt, t);
+}
+
+int launch_align_jobs(const uint32_t *packed, const uint64_t *offs, uint32_t *jobs,
+                      uint32_t count, uint32_t identity, cudaStream_t s) {
+  if (count == 0) return NGIA_OK;
+  align_jobs_kernel<<<ceil_div(count, 128u), 128, 0, s>>>(
+      packed, offs, jobs, count, identity_threshold(identity), round_mode());
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
+                                uint32_t *jobs, const uint32_t *d_count,
+                                uint32_t max_count, uint32_t identity,
+                                cudaStream_t s) {
+  if (max_count == 0) return NGIA_OK;
+  const uint32_t blocks = ceil_div(max_count, 128u);
+  align_jobs_dev_count_kernel<<<blocks, 128, 0, s>>>(
+      packed, offs, jobs, d_count, identity_threshold(identity), round_mode());
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+int launch_align_class(int cls, const uint32_t *packed, const uint64_t *offs,
+                       const uint2 *pairs, const uint32_t *order, uint32_t begin,
+                       uint32_t end, uint32_t *scores, uint32_t identity,
+                       cudaStream_t s) {
+  if (end <= begin) return NGIA_OK;
+  const float t = identity_threshold(identity);
+  const int fm = round_mode();
+  const uint32_t blocks = ceil_div(end - begin, 128u);
+  switch (cls) {
+    case 0: align_class_kernel<4><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case 1: align_class_kernel<8><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case 2: align_class_kernel<12><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case 3: align_class_kernel<16><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case 4: align_class_kernel<24><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case 5: align_class_kernel<32><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case kGeneralClass: align_class_kernel<0><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    default: return NGIA_ERR_ARG;
+  }
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+}  // namespace ngia
+
+extern "C" int ngia_align_pairs(const uint32_t *d_packed, const uint64_t *d_rec_offsets,
+                                uint32_t *d_jobs, uint32_t count, uint32_t identity,
+                                void *stream) {
+  if (identity < 1 || identity > 99) return NGIA_ERR_ARG;
+  if (count == 0) return NGIA_OK;
+  if (!d_packed || !d_rec_offsets || !d_jobs) return NGIA_ERR_ARG;
+  return ngia::launch_align_jobs(d_packed, d_rec_offsets, d_jobs, count, identity,
+                                 ngia::as_stream(stream));
+}

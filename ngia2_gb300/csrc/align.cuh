@@ -1,0 +1,246 @@
+// align.cuh -- banded bit-parallel LCS of one (rep, tar) pair (internal header).
+//
+// Restates BuildGraph::kernel_dynamic (src/buildGraph.hpp:192-253), identical
+// to FastClustering::kernel_dynamic (src/fastClustering.hpp:183-244).
+//
+// Recurrence.  Rows are the representative's residues, columns the target's.
+// A row bit is 1 while the row is unmatched.  One column step with match mask
+// M (rows whose 4-bit code equals the column's code; code 0 matches nothing)
+// is the bit-parallel LCS update
+//     V' = (V + (V & M) + carry_in) | (V & ~M)
+// applied to the multi-word vector of the rows inside the band, the carry
+// rippling upward from the band's lowest row block (carry 0 there).  The
+// reference applies it block by block (32 columns x 32 rows, column carries
+// kept in a shift register); here one column step updates every live row
+// word at once, which is the same set of dependencies evaluated in another
+// order, and the word-to-word carry is the hardware carry flag.
+//
+// Window form (lcs_window<W>).  Live row blocks [J0(I), J1(I)) never exceed
+// min(ls + rs, nr) words and both ends advance by at most one block per
+// column block, so the live rows sit in a register window V[0..W) based at
+// J0: when J0 advances, V[0] retires into the LCS sum and the window shifts
+// down; a row block entering at J1 gets its four bit planes loaded.  Window
+// slots above J1 hold all-ones with zero planes: zero planes mean code 0,
+// which matches nothing, so those words stay all-ones and only pass the carry
+// through -- exactly the "not yet visited" state of the reference.
+//
+// Match masks are computed from the bit planes with no lookup table:
+//   u = (P0 & T0) | (~P0 & B);  u &= ~(Pe ^ Te) for e = 1..3;  t = V & u
+// where Te = all-ones if bit e of the column code is set, B = ~T0 & (T1|T2|T3)
+// (so a zero column code gives u = 0).  Since t = V & M is a subset of V,
+// V & ~M = V ^ t and the update is V' = (V + t + c) | (V ^ t).
+#pragma once
+
+#include "carry_chain.cuh"
+#include "common.cuh"
+
+namespace ngia {
+
+// s[0..W) = a + b as one W-word number (W multiple of 4, carry in = cin != 0
+// when CIN).
+template <int W, bool CIN>
+__device__ __forceinline__ void add_words(uint32_t *s, const uint32_t *a,
+                                          const uint32_t *b, uint32_t cin) {
+  if constexpr (W == 4) {
+    if constexpr (CIN) add_chain4_cn(s, a, b, cin);
+    else add_chain4_zn(s, a, b);
+  } else if constexpr (W == 8) {
+    if constexpr (CIN) add_chain8_cn(s, a, b, cin);
+    else add_chain8_zn(s, a, b);
+  } else {
+    uint32_t c;
+    if constexpr (CIN) add_chain8_cc(s, a, b, cin, c);
+    else add_chain8_zc(s, a, b, c);
+    add_words<W - 8, true>(s + 8, a + 8, b + 8, c);
+  }
+}
+
+// Column-code masks of a target block, one column per step.  The four planes
+// are bit-reversed once per block so that column k's bits sit in bit 31 after
+// k left shifts; Te = arithmetic shift of that sign bit across the word.
+struct ColMask {
+  uint32_t T0, T1, T2, T3, B;
+};
+struct ColumnPlanes {
+  uint32_t r0, r1, r2, r3;
+  __device__ __forceinline__ explicit ColumnPlanes(const uint32_t *tb) {
+#ifdef __CUDA_ARCH__
+    r0 = __brev(__ldg(tb));
+    r1 = __brev(__ldg(tb + 1));
+    r2 = __brev(__ldg(tb + 2));
+    r3 = __brev(__ldg(tb + 3));
+#endif
+  }
+  // masks of the next column, then advance
+  __device__ __forceinline__ ColMask next() {
+    ColMask m;
+    m.T0 = (uint32_t)((int32_t)r0 >> 31);
+    m.T1 = (uint32_t)((int32_t)r1 >> 31);
+    m.T2 = (uint32_t)((int32_t)r2 >> 31);
+    m.T3 = (uint32_t)((int32_t)r3 >> 31);
+    m.B = ~m.T0 & (m.T1 | m.T2 | m.T3);
+    r0 <<= 1;
+    r1 <<= 1;
+    r2 <<= 1;
+    r3 <<= 1;
+    return m;
+  }
+};
+
+__device__ __forceinline__ uint32_t match_and(uint32_t v, uint32_t p0, uint32_t p1,
+                                              uint32_t p2, uint32_t p3,
+                                              const ColMask &c) {
+  uint32_t u = (p0 & c.T0) | (~p0 & c.B);
+  u &= ~(p1 ^ c.T1);
+  u &= ~(p2 ^ c.T2);
+  u &= ~(p3 ^ c.T3);
+  return v & u;
+}
+
+template <int W>
+__device__ __forceinline__ void window_step(uint32_t (&V)[W], const uint32_t (&P0)[W],
+                                            const uint32_t (&P1)[W],
+                                            const uint32_t (&P2)[W],
+                                            const uint32_t (&P3)[W],
+                                            const ColMask &c) {
+  uint32_t t[W], s[W];
+#pragma unroll
+  for (int m = 0; m < W; ++m) t[m] = match_and(V[m], P0[m], P1[m], P2[m], P3[m], c);
+  add_words<W, false>(s, V, t, 0);
+#pragma unroll
+  for (int m = 0; m < W; ++m) V[m] = s[m] | (V[m] ^ t[m]);
+}
+
+// LCS of the banded computation, window form; requires b.width <= W.
+template <int W>
+__device__ inline uint32_t lcs_window(const uint32_t *__restrict__ rep,
+                               const uint32_t *__restrict__ tar, const Band &b) {
+  uint32_t V[W], P0[W], P1[W], P2[W], P3[W];
+#pragma unroll
+  for (int m = 0; m < W; ++m) {
+    V[m] = kFull;
+    P0[m] = P1[m] = P2[m] = P3[m] = 0;
+  }
+  uint32_t lcs = 0, act = 0;  // act = row blocks loaded so far
+  for (uint32_t i = 0; i < b.nc; ++i) {
+    if (i > b.ls) {  // J0 advances: retire the bottom row block
+      lcs += __popc(~V[0]);
+#pragma unroll
+      for (int m = 0; m < W - 1; ++m) {
+        V[m] = V[m + 1];
+        P0[m] = P0[m + 1];
+        P1[m] = P1[m + 1];
+        P2[m] = P2[m + 1];
+        P3[m] = P3[m + 1];
+      }
+      V[W - 1] = kFull;
+      P0[W - 1] = P1[W - 1] = P2[W - 1] = P3[W - 1] = 0;
+    }
+    const uint32_t j0 = i > b.ls ? i - b.ls : 0;
+    const uint32_t j1 = (i + b.rs < b.nr) ? i + b.rs : b.nr;
+    for (; act < j1; ++act) {  // row blocks entering the band
+      const uint32_t *rb = rep + 1 + 4 * act;
+      const uint32_t q0 = __ldg(rb), q1 = __ldg(rb + 1), q2 = __ldg(rb + 2),
+                     q3 = __ldg(rb + 3);
+      const uint32_t slot = act - j0;
+#pragma unroll
+      for (int m = 0; m < W; ++m) {
+        if ((uint32_t)m == slot) {
+          P0[m] = q0;
+          P1[m] = q1;
+          P2[m] = q2;
+          P3[m] = q3;
+        }
+      }
+    }
+    ColumnPlanes col(tar + 1 + 4 * i);
+#pragma unroll 4
+    for (int k = 0; k < 32; ++k) window_step<W>(V, P0, P1, P2, P3, col.next());
+  }
+#pragma unroll
+  for (int m = 0; m < W; ++m) lcs += __popc(~V[m]);
+  return lcs;
+}
+
+// General form for any band width: per column block the live rows are
+// processed in chunks of 8 words held in `lines` (the row vector, one word per
+// row block), with the 32 column carries between chunks kept as one word
+// (bit k = carry of column k), like the reference's carry register.
+constexpr uint32_t kMaxRowBlocks = (NGIA_MAX_READ + 31) / 32;  // 2048
+
+__device__ inline uint32_t lcs_general(const uint32_t *__restrict__ rep,
+                                const uint32_t *__restrict__ tar, const Band &b,
+                                uint32_t *lines) {
+  for (uint32_t w = 0; w < b.nr; ++w) lines[w] = kFull;
+  for (uint32_t i = 0; i < b.nc; ++i) {
+    const uint32_t j0 = i > b.ls ? i - b.ls : 0;
+    const uint32_t j1 = (i + b.rs < b.nr) ? i + b.rs : b.nr;
+    const uint32_t *tb = tar + 1 + 4 * i;
+    uint32_t cin_word = 0;  // carries into the current chunk, bit k = column k
+    for (uint32_t j = j0; j < j1; j += 8) {
+      uint32_t V[8], P0[8], P1[8], P2[8], P3[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const uint32_t r = j + m;
+        if (r < j1) {
+          const uint32_t *rb = rep + 1 + 4 * r;
+          V[m] = lines[r];
+          P0[m] = __ldg(rb);
+          P1[m] = __ldg(rb + 1);
+          P2[m] = __ldg(rb + 2);
+          P3[m] = __ldg(rb + 3);
+        } else {
+          V[m] = kFull;
+          P0[m] = P1[m] = P2[m] = P3[m] = 0;
+        }
+      }
+      uint32_t cout_word = 0;
+      ColumnPlanes col(tb);
+#pragma unroll 4
+      for (int k = 0; k < 32; ++k) {
+        const ColMask c = col.next();
+        uint32_t t[8], s[8], co;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) t[m] = match_and(V[m], P0[m], P1[m], P2[m], P3[m], c);
+        add_chain8_cc(s, V, t, cin_word & 1u, co);
+        cin_word >>= 1;
+        cout_word |= co << k;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) V[m] = s[m] | (V[m] ^ t[m]);
+      }
+#pragma unroll
+      for (int m = 0; m < 8; ++m)
+        if (j + m < j1) lines[j + m] = V[m];
+      cin_word = cout_word;
+    }
+  }
+  uint32_t lcs = 0;
+  for (uint32_t w = 0; w < b.nr; ++w) lcs += __popc(~lines[w]);
+  return lcs;
+}
+
+// Window width classes of the batched aligner; class kGeneralClass uses
+// lcs_general.  Pairs failing the length filter get class kSkipClass.
+// Widths: 4, 8, 12, 16, 24, 32.
+constexpr int kNumWindowClasses = 6;
+constexpr int kGeneralClass = kNumWindowClasses;
+constexpr int kSkipClass = kNumWindowClasses + 1;
+constexpr int kNumClasses = kNumWindowClasses + 2;
+
+__host__ __device__ inline int class_width(int c) {
+  return c < 4 ? 4 * (c + 1) : (c == 4 ? 24 : 32);
+}
+
+__host__ __device__ inline int width_class(const Band &b) {
+  if (!b.pass) return kSkipClass;
+  const uint32_t w = b.width;
+  if (w <= 4) return 0;
+  if (w <= 8) return 1;
+  if (w <= 12) return 2;
+  if (w <= 16) return 3;
+  if (w <= 24) return 4;
+  if (w <= 32) return 5;
+  return kGeneralClass;
+}
+
+}  // namespace ngia

@@ -1,0 +1,70 @@
+// bucket.cu -- stage (b): band-key bucketing.
+//
+// Restates MakeDB::groupSignatures (src/makedb.hpp:289-364): for every band,
+// sort (signature, index) stably -- the reference's 4-pass LSD radix sort of
+// sig<<32|idx -- and link each entry to the previous entry of its signature
+// run:  rep[b][idx] = previous idx if the signatures are equal, else idx.
+// Equivalently rep[b][i] is the largest j < i with sig[b][j] == sig[b][i].
+//
+// Device form: all bands are sorted together as 64 segments by the segmented
+// radix sort (sort.cu), then one coalesced pass over the sorted runs writes
+// the predecessor links.
+#include "kernels.cuh"
+
+namespace ngia {
+
+__global__ void __launch_bounds__(256)
+rep_chain_kernel(const uint32_t *__restrict__ skeys, const uint32_t *__restrict__ svals,
+                 uint32_t n, uint32_t bands, uint32_t *__restrict__ rep) {
+  const size_t total = (size_t)n * bands;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const size_t band = e / n;
+    const uint32_t p = (uint32_t)(e - band * n);
+    const uint32_t idx = svals[e];
+    const uint32_t r = (p > 0 && skeys[e - 1] == skeys[e]) ? svals[e - 1] : idx;
+    rep[band * n + idx] = r;
+  }
+}
+
+size_t bucket_scratch_bytes(uint32_t n, uint32_t bands) {
+  return 2 * (size_t)n * bands * sizeof(uint32_t) + radix_sort_scratch_bytes(n, bands);
+}
+
+int bucket(const uint32_t *sigs, uint32_t n, uint32_t bands, uint32_t *rep,
+           void *scratch, cudaStream_t s) {
+  if (n == 0 || bands == 0) return NGIA_OK;
+  const size_t total = (size_t)n * bands;
+  uint32_t *sk = static_cast<uint32_t *>(scratch);
+  uint32_t *sv = sk + total;
+  NGIA_TRY(radix_sort_pairs(sigs, nullptr, sk, sv, n, bands, 0, 32, sv + total, s));
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const size_t want = ceil_div<size_t>(total, 256);
+  const size_t cap = (size_t)sms * 8;
+  rep_chain_kernel<<<(uint32_t)(want < cap ? want : cap), 256, 0, s>>>(sk, sv, n, bands, rep);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+}  // namespace ngia
+
+extern "C" int ngia_bucket(const uint32_t *d_sigs, uint32_t n, uint32_t bands,
+                           uint32_t *d_rep, void *stream) {
+  if (bands < 1 || bands > NGIA_BANDS) return NGIA_ERR_ARG;
+  if (n == 0) return NGIA_OK;
+  if (!d_sigs || !d_rep) return NGIA_ERR_ARG;
+  cudaStream_t s = ngia::as_stream(stream);
+  void *scratch = nullptr;
+  const size_t bytes = ngia::bucket_scratch_bytes(n, bands);
+  cudaError_t e = cudaMallocAsync(&scratch, bytes, s);
+  if (e != cudaSuccess) {
+    ngia::cuda_fail(e);
+    return NGIA_ERR_NOMEM;
+  }
+  int st = ngia::bucket(d_sigs, n, bands, d_rep, scratch, s);
+  e = cudaFreeAsync(scratch, s);
+  if (st == NGIA_OK && e != cudaSuccess) st = ngia::cuda_fail(e);
+  return st;
+}

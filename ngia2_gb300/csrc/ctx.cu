@@ -1,0 +1,390 @@
+// ctx.cu -- the resident-database context (ngia_ctx), the batched graph build
+// and fast-mode driver, status handling, and the edge sort+unique entry point.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "align.cuh"
+#include "host.hpp"
+#include "kernels.cuh"
+
+namespace ngia {
+
+static thread_local int g_last_cuda = 0;
+static int g_round_mode = NGIA_ROUND_FMA;
+
+int cuda_fail(cudaError_t e) {
+  g_last_cuda = (int)e;
+  (void)cudaGetLastError();  // clear a sticky-free error so later calls can run
+  return e == cudaErrorMemoryAllocation ? NGIA_ERR_NOMEM : NGIA_ERR_CUDA;
+}
+
+int round_mode() { return g_round_mode; }
+
+static std::atomic<unsigned long long> g_launches(0);
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// Grow-only device buffer.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t want) {
+    if (want <= bytes) return NGIA_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (want == 0) return NGIA_OK;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      cuda_fail(e);
+      return NGIA_ERR_NOMEM;
+    }
+    bytes = want;
+    return NGIA_OK;
+  }
+  template <typename T>
+  T *as() const { return static_cast<T *>(p); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+}  // namespace ngia
+
+struct ngia_ctx {
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaEvent_t ev[8] = {};
+  // resident database
+  uint32_t n = 0;
+  uint64_t packed_words = 0;
+  uint32_t rep_bands = 0;
+  ngia::DevBuf packed, offs, lens, rep, sigs;
+  // graph build work
+  ngia::DevBuf ucount, uoff, counters, pairs, scores, cls, cls_sorted, order, sort_tmp,
+      emit_tmp, edges, scan_tmp, jobs;
+  uint64_t n_edges = 0;
+};
+
+namespace ngia {
+
+struct Counters {  // device-side counters of one graph build
+  unsigned long long cand_total;
+  unsigned long long cells;
+  uint64_t unique_total;
+  unsigned int class_count[kNumClasses];
+  uint32_t fast_count;
+};
+
+static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.0;
+  return ms;
+}
+
+int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
+  if (c->n == 0) return NGIA_ERR_STATE;
+  if (bands < 1 || bands > (uint32_t)kBands) return NGIA_ERR_ARG;
+  cudaStream_t s = c->stream;
+  NGIA_TRY(c->sigs.reserve((size_t)kBands * c->n * 4));
+  NGIA_TRY(c->rep.reserve((size_t)kBands * c->n * 4));
+  NGIA_TRY(c->sort_tmp.reserve(bucket_scratch_bytes(c->n, bands)));
+  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  NGIA_TRY(launch_sketch(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
+                         c->sigs.as<uint32_t>(), s));
+  NGIA_CUDA(cudaEventRecord(c->ev[1], s));
+  NGIA_TRY(bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(),
+                  c->sort_tmp.p, s));
+  NGIA_CUDA(cudaEventRecord(c->ev[2], s));
+  c->rep_bands = bands;
+  if (st) {
+    NGIA_CUDA(cudaEventSynchronize(c->ev[2]));
+    st->ms_sketch = ev_ms(c->ev[0], c->ev[1]);
+    st->ms_bucket = ev_ms(c->ev[1], c->ev[2]);
+  }
+  return NGIA_OK;
+}
+
+int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_n_edges,
+                    ngia_stats *st) {
+  if (c->n == 0 || c->rep_bands == 0) return NGIA_ERR_STATE;
+  if (identity < 1 || identity > 99) return NGIA_ERR_ARG;
+  if (bands < 1 || bands > c->rep_bands) return NGIA_ERR_ARG;
+  cudaStream_t s = c->stream;
+  const uint32_t n = c->n;
+  const uint32_t *rep = c->rep.as<uint32_t>();
+  const uint32_t *lens = c->lens.as<uint32_t>();
+  NGIA_TRY(c->counters.reserve(sizeof(Counters)));
+  NGIA_TRY(c->ucount.reserve((size_t)n * 4));
+  NGIA_TRY(c->uoff.reserve((size_t)n * 8));
+  Counters *dc = c->counters.as<Counters>();
+  NGIA_CUDA(cudaMemsetAsync(dc, 0, sizeof(Counters), s));
+  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  // 1. candidates: per-target unique counts, offsets, total
+  NGIA_TRY(collect_count(rep, lens, n, bands, identity, c->ucount.as<uint32_t>(),
+                         &dc->cand_total, s));
+  NGIA_TRY(c->scan_tmp.reserve(scan_scratch_bytes(n)));
+  NGIA_TRY(exclusive_scan_u64(c->ucount.as<uint32_t>(), c->uoff.as<uint64_t>(), n,
+                              &dc->unique_total, c->scan_tmp.as<uint64_t>(), s));
+  Counters hc;
+  NGIA_CUDA(cudaMemcpyAsync(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  const uint64_t total = hc.unique_total;
+  if (total > 0xFFFFFFFFull) return NGIA_ERR_NOMEM;  // beyond one launch's index range
+  const uint32_t m = (uint32_t)total;
+  NGIA_TRY(c->pairs.reserve((size_t)(m ? m : 1) * 8));
+  NGIA_TRY(c->scores.reserve((size_t)(m ? m : 1) * 4));
+  NGIA_TRY(c->cls.reserve((size_t)(m ? m : 1) * 4));
+  NGIA_TRY(c->cls_sorted.reserve((size_t)(m ? m : 1) * 4));
+  NGIA_TRY(c->order.reserve((size_t)(m ? m : 1) * 4));
+  NGIA_TRY(c->sort_tmp.reserve(radix_sort_scratch_bytes(m, 1)));
+  uint2 *pairs = c->pairs.as<uint2>();
+  uint32_t *scores = c->scores.as<uint32_t>();
+  NGIA_TRY(collect_write(rep, lens, n, bands, identity, c->uoff.as<uint64_t>(), pairs, s));
+  // 2. width classes, stably ordered (target order kept inside a class)
+  NGIA_TRY(classify(lens, pairs, m, identity, c->cls.as<uint32_t>(), dc->class_count,
+                    &dc->cells, s));
+  NGIA_TRY(radix_sort_pairs(c->cls.as<uint32_t>(), nullptr, c->cls_sorted.as<uint32_t>(),
+                            c->order.as<uint32_t>(), m, 1, 0, 8, c->sort_tmp.p, s));
+  NGIA_CUDA(cudaMemsetAsync(scores, 0, (size_t)(m ? m : 1) * 4, s));
+  NGIA_CUDA(cudaMemcpyAsync(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaEventRecord(c->ev[1], s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  // 3. align, one launch per width class, widest first
+  uint32_t begin[kNumClasses + 1];
+  begin[0] = 0;
+  for (int k = 0; k < kNumClasses; ++k) begin[k + 1] = begin[k] + hc.class_count[k];
+  const int launch_order[] = {kGeneralClass, 5, 4, 3, 2, 1, 0};
+  for (int cl : launch_order)
+    NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), pairs,
+                                c->order.as<uint32_t>(), begin[cl], begin[cl + 1], scores,
+                                identity, s));
+  NGIA_CUDA(cudaEventRecord(c->ev[2], s));
+  // 4. emit: compact hits, sort by (rep, tar)
+  NGIA_TRY(c->emit_tmp.reserve(emit_scratch_bytes(m, n)));
+  NGIA_TRY(c->edges.reserve((size_t)(m ? m : 1) * sizeof(ngia_edge)));
+  uint64_t ne = 0;
+  NGIA_TRY(emit_sorted(pairs, scores, m, n, c->edges.as<ngia_edge>(), &ne, c->emit_tmp.p, s));
+  NGIA_CUDA(cudaEventRecord(c->ev[3], s));
+  NGIA_CUDA(cudaEventSynchronize(c->ev[3]));
+  c->n_edges = ne;
+  if (h_n_edges) *h_n_edges = ne;
+  if (st) {
+    st->candidate_pairs = hc.cand_total;
+    st->unique_pairs = total;
+    st->aligned_cells = hc.cells;
+    st->edges = ne;
+    st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
+    st->ms_align = ev_ms(c->ev[1], c->ev[2]);
+    st->ms_emit = ev_ms(c->ev[2], c->ev[3]);
+  }
+  return NGIA_OK;
+}
+
+int ctx_fast_cluster(ngia_ctx *c, uint32_t identity, uint32_t bands, uint32_t *h_cluster,
+                     ngia_stats *st) {
+  if (c->n == 0 || c->rep_bands == 0) return NGIA_ERR_STATE;
+  if (identity < 1 || identity > 99) return NGIA_ERR_ARG;
+  if (bands < 1 || bands > c->rep_bands) return NGIA_ERR_ARG;
+  cudaStream_t s = c->stream;
+  const uint32_t n = c->n;
+  NGIA_TRY(c->counters.reserve(sizeof(Counters)));
+  NGIA_TRY(c->jobs.reserve((size_t)n * 12));
+  NGIA_TRY(c->ucount.reserve((size_t)n * 4));  // parent pointers
+  uint32_t *parent = c->ucount.as<uint32_t>();
+  Counters *dc = c->counters.as<Counters>();
+  NGIA_CUDA(cudaMemsetAsync(parent, 0xFF, (size_t)n * 4, s));
+  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  for (uint32_t b = 0; b < bands; ++b)
+    NGIA_TRY(fast_round(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(),
+                        c->rep.as<uint32_t>() + (size_t)b * n, parent, n, identity,
+                        c->jobs.as<uint32_t>(), &dc->fast_count, s));
+  NGIA_CUDA(cudaEventRecord(c->ev[1], s));
+  std::vector<uint32_t> par(n);
+  NGIA_CUDA(cudaMemcpyAsync(par.data(), parent, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  // Root resolution (src/fastClustering.hpp:338-347): parents precede children.
+  for (uint32_t i = 0; i < n; ++i)
+    h_cluster[i] = par[i] == kFull ? i : h_cluster[par[i]];
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    st->ms_align = ev_ms(c->ev[0], c->ev[1]);
+  }
+  return NGIA_OK;
+}
+
+int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64_t *h_offs,
+             const uint32_t *h_lens, uint32_t n, const uint32_t *h_rep, uint32_t bands) {
+  if (n == 0 || !h_packed || !h_offs || !h_lens) return NGIA_ERR_ARG;
+  if (h_rep && (bands < 1 || bands > (uint32_t)kBands)) return NGIA_ERR_ARG;
+  cudaStream_t s = c->stream;
+  NGIA_TRY(c->packed.reserve(words * 4));
+  NGIA_TRY(c->offs.reserve((size_t)n * 8));
+  NGIA_TRY(c->lens.reserve((size_t)n * 4));
+  NGIA_CUDA(cudaMemcpyAsync(c->packed.p, h_packed, words * 4, cudaMemcpyHostToDevice, s));
+  NGIA_CUDA(cudaMemcpyAsync(c->offs.p, h_offs, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+  NGIA_CUDA(cudaMemcpyAsync(c->lens.p, h_lens, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  c->n = n;
+  c->packed_words = words;
+  c->rep_bands = 0;
+  c->n_edges = 0;
+  if (h_rep) {
+    NGIA_TRY(c->rep.reserve((size_t)kBands * n * 4));
+    NGIA_CUDA(cudaMemcpyAsync(c->rep.p, h_rep, (size_t)bands * n * 4,
+                              cudaMemcpyHostToDevice, s));
+    c->rep_bands = bands;
+  }
+  return NGIA_OK;
+}
+
+}  // namespace ngia
+
+// ---- C ABI --------------------------------------------------------------------------
+extern "C" {
+
+const char *ngia_status_string(int status) {
+  switch (status) {
+    case NGIA_OK: return "ok";
+    case NGIA_ERR_ARG: return "invalid argument";
+    case NGIA_ERR_CUDA: return "CUDA error";
+    case NGIA_ERR_NOMEM: return "out of memory";
+    case NGIA_ERR_IO: return "I/O error";
+    case NGIA_ERR_FORMAT: return "malformed input";
+    case NGIA_ERR_STATE: return "call out of order";
+    default: return "unknown status";
+  }
+}
+
+int ngia_last_cuda_error(void) { return ngia::g_last_cuda; }
+
+unsigned long long ngia_kernel_launches(void) { return ngia::g_launches.load(); }
+
+const char *ngia_version(void) { return "ngia-gb300 0.1 (sm_103a)"; }
+
+int ngia_set_round_mode(int mode) {
+  const int old = ngia::g_round_mode;
+  if (mode == NGIA_ROUND_SPLIT || mode == NGIA_ROUND_FMA) ngia::g_round_mode = mode;
+  return old;
+}
+
+int ngia_ctx_create(ngia_ctx **out, void *stream) {
+  if (!out) return NGIA_ERR_ARG;
+  *out = nullptr;
+  ngia_ctx *c = new (std::nothrow) ngia_ctx();
+  if (!c) return NGIA_ERR_NOMEM;
+  cudaError_t e = cudaSuccess;
+  if (stream) {
+    c->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    c->own_stream = (e == cudaSuccess);
+  }
+  for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+  if (e != cudaSuccess) {
+    ngia_ctx_destroy(c);
+    return ngia::cuda_fail(e);
+  }
+  *out = c;
+  return NGIA_OK;
+}
+
+void ngia_ctx_destroy(ngia_ctx *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  ngia::DevBuf *bufs[] = {&c->packed, &c->offs,  &c->lens,       &c->rep,    &c->sigs,
+                          &c->ucount, &c->uoff,  &c->counters,   &c->pairs,  &c->scores,
+                          &c->cls,    &c->cls_sorted, &c->order, &c->sort_tmp,
+                          &c->emit_tmp, &c->edges, &c->scan_tmp, &c->jobs};
+  for (ngia::DevBuf *b : bufs) b->release();
+  for (int k = 0; k < 8; ++k)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int ngia_ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t packed_words,
+                  const uint64_t *h_rec_offsets, const uint32_t *h_lens, uint32_t n,
+                  const uint32_t *h_rep, uint32_t bands) {
+  if (!c) return NGIA_ERR_ARG;
+  NGIA_TRY(ngia::ctx_load(c, h_packed, packed_words, h_rec_offsets, h_lens, n, h_rep, bands));
+  NGIA_CUDA(cudaStreamSynchronize(c->stream));
+  return NGIA_OK;
+}
+
+int ngia_ctx_load_packed_file(ngia_ctx *c, const char *path, uint32_t bands,
+                              int use_file_rep_rows) {
+  if (!c || !path) return NGIA_ERR_ARG;
+  if (bands < 1 || bands > NGIA_BANDS) return NGIA_ERR_ARG;
+  ngia::PackedDb db;
+  NGIA_TRY(ngia::read_packed(path, use_file_rep_rows ? bands : 0, db));
+  NGIA_TRY(ngia::ctx_load(c, db.packed.data(), db.packed.size(), db.offsets.data(),
+                          db.lens.data(), db.n, use_file_rep_rows ? db.rep.data() : nullptr,
+                          bands));
+  NGIA_CUDA(cudaStreamSynchronize(c->stream));
+  if (!use_file_rep_rows) NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, nullptr));
+  return NGIA_OK;
+}
+
+int ngia_ctx_sketch_bucket(ngia_ctx *c, uint32_t bands) {
+  if (!c) return NGIA_ERR_ARG;
+  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, nullptr));
+  NGIA_CUDA(cudaStreamSynchronize(c->stream));
+  return NGIA_OK;
+}
+
+int ngia_ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands,
+                         uint64_t *h_n_edges, ngia_stats *stats) {
+  if (!c) return NGIA_ERR_ARG;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  return ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats);
+}
+
+int ngia_ctx_group_align(ngia_ctx *c, uint32_t identity, uint32_t bands,
+                         uint64_t *h_n_edges, ngia_stats *stats) {
+  if (!c) return NGIA_ERR_ARG;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats));
+  return ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats);
+}
+
+int ngia_ctx_edges(ngia_ctx *c, ngia_edge *h_edges, uint64_t cap) {
+  if (!c || (!h_edges && cap)) return NGIA_ERR_ARG;
+  const uint64_t m = c->n_edges < cap ? c->n_edges : cap;
+  if (m == 0) return NGIA_OK;
+  NGIA_CUDA(cudaMemcpyAsync(h_edges, c->edges.p, m * sizeof(ngia_edge),
+                            cudaMemcpyDeviceToHost, c->stream));
+  NGIA_CUDA(cudaStreamSynchronize(c->stream));
+  return NGIA_OK;
+}
+
+int ngia_ctx_fast_cluster(ngia_ctx *c, uint32_t identity, uint32_t bands,
+                          uint32_t *h_cluster, ngia_stats *stats) {
+  if (!c || !h_cluster) return NGIA_ERR_ARG;
+  return ngia::ctx_fast_cluster(c, identity, bands, h_cluster, stats);
+}
+
+int ngia_ctx_rep_rows(ngia_ctx *c, uint32_t *h_rep, uint32_t bands) {
+  if (!c || !h_rep) return NGIA_ERR_ARG;
+  if (bands < 1 || bands > c->rep_bands) return NGIA_ERR_ARG;
+  NGIA_CUDA(cudaMemcpyAsync(h_rep, c->rep.p, (size_t)bands * c->n * 4,
+                            cudaMemcpyDeviceToHost, c->stream));
+  NGIA_CUDA(cudaStreamSynchronize(c->stream));
+  return NGIA_OK;
+}
+
+int ngia_ctx_run_host(ngia_ctx *c, const uint32_t *h_packed, uint64_t packed_words,
+                      const uint64_t *h_rec_offsets, const uint32_t *h_lens, uint32_t n,
+                      uint32_t identity, uint32_t bands, ngia_edge *h_edges, uint64_t cap,
+                      uint64_t *h_n_edges, ngia_stats *stats) {
+  if (!c || !h_n_edges) return NGIA_ERR_ARG;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  NGIA_TRY(ngia::ctx_load(c, h_packed, packed_words, h_rec_offsets, h_lens, n, nullptr, bands));
+  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats));
+  NGIA_TRY(ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats));
+  return ngia_ctx_edges(c, h_edges, cap);
+}
+
+}  // extern "C"

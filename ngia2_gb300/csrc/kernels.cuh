@@ -1,0 +1,59 @@
+// kernels.cuh -- launchers shared between the translation units of libngia
+// (internal header).
+#pragma once
+
+#include "common.cuh"
+
+namespace ngia {
+
+// sketch.cu
+int launch_sketch(const uint32_t *packed, const uint64_t *offs, uint32_t n,
+                  uint32_t *sigs, cudaStream_t s);
+
+// sort.cu
+size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs);
+int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
+                     uint32_t *keys_out, uint32_t *vals_out, uint32_t seg_len,
+                     uint32_t segs, int begin_bit, int end_bit, void *scratch,
+                     cudaStream_t s);
+size_t scan_scratch_bytes(uint32_t n);
+int exclusive_scan_u64(const uint32_t *in, uint64_t *out, uint32_t n,
+                       uint64_t *d_total, void *scratch, cudaStream_t s);
+
+// bucket.cu
+size_t bucket_scratch_bytes(uint32_t n, uint32_t bands);
+int bucket(const uint32_t *sigs, uint32_t n, uint32_t bands, uint32_t *rep,
+           void *scratch, cudaStream_t s);
+
+// align.cu
+int launch_align_jobs(const uint32_t *packed, const uint64_t *offs, uint32_t *jobs,
+                      uint32_t count, uint32_t identity, cudaStream_t s);
+int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
+                                uint32_t *jobs, const uint32_t *d_count,
+                                uint32_t max_count, uint32_t identity,
+                                cudaStream_t s);
+int launch_align_class(int cls, const uint32_t *packed, const uint64_t *offs,
+                       const uint2 *pairs, const uint32_t *order, uint32_t begin,
+                       uint32_t end, uint32_t *scores, uint32_t identity,
+                       cudaStream_t s);
+
+// pairs.cu
+int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
+                  uint32_t identity, uint32_t *ucount, unsigned long long *cand_total,
+                  cudaStream_t s);
+int collect_write(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
+                  uint32_t identity, const uint64_t *offsets, uint2 *pairs,
+                  cudaStream_t s);
+int classify(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t identity,
+             uint32_t *cls, unsigned int *class_count, unsigned long long *cells,
+             cudaStream_t s);
+int bits_for(uint32_t max_value);
+size_t emit_scratch_bytes(uint32_t count, uint32_t n_nodes);
+int emit_sorted(const uint2 *pairs, const uint32_t *scores, uint32_t count,
+                uint32_t n_nodes, ngia_edge *out, uint64_t *h_m, void *scratch,
+                cudaStream_t s);
+int fast_round(const uint32_t *packed, const uint64_t *offs, const uint32_t *rep_row,
+               uint32_t *parent, uint32_t n, uint32_t identity, uint32_t *jobs,
+               uint32_t *d_count, cudaStream_t s);
+
+}  // namespace ngia

@@ -1,0 +1,371 @@
+// pairs.cu -- candidate collection, width-class binning and edge emission.
+//
+// Candidates (src/buildGraph.hpp:262-300): target i of band b is a job with
+// rep r = rep[b][i] when r != i and len[i] >= len[r] * t.  The reference
+// aligns every band's jobs separately, so a pair found in k bands is aligned k
+// times and the duplicate edges are removed after sorting
+// (src/buildGraph.hpp:357-358).  The score of a pair does not depend on the
+// band, so here the candidates of all bands are deduplicated per target
+// before alignment: each distinct (rep, tar) pair is aligned once, and the
+// emitted edge set is the reference's sorted unique edge list.
+//
+// Layout: a block loads the rep rows of 32 consecutive targets for all bands
+// (coalesced along i), then each warp takes one target: lane l holds bands l
+// and l+32; equal reps are found with match_any, and the first band of every
+// distinct rep keeps it.  Pairs come out grouped by target in index order.
+#include "align.cuh"
+#include "kernels.cuh"
+
+namespace ngia {
+
+constexpr uint32_t kTargetsPerBlock = 32;
+constexpr uint32_t kPairThreads = 256;
+
+struct TargetScan {
+  uint32_t first0, first1;  // ballots of first occurrences (slot 0 / slot 1)
+  uint32_t cand;            // candidates including duplicates
+  uint32_t v0, v1;
+};
+
+__device__ __forceinline__ TargetScan scan_target(const uint32_t *tile_rep /*[64][32]*/,
+                                                  uint32_t col, uint32_t i,
+                                                  const uint32_t *__restrict__ lens,
+                                                  uint32_t bands, float t,
+                                                  uint32_t *warp_vals) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const float li = __uint2float_rn(__ldg(lens + i));
+  TargetScan ts;
+  ts.v0 = lane < bands ? tile_rep[lane * kTargetsPerBlock + col] : i;
+  ts.v1 = lane + 32 < bands ? tile_rep[(lane + 32) * kTargetsPerBlock + col] : i;
+  const bool ok0 = ts.v0 != i && li >= __fmul_rn(__uint2float_rn(__ldg(lens + ts.v0)), t);
+  const bool ok1 = ts.v1 != i && li >= __fmul_rn(__uint2float_rn(__ldg(lens + ts.v1)), t);
+  const uint32_t b0 = __ballot_sync(kFull, ok0), b1 = __ballot_sync(kFull, ok1);
+  ts.cand = __popc(b0) + __popc(b1);
+  const uint32_t tag0 = ok0 ? ts.v0 : (0x80000000u | lane);
+  const uint32_t p0 = __match_any_sync(kFull, tag0);
+  const bool f0 = ok0 && (p0 & lt_mask) == 0;
+  bool f1 = false;
+  if (b1) {
+    const uint32_t tag1 = ok1 ? ts.v1 : (0xC0000000u | lane);
+    const uint32_t p1 = __match_any_sync(kFull, tag1);
+    f1 = ok1 && (p1 & lt_mask) == 0;
+    warp_vals[lane] = tag0;
+    __syncwarp();
+    if (f1) {
+      for (uint32_t l = 0; l < 32; ++l)
+        if (warp_vals[l] == ts.v1) f1 = false;
+    }
+    __syncwarp();
+  }
+  ts.first0 = __ballot_sync(kFull, f0);
+  ts.first1 = __ballot_sync(kFull, f1);
+  return ts;
+}
+
+// mode 0: count unique pairs per target; mode 1: write them at offsets[i].
+template <int MODE>
+__global__ void __launch_bounds__(kPairThreads)
+collect_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict__ lens,
+               uint32_t n, uint32_t bands, float t, uint32_t *__restrict__ ucount,
+               unsigned long long *__restrict__ cand_total,
+               const uint64_t *__restrict__ offsets, uint2 *__restrict__ pairs) {
+  __shared__ uint32_t tile[kBands * kTargetsPerBlock];
+  __shared__ uint32_t vals[kPairThreads / 32][32];
+  const uint32_t i0 = blockIdx.x * kTargetsPerBlock;
+  for (uint32_t e = threadIdx.x; e < bands * kTargetsPerBlock; e += kPairThreads) {
+    const uint32_t b = e / kTargetsPerBlock, c = e % kTargetsPerBlock;
+    tile[e] = (i0 + c < n) ? rep[(size_t)b * n + i0 + c] : 0u;
+  }
+  __syncthreads();
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  uint32_t cand_sum = 0;
+  for (uint32_t c = warp; c < kTargetsPerBlock; c += kPairThreads / 32) {
+    const uint32_t i = i0 + c;
+    if (i >= n) break;
+    const TargetScan ts = scan_target(tile, c, i, lens, bands, t, vals[warp]);
+    cand_sum += ts.cand;
+    if (MODE == 0) {
+      if (lane == 0) ucount[i] = __popc(ts.first0) + __popc(ts.first1);
+    } else {
+      const uint32_t lt_mask = (1u << lane) - 1u;
+      const uint64_t base = offsets[i];
+      if (ts.first0 >> lane & 1u)
+        pairs[base + __popc(ts.first0 & lt_mask)] = make_uint2(ts.v0, i);
+      if (ts.first1 >> lane & 1u)
+        pairs[base + __popc(ts.first0) + __popc(ts.first1 & lt_mask)] = make_uint2(ts.v1, i);
+    }
+  }
+  if (MODE == 0 && lane == 0 && cand_sum) atomicAdd(cand_total, (unsigned long long)cand_sum);
+}
+
+int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
+                  uint32_t identity, uint32_t *ucount, unsigned long long *cand_total,
+                  cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  collect_kernel<0><<<ceil_div(n, kTargetsPerBlock), kPairThreads, 0, s>>>(
+      rep, lens, n, bands, identity_threshold(identity), ucount, cand_total, nullptr,
+      nullptr);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+int collect_write(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
+                  uint32_t identity, const uint64_t *offsets, uint2 *pairs,
+                  cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  collect_kernel<1><<<ceil_div(n, kTargetsPerBlock), kPairThreads, 0, s>>>(
+      rep, lens, n, bands, identity_threshold(identity), nullptr, nullptr, offsets,
+      pairs);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+// ---- width classes ------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pairs,
+                uint64_t count, float t, int fma_mode, uint32_t *__restrict__ cls,
+                unsigned int *__restrict__ class_count,
+                unsigned long long *__restrict__ cells) {
+  __shared__ unsigned int sc[kNumClasses];
+  __shared__ unsigned long long scells;
+  if (threadIdx.x < kNumClasses) sc[threadIdx.x] = 0;
+  if (threadIdx.x == 0) scells = 0;
+  __syncthreads();
+  unsigned long long my_cells = 0;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
+       p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint2 pr = pairs[p];
+    const Band b = make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode);
+    const int c = width_class(b);
+    cls[p] = (uint32_t)c;
+    atomicAdd(&sc[c], 1u);
+    my_cells += band_blocks(b);
+  }
+  atomicAdd(&scells, my_cells);
+  __syncthreads();
+  if (threadIdx.x < kNumClasses && sc[threadIdx.x]) atomicAdd(&class_count[threadIdx.x], sc[threadIdx.x]);
+  if (threadIdx.x == 0 && scells) atomicAdd(cells, scells * 1024ull);
+}
+
+int classify(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t identity,
+             uint32_t *cls, unsigned int *class_count, unsigned long long *cells,
+             cudaStream_t s) {
+  if (count == 0) return NGIA_OK;
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t want = ceil_div(count, 256u), cap = (uint32_t)sms * 8;
+  classify_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
+      lens, pairs, count, identity_threshold(identity), round_mode(), cls, class_count,
+      cells);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+// ---- emission -----------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+positive_flags_kernel(const uint32_t *__restrict__ scores, uint32_t stride, uint32_t count,
+                      uint32_t *__restrict__ flags) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < count) flags[p] = scores[(size_t)p * stride] > 0 ? 1u : 0u;
+}
+
+// Pairs with score > 0, compacted in pair order into (rep keys, tar, score).
+__global__ void __launch_bounds__(256)
+compact_pairs_kernel(const uint2 *__restrict__ pairs, const uint32_t *__restrict__ scores,
+                     uint32_t count, const uint64_t *__restrict__ off,
+                     uint32_t *__restrict__ erep, uint32_t *__restrict__ etar,
+                     uint32_t *__restrict__ escore) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= count) return;
+  const uint32_t sc = scores[p];
+  if (sc == 0) return;
+  const uint64_t e = off[p];
+  const uint2 pr = pairs[p];
+  erep[e] = pr.x;
+  etar[e] = pr.y;
+  escore[e] = sc;
+}
+
+__global__ void __launch_bounds__(256)
+gather_edges_kernel(const uint32_t *__restrict__ srep, const uint32_t *__restrict__ sidx,
+                    const uint32_t *__restrict__ etar, const uint32_t *__restrict__ escore,
+                    uint32_t m, ngia_edge *__restrict__ out) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  const uint32_t e = sidx[k];
+  ngia_edge ed;
+  ed.rep = (int32_t)srep[k];
+  ed.tar = (int32_t)etar[e];
+  ed.weight = __fdiv_rn(__uint2float_rn(escore[e]), 100.0f);
+  out[k] = ed;
+}
+
+// Job triples with score > 0 -> edges in job order.
+__global__ void __launch_bounds__(256)
+jobs_to_edges_kernel(const uint32_t *__restrict__ jobs, uint32_t count,
+                     const uint64_t *__restrict__ off, ngia_edge *__restrict__ out) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= count) return;
+  const uint32_t sc = jobs[3 * (size_t)j + 2];
+  if (sc == 0) return;
+  ngia_edge ed;
+  ed.rep = (int32_t)jobs[3 * (size_t)j];
+  ed.tar = (int32_t)jobs[3 * (size_t)j + 1];
+  ed.weight = __fdiv_rn(__uint2float_rn(sc), 100.0f);
+  out[off[j]] = ed;
+}
+
+__global__ void store_u32_from_u64_kernel(const uint64_t *src, uint32_t *dst) { *dst = (uint32_t)*src; }
+
+int bits_for(uint32_t max_value) {
+  int b = 0;
+  while (b < 32 && (max_value >> b) != 0) ++b;
+  return b;
+}
+
+size_t emit_scratch_bytes(uint32_t count, uint32_t n_nodes) {
+  (void)n_nodes;
+  const size_t c = count ? count : 1;
+  // flags + offsets + 3 compacted arrays + 2 sorted arrays + sort scratch + scan
+  return c * 4 + c * 8 + 3 * c * 4 + 2 * c * 4 + radix_sort_scratch_bytes(count, 1) +
+         scan_scratch_bytes(count) + 64;
+}
+
+// Pairs (target order) with scores -> edges sorted by (rep, tar).  Sorting the
+// target-ordered list stably by rep gives (rep, tar) order.  *h_m = edges.
+int emit_sorted(const uint2 *pairs, const uint32_t *scores, uint32_t count,
+                uint32_t n_nodes, ngia_edge *out, uint64_t *h_m, void *scratch,
+                cudaStream_t s) {
+  *h_m = 0;
+  if (count == 0) return NGIA_OK;
+  char *w = static_cast<char *>(scratch);
+  uint32_t *flags = reinterpret_cast<uint32_t *>(w);
+  w += (size_t)count * 4;
+  uint64_t *off = reinterpret_cast<uint64_t *>((reinterpret_cast<uintptr_t>(w) + 15) & ~uintptr_t(15));
+  w = reinterpret_cast<char *>(off + count);
+  uint32_t *erep = reinterpret_cast<uint32_t *>(w);
+  uint32_t *etar = erep + count;
+  uint32_t *escore = etar + count;
+  uint32_t *srep = escore + count;
+  uint32_t *sidx = srep + count;
+  char *sort_scratch = reinterpret_cast<char *>(sidx + count);
+  uint64_t *scan_tmp = reinterpret_cast<uint64_t *>(
+      (reinterpret_cast<uintptr_t>(sort_scratch + radix_sort_scratch_bytes(count, 1)) + 15) &
+      ~uintptr_t(15));
+  uint64_t *d_total = scan_tmp + ceil_div<size_t>(count, 2048) + 1;
+  const uint32_t blocks = ceil_div(count, 256u);
+  positive_flags_kernel<<<blocks, 256, 0, s>>>(scores, 1, count, flags);
+  NGIA_LAUNCHED();
+  NGIA_TRY(exclusive_scan_u64(flags, off, count, d_total, scan_tmp, s));
+  compact_pairs_kernel<<<blocks, 256, 0, s>>>(pairs, scores, count, off, erep, etar, escore);
+  NGIA_LAUNCHED();
+  uint64_t m = 0;
+  NGIA_CUDA(cudaMemcpyAsync(&m, d_total, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  *h_m = m;
+  if (m == 0) return NGIA_OK;
+  const int bits = bits_for(n_nodes ? n_nodes - 1 : 0);
+  NGIA_TRY(radix_sort_pairs(erep, nullptr, srep, sidx, (uint32_t)m, 1, 0,
+                            bits > 0 ? bits : 8, sort_scratch, s));
+  gather_edges_kernel<<<ceil_div((uint32_t)m, 256u), 256, 0, s>>>(srep, sidx, etar, escore,
+                                                                  (uint32_t)m, out);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+// ---- fast mode ------------------------------------------------------------------------
+// Jobs of one band (src/fastClustering.hpp:256-258): rep[i] != i and i not
+// yet assigned.  The order of jobs inside a band does not affect the result
+// (each target appears once per band), so they are appended with one atomic
+// per warp.
+__global__ void __launch_bounds__(256)
+fast_jobs_kernel(const uint32_t *__restrict__ rep_row, const uint32_t *__restrict__ parent,
+                 uint32_t n, uint32_t *__restrict__ jobs, uint32_t *__restrict__ d_count) {
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t r = i < n ? rep_row[i] : 0u;
+    const bool job = i < n && r != i && parent[i] == kFull;
+    const uint32_t bal = __ballot_sync(kFull, job);
+    uint32_t slot = 0;
+    if (lane == 0 && bal) slot = atomicAdd(d_count, (uint32_t)__popc(bal));
+    slot = __shfl_sync(kFull, slot, 0) + __popc(bal & ((1u << lane) - 1u));
+    if (job) {
+      jobs[3 * (size_t)slot] = r;
+      jobs[3 * (size_t)slot + 1] = i;
+      jobs[3 * (size_t)slot + 2] = 0;
+    }
+  }
+}
+
+// A hit assigns the target to its rep (src/fastClustering.hpp:330-334).
+__global__ void __launch_bounds__(256)
+fast_assign_kernel(const uint32_t *__restrict__ jobs, const uint32_t *__restrict__ d_count,
+                   uint32_t *__restrict__ parent) {
+  const uint32_t count = *d_count;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count;
+       j += gridDim.x * blockDim.x)
+    if (jobs[3 * (size_t)j + 2] > 0) parent[jobs[3 * (size_t)j + 1]] = jobs[3 * (size_t)j];
+}
+
+int fast_round(const uint32_t *packed, const uint64_t *offs, const uint32_t *rep_row,
+               uint32_t *parent, uint32_t n, uint32_t identity, uint32_t *jobs,
+               uint32_t *d_count, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  NGIA_CUDA(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), s));
+  const uint32_t want = ceil_div(n, 256u), cap = (uint32_t)sms * 8;
+  fast_jobs_kernel<<<want < cap ? want : cap, 256, 0, s>>>(rep_row, parent, n, jobs, d_count);
+  NGIA_LAUNCHED();
+  NGIA_TRY(launch_align_jobs_dev_count(packed, offs, jobs, d_count, n, identity, s));
+  fast_assign_kernel<<<want < cap ? want : cap, 256, 0, s>>>(jobs, d_count, parent);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+}  // namespace ngia
+
+extern "C" int ngia_emit_edges(const uint32_t *d_jobs, uint32_t count, ngia_edge *d_edges,
+                               uint32_t *d_n_edges, void *stream) {
+  using namespace ngia;
+  if (!d_n_edges) return NGIA_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  if (count == 0) {
+    NGIA_CUDA(cudaMemsetAsync(d_n_edges, 0, sizeof(uint32_t), s));
+    return NGIA_OK;
+  }
+  if (!d_jobs || !d_edges) return NGIA_ERR_ARG;
+  const size_t bytes = (size_t)count * 4 + (size_t)count * 8 + scan_scratch_bytes(count) + 64;
+  void *scratch = nullptr;
+  cudaError_t e = cudaMallocAsync(&scratch, bytes, s);
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    return NGIA_ERR_NOMEM;
+  }
+  uint32_t *flags = static_cast<uint32_t *>(scratch);
+  uint64_t *off = reinterpret_cast<uint64_t *>(
+      (reinterpret_cast<uintptr_t>(flags + count) + 15) & ~uintptr_t(15));
+  uint64_t *scan_tmp = off + count;
+  uint64_t *d_total = scan_tmp + ceil_div<size_t>(count, 2048) + 1;
+  int st = NGIA_OK;
+  const uint32_t blocks = ceil_div(count, 256u);
+  positive_flags_kernel<<<blocks, 256, 0, s>>>(d_jobs + 2, 3, count, flags);
+  note_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) st = cuda_fail(e);
+  if (st == NGIA_OK) st = exclusive_scan_u64(flags, off, count, d_total, scan_tmp, s);
+  if (st == NGIA_OK) {
+    jobs_to_edges_kernel<<<blocks, 256, 0, s>>>(d_jobs, count, off, d_edges);
+    note_launch();
+    store_u32_from_u64_kernel<<<1, 1, 0, s>>>(d_total, d_n_edges);
+    note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) st = cuda_fail(e);
+  }
+  e = cudaFreeAsync(scratch, s);
+  if (st == NGIA_OK && e != cudaSuccess) st = cuda_fail(e);
+  return st;
+}

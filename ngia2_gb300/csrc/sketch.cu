@@ -1,0 +1,124 @@
+// sketch.cu -- stage (a): 64 minhash signatures per packed record.
+//
+// Restates the signing loop of MakeDB::packData (src/makedb.hpp:224-248):
+//   k-mer  = the last 8 residue codes as one 32-bit word, newest code in the
+//            low nibble (codes before position 0 are 0);
+//   signed positions: 7..L-1, or only L-1 when L < 8; none when L = 0;
+//   band k = min over signed positions of H(kmer ^ (k*0x9e3779b1 + 0x85ebca6b))
+//   with H Wang's 32-bit integer hash followed by two extra xor-shift-multiply
+//   rounds (the steps below), minimum 0xFFFFFFFF when nothing is signed.
+//
+// Mapping: one warp per record; each lane signs a contiguous run of the
+// positions and keeps all 64 running minima in registers (64 independent
+// hash chains per position give the scheduler plenty of independent work),
+// then one redux.sync min per band combines the lanes.  The workload is
+// integer-ALU bound (about 13 integer ops per band per position against half
+// a byte read per position).  Records are in length-descending index order,
+// so the longest records are scheduled first.
+#include "kernels.cuh"
+
+namespace ngia {
+
+// First xor-shift of the hash with the band seed folded in:
+//   x = kmer ^ seed;  x = (x ^ 61) ^ (x >> 16)
+//     = (kmer ^ (kmer >> 16)) ^ (seed ^ 61 ^ (seed >> 16))
+__host__ __device__ constexpr uint32_t band_seed_fold(uint32_t band) {
+  return (band * 0x9e3779b1u + 0x85ebca6bu) ^ 61u ^
+         ((band * 0x9e3779b1u + 0x85ebca6bu) >> 16);
+}
+
+__device__ __forceinline__ uint32_t band_hash_tail(uint32_t x) {
+  x = x * 9u;  // x + (x << 3)
+  x ^= x >> 4;
+  x *= 0x27d4eb2du;
+  x ^= x >> 15;
+  x = (x ^ (x >> 8)) * 0x9e3779b1u;
+  x ^= x >> 14;
+  return x;
+}
+
+struct PlaneCursor {  // decodes residue codes from a record's bit planes
+  const uint32_t *rec;
+  uint32_t block = 0xFFFFFFFFu;
+  uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+  __device__ __forceinline__ uint32_t code(uint32_t pos) {
+    const uint32_t blk = pos >> 5;
+    if (blk != block) {
+      const uint32_t *b = rec + 1 + 4 * blk;
+      p0 = __ldg(b);
+      p1 = __ldg(b + 1);
+      p2 = __ldg(b + 2);
+      p3 = __ldg(b + 3);
+      block = blk;
+    }
+    const uint32_t s = pos & 31u;
+    return ((p0 >> s) & 1u) | (((p1 >> s) & 1u) << 1) | (((p2 >> s) & 1u) << 2) |
+           (((p3 >> s) & 1u) << 3);
+  }
+};
+
+__global__ void __launch_bounds__(256)
+sketch_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
+              uint32_t n, uint32_t *__restrict__ sigs) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    PlaneCursor cur;
+    cur.rec = packed + offs[i];
+    const uint32_t len = __ldg(cur.rec);
+    const uint32_t first = len >= 8 ? 7u : (len > 0 ? len - 1 : 0u);
+    const uint32_t span = len - first;  // signed positions
+    const uint32_t per = (span + 31u) >> 5;
+    const uint32_t pb = first + lane * per;
+    const uint32_t pe = min(pb + per, len);
+
+    uint32_t mn[kBands];
+#pragma unroll
+    for (int k = 0; k < kBands; ++k) mn[k] = kFull;
+
+    if (pb < pe) {
+      uint32_t kmer = 0;
+      for (uint32_t q = pb >= 7 ? pb - 7 : 0; q < pb; ++q) kmer = (kmer << 4) | cur.code(q);
+      for (uint32_t p = pb; p < pe; ++p) {
+        kmer = (kmer << 4) | cur.code(p);
+        const uint32_t y = kmer ^ (kmer >> 16);
+#pragma unroll
+        for (int k = 0; k < kBands; ++k)
+          mn[k] = min(mn[k], band_hash_tail(y ^ band_seed_fold((uint32_t)k)));
+      }
+    }
+    uint32_t lo = kFull, hi = kFull;
+#pragma unroll
+    for (int k = 0; k < kBands; ++k) {
+      const uint32_t r = __reduce_min_sync(kFull, mn[k]);
+      if ((uint32_t)(k & 31) == lane) {
+        if (k < 32) lo = r;
+        else hi = r;
+      }
+    }
+    sigs[(size_t)lane * n + i] = lo;
+    sigs[(size_t)(lane + 32) * n + i] = hi;
+  }
+}
+
+int launch_sketch(const uint32_t *packed, const uint64_t *offs, uint32_t n,
+                  uint32_t *sigs, cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t want = ceil_div(n, 8u);  // 8 warps per block
+  const uint32_t cap = (uint32_t)sms * 16u;
+  sketch_kernel<<<want < cap ? want : cap, 256, 0, s>>>(packed, offs, n, sigs);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+}  // namespace ngia
+
+extern "C" int ngia_sketch(const uint32_t *d_packed, const uint64_t *d_rec_offsets,
+                           uint32_t n, uint32_t *d_sigs, void *stream) {
+  if (n == 0) return NGIA_OK;
+  if (!d_packed || !d_rec_offsets || !d_sigs) return NGIA_ERR_ARG;
+  return ngia::launch_sketch(d_packed, d_rec_offsets, n, d_sigs, ngia::as_stream(stream));
+}

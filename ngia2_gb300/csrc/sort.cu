@@ -1,0 +1,259 @@
+// sort.cu -- device primitives: segmented stable LSD radix sort of (u32 key,
+// u32 value) pairs and device-wide exclusive scans.  Hand-written; no library
+// sort or scan is used.
+//
+// Radix sort: 8-bit digits, one pass per digit, three kernels per pass:
+//   1. histogram: per (segment, tile of 4096) digit counts;
+//   2. scan: per segment, exclusive scan of the counts in digit-major order,
+//      giving every (digit, tile) its first output slot;
+//   3. scatter: each tile ranks its elements stably (match_any within a warp,
+//      per-warp digit counts across warps, a running count across rounds) and
+//      writes them to their slots.
+// Stability makes the passes compose into a sort by (key, input order); with
+// values = input index that is exactly a sort by (key, index).
+#include "kernels.cuh"
+
+namespace ngia {
+
+constexpr uint32_t kTile = 4096;
+constexpr uint32_t kSortThreads = 256;
+constexpr uint32_t kSortWarps = kSortThreads / 32;
+
+__global__ void __launch_bounds__(kSortThreads)
+rs_hist_kernel(const uint32_t *__restrict__ keys, uint32_t seg_len, int shift,
+               uint32_t ntiles, uint32_t *__restrict__ counts) {
+  __shared__ uint32_t h[kSortWarps][256];
+  const uint32_t seg = blockIdx.y, tile = blockIdx.x, warp = threadIdx.x >> 5;
+  for (uint32_t d = threadIdx.x; d < kSortWarps * 256; d += kSortThreads) (&h[0][0])[d] = 0;
+  __syncthreads();
+  const uint32_t *k = keys + (size_t)seg * seg_len;
+  const uint32_t beg = tile * kTile;
+  const uint32_t end = min(beg + kTile, seg_len);
+  for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads)
+    atomicAdd(&h[warp][(k[i] >> shift) & 255u], 1u);
+  __syncthreads();
+  uint32_t c = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < kSortWarps; ++w) c += h[w][threadIdx.x];
+  counts[((size_t)seg * 256 + threadIdx.x) * ntiles + tile] = c;
+}
+
+// In-place exclusive scan of `len` u32 per segment (one block per segment).
+__global__ void __launch_bounds__(1024)
+segment_scan_kernel(uint32_t *__restrict__ data, uint32_t len) {
+  __shared__ uint32_t part[1024];
+  uint32_t *d = data + (size_t)blockIdx.x * len;
+  const uint32_t per = (len + 1023) / 1024;
+  const uint32_t beg = threadIdx.x * per, end = min(beg + per, len);
+  uint32_t s = 0;
+  for (uint32_t i = beg; i < end; ++i) s += d[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024; off <<= 1) {  // Hillis-Steele inclusive
+    uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  for (uint32_t i = beg; i < end; ++i) {
+    const uint32_t v = d[i];
+    d[i] = run;
+    run += v;
+  }
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+                  uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
+                  uint32_t seg_len, int shift, uint32_t ntiles,
+                  const uint32_t *__restrict__ offsets) {
+  __shared__ uint32_t base[256];
+  __shared__ uint32_t wc[kSortWarps][256];
+  const uint32_t seg = blockIdx.y, tile = blockIdx.x;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  base[threadIdx.x] = offsets[((size_t)seg * 256 + threadIdx.x) * ntiles + tile];
+#pragma unroll
+  for (uint32_t w = 0; w < kSortWarps; ++w) wc[w][threadIdx.x] = 0;
+  __syncthreads();
+  const size_t so = (size_t)seg * seg_len;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (uint32_t r = 0; r < kTile / kSortThreads; ++r) {
+    const uint32_t first = tile * kTile + r * kSortThreads;
+    if (first >= seg_len) break;  // block-uniform
+    const uint32_t i = first + threadIdx.x;
+    const bool valid = i < seg_len;
+    const uint32_t key = valid ? kin[so + i] : 0u;
+    const uint32_t val = valid ? (vin ? vin[so + i] : i) : 0u;
+    const uint32_t d = (key >> shift) & 255u;
+    const uint32_t tag = valid ? d : 0x100u + lane;  // invalid lanes match nobody
+    const uint32_t peers = __match_any_sync(kFull, tag);
+    const uint32_t rank = __popc(peers & lt_mask);
+    if (valid && rank == 0) wc[warp][d] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      uint32_t pos = base[d] + rank;
+      for (uint32_t w = 0; w < warp; ++w) pos += wc[w][d];
+      kout[so + pos] = key;
+      vout[so + pos] = val;
+    }
+    __syncthreads();
+    uint32_t tot = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kSortWarps; ++w) {
+      tot += wc[w][threadIdx.x];
+      wc[w][threadIdx.x] = 0;
+    }
+    base[threadIdx.x] += tot;
+    __syncthreads();
+  }
+}
+
+size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs) {
+  const size_t ntiles = ceil_div<size_t>(seg_len, kTile);
+  const size_t n = (size_t)seg_len * segs;
+  return 2 * n * sizeof(uint32_t) + segs * 256 * ntiles * sizeof(uint32_t) + 256;
+}
+
+int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
+                     uint32_t *keys_out, uint32_t *vals_out, uint32_t seg_len,
+                     uint32_t segs, int begin_bit, int end_bit, void *scratch,
+                     cudaStream_t s) {
+  if (seg_len == 0 || segs == 0) return NGIA_OK;
+  const uint32_t ntiles = ceil_div(seg_len, kTile);
+  const size_t n = (size_t)seg_len * segs;
+  uint32_t *tk = static_cast<uint32_t *>(scratch);
+  uint32_t *tv = tk + n;
+  uint32_t *counts = tv + n;
+  const int passes = (end_bit - begin_bit + 7) / 8;
+  if (passes <= 0) {
+    NGIA_CUDA(cudaMemcpyAsync(keys_out, keys_in, n * 4, cudaMemcpyDeviceToDevice, s));
+    if (vals_in) {
+      NGIA_CUDA(cudaMemcpyAsync(vals_out, vals_in, n * 4, cudaMemcpyDeviceToDevice, s));
+      return NGIA_OK;
+    }
+    return NGIA_ERR_ARG;  // identity values with zero passes: caller's job
+  }
+  const uint32_t *sk = keys_in, *sv = vals_in;
+  for (int p = 0; p < passes; ++p) {
+    // the last pass lands in keys_out / vals_out
+    const bool to_out = ((passes - 1 - p) % 2) == 0;
+    uint32_t *dk = to_out ? keys_out : tk, *dv = to_out ? vals_out : tv;
+    const int shift = begin_bit + 8 * p;
+    dim3 grid(ntiles, segs);
+    rs_hist_kernel<<<grid, kSortThreads, 0, s>>>(sk, seg_len, shift, ntiles, counts);
+    NGIA_LAUNCHED();
+    segment_scan_kernel<<<segs, 1024, 0, s>>>(counts, 256 * ntiles);
+    NGIA_LAUNCHED();
+    rs_scatter_kernel<<<grid, kSortThreads, 0, s>>>(sk, sv, dk, dv, seg_len, shift,
+                                                    ntiles, counts);
+    NGIA_LAUNCHED();
+    sk = dk;
+    sv = dv;
+  }
+  return NGIA_OK;
+}
+
+// ---- device-wide exclusive scan (u32 in, u64 out) ---------------------------------
+constexpr uint32_t kScanThreads = 256, kScanItems = 8;
+constexpr uint32_t kScanBlock = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint64_t block_excl_scan(uint64_t v, uint64_t *sh,
+                                                    uint64_t &total) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t y = __shfl_up_sync(kFull, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint64_t w = lane < blockDim.x / 32 ? sh[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(kFull, w, o);
+      if (lane >= (uint32_t)o) w += y;
+    }
+    sh[lane] = w;
+  }
+  __syncthreads();
+  total = sh[blockDim.x / 32 - 1];
+  const uint64_t before = warp ? sh[warp - 1] : 0ull;
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+scan_reduce_kernel(const uint32_t *__restrict__ in, uint32_t n, uint64_t *__restrict__ sums) {
+  __shared__ uint64_t sh[32];
+  const size_t beg = (size_t)blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
+  uint64_t s = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kScanItems; ++k)
+    if (beg + k < n) s += in[beg + k];
+  uint64_t total;
+  block_excl_scan(s, sh, total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of the block sums by one block, looping over chunks.
+__global__ void __launch_bounds__(kScanThreads)
+scan_sums_kernel(uint64_t *__restrict__ sums, uint32_t nb, uint64_t *__restrict__ grand) {
+  __shared__ uint64_t sh[32];
+  uint64_t carry = 0;
+  for (uint32_t c = 0; c < nb; c += kScanThreads) {
+    const uint32_t i = c + threadIdx.x;
+    const uint64_t v = i < nb ? sums[i] : 0ull;
+    uint64_t total;
+    const uint64_t ex = block_excl_scan(v, sh, total);
+    if (i < nb) sums[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0 && grand) *grand = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+scan_apply_kernel(const uint32_t *__restrict__ in, uint32_t n,
+                  const uint64_t *__restrict__ sums, uint64_t *__restrict__ out) {
+  __shared__ uint64_t sh[32];
+  const size_t beg = (size_t)blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint64_t s = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kScanItems; ++k) {
+    v[k] = beg + k < n ? in[beg + k] : 0u;
+    s += v[k];
+  }
+  uint64_t total;
+  uint64_t run = sums[blockIdx.x] + block_excl_scan(s, sh, total);
+#pragma unroll
+  for (uint32_t k = 0; k < kScanItems; ++k) {
+    if (beg + k < n) out[beg + k] = run;
+    run += v[k];
+  }
+}
+
+size_t scan_scratch_bytes(uint32_t n) {
+  return (ceil_div<size_t>(n, kScanBlock) + 1) * sizeof(uint64_t);
+}
+
+int exclusive_scan_u64(const uint32_t *in, uint64_t *out, uint32_t n,
+                       uint64_t *d_total, void *scratch, cudaStream_t s) {
+  if (n == 0) {
+    if (d_total) NGIA_CUDA(cudaMemsetAsync(d_total, 0, sizeof(uint64_t), s));
+    return NGIA_OK;
+  }
+  const uint32_t nb = ceil_div(n, kScanBlock);
+  uint64_t *sums = static_cast<uint64_t *>(scratch);
+  scan_reduce_kernel<<<nb, kScanThreads, 0, s>>>(in, n, sums);
+  NGIA_LAUNCHED();
+  scan_sums_kernel<<<1, kScanThreads, 0, s>>>(sums, nb, d_total);
+  NGIA_LAUNCHED();
+  scan_apply_kernel<<<nb, kScanThreads, 0, s>>>(in, n, sums, out);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+}  // namespace ngia

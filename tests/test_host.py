@@ -1,0 +1,128 @@
+"""Host-side parts of the drop-in that need no GPU: the C-ABI library loads and
+exports every entry point of include/ngia.h; Leiden and the result file are
+bit-exact with the reference; the CLI's argument handling."""
+from __future__ import annotations
+
+import hashlib
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import ngia2_gb300 as ng
+from conftest import GOLDEN, IDENTITIES, ROOT, SETS, load_edges, result_sha
+
+
+def header_symbols() -> set[str]:
+    text = (ROOT / "include" / "ngia.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"\b(ngia_[a-z0-9_]+)\s*\(", text))
+
+
+def test_library_exports_every_declared_symbol(built):
+    L = ng.lib()
+    declared = header_symbols()
+    assert declared, "no declarations found"
+    for name in declared:
+        assert hasattr(L, name), name
+    assert declared == set(ng.exported_symbols())
+    assert b"sm_103a" in L.ngia_version()
+
+
+def test_status_strings(built):
+    L = ng.lib()
+    assert L.ngia_status_string(0) == b"ok"
+    assert L.ngia_status_string(-1) == b"invalid argument"
+    assert L.ngia_status_string(-2) == b"CUDA error"
+
+
+def test_argument_errors_need_no_gpu(built):
+    L = ng.lib()
+    assert L.ngia_align_pairs(0, 0, 0, 0, 90, 0) == 0  # empty batch is a no-op
+    assert L.ngia_align_pairs(0, 0, 0, 5, 0, 0) == -1  # identity out of range
+    assert L.ngia_align_pairs(0, 0, 0, 5, 100, 0) == -1
+    assert L.ngia_bucket(0, 10, 65, 0, 0) == -1  # bands out of range
+    assert L.ngia_sketch(0, 0, 10, 0, 0) == -1  # NULL pointers
+
+
+def edges_struct(e: np.ndarray) -> np.ndarray:
+    out = np.zeros(len(e), ng.EDGE_DTYPE)
+    out["rep"] = e[:, 0]
+    out["tar"] = e[:, 1]
+    out["weight"] = e[:, 2].astype(np.float32) / np.float32(100)
+    return out
+
+
+@pytest.mark.parametrize("name,identity", [(s, i) for s in SETS for i in IDENTITIES[s]])
+def test_leiden_matches_reference(built, golden, name, identity):
+    n = golden[name]["db"]["n"]
+    clu = ng.leiden(edges_struct(load_edges(name, identity)), n, ng.leiden_resolution(identity))
+    assert np.array_equal(clu, np.load(GOLDEN / f"{name}.leiden_{identity}.npy"))
+
+
+def test_leiden_resolution(built):
+    assert ng.leiden_resolution(50) == 1.0
+    assert abs(ng.leiden_resolution(90) - 0.2) < 1e-7
+    assert abs(ng.leiden_resolution(95) - 0.1) < 1e-7
+    assert abs(ng.leiden_resolution(1) - 0.02) < 1e-7
+
+
+@pytest.mark.parametrize("name,identity", [(s, i) for s in SETS for i in IDENTITIES[s]])
+def test_result_file_matches_reference(built, golden, tmp_path, name, identity):
+    want = result_sha(name, identity)
+    for kind, arr in (("leiden", np.load(GOLDEN / f"{name}.leiden_{identity}.npy")),
+                      ("fast", np.load(GOLDEN / f"{name}.fast_{identity}.npy"))):
+        out = tmp_path / f"{kind}.txt"
+        ng.save_result(arr, golden[name]["packed"], out)
+        assert hashlib.sha256(out.read_bytes()).hexdigest() == want[kind], kind
+
+
+def test_read_packed_layout(golden):
+    for name in SETS:
+        db = golden[name]["db"]
+        n = db["n"]
+        assert np.all(np.diff(db["lens"].astype(np.int64)) <= 0)  # length-descending
+        assert int(db["pack_off"][0]) == 4 + 24 * n + 256 * n
+        words = 1 + ((db["lens"].astype(np.int64) + 31) // 32) * 4
+        assert np.array_equal(np.diff(db["offsets"].astype(np.int64)), words[:-1])
+        assert np.all(db["packed"][db["offsets"].astype(np.int64)] == db["lens"])
+        last = n - 1
+        size = int(db["fasta_off"][last]) + int(db["name_lens"][last]) + int(db["lens"][last]) + 2
+        assert size == db["raw"].size
+        rep = db["rep"].astype(np.int64)
+        assert np.all(rep <= np.arange(n))
+
+
+def run_cli(*args):
+    return subprocess.run([str(ng.CLI_PATH), *args], capture_output=True, text=True,
+                          timeout=60)
+
+
+def test_cli_usage_paths(built, tmp_path):
+    r = run_cli()
+    assert r.returncode == 0 and "usage" in r.stdout
+    r = run_cli("-m", "clustering", "-p", str(tmp_path / "missing.packed"), "-r",
+                str(tmp_path / "r.txt"))
+    assert r.returncode == 0 and "does not exists" in r.stdout and "Usage" in r.stdout
+    r = run_cli("-m", "makedb", "-f", str(tmp_path / "missing.fa"), "-p", str(tmp_path / "x"))
+    assert r.returncode == 0 and "Usage" in r.stdout
+    bad = tmp_path / "bad.fa"
+    bad.write_bytes(b">a\r\nACGT\n")
+    r = run_cli("-m", "makedb", "-f", str(bad), "-p", str(tmp_path / "x"))
+    assert r.returncode == 0 and "\\r" in r.stdout
+    bad.write_bytes(b">a\nACGT")
+    r = run_cli("-m", "makedb", "-f", str(bad), "-p", str(tmp_path / "x"))
+    assert r.returncode == 0 and "end with" in r.stdout
+    r = run_cli("-m", "nonsense")
+    assert r.returncode == 0 and "makedb/clustering/fast" in r.stdout
+
+
+def test_cli_checks_identity_and_bands(built, golden, tmp_path):
+    packed = str(golden["prot"]["packed"])
+    for flags in (("-i", "0"), ("-i", "100"), ("-i", "abc"), ("-b", "0"), ("-b", "65")):
+        r = run_cli("-m", "clustering", "-p", packed, "-r", str(tmp_path / "r.txt"), *flags)
+        assert r.returncode == 0 and "Usage" in r.stdout, flags
+    # README spelling: cluster -i -p -r goes to the same checks
+    r = run_cli("cluster", "-i", "100", "-p", packed, "-r", str(tmp_path / "r.txt"))
+    assert r.returncode == 0 and "identity should be 1-99" in r.stdout

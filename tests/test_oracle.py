@@ -1,0 +1,117 @@
+"""The CPU oracle pinned against the reference's own outputs (golden fixtures
+made by running the reference's makedb / kernel / buildGraph code)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN, IDENTITIES, SETS, load_edges, load_pairs
+
+
+def records(db):
+    for i in range(db["n"]):
+        o = int(db["offsets"][i])
+        yield db["packed"][o:o + 1 + ((int(db["lens"][i]) + 31) // 32) * 4]
+
+
+def fasta_records(path):
+    """(name, residues) of the FASTA records makedb keeps, in file order."""
+    data = path.read_bytes()
+    out = []
+    for rec in data.split(b"\n>"):
+        lines = rec.split(b"\n")
+        name = lines[0] if lines[0].startswith(b">") else b">" + lines[0]
+        seq = b"".join(lines[1:])
+        out.append((name, seq))
+    return out
+
+
+@pytest.mark.parametrize("name", SETS)
+def test_pack_matches_reference(built, golden, name):
+    db = golden[name]["db"]
+    recs = [r for r in fasta_records(golden[name]["fa"]) if len(r[1]) < 0xFFFF]
+    # makedb order: stable by length descending
+    order = sorted(range(len(recs)), key=lambda i: -len(recs[i][1]))
+    assert db["n"] == len(recs)
+    for i, rec in zip(order, records(db)):
+        assert np.array_equal(oracle.pack_record(recs[i][1]), rec)
+
+
+@pytest.mark.parametrize("name", SETS)
+def test_sketch_matches_reference(built, golden, name):
+    db = golden[name]["db"]
+    sigs = np.load(GOLDEN / f"{name}.sigs.npy")
+    mine = oracle.sketch_all(db["packed"], db["offsets"], db["lens"])
+    assert np.array_equal(mine, sigs.T)
+
+
+@pytest.mark.parametrize("name", SETS)
+def test_bucket_matches_reference(built, golden, name):
+    db = golden[name]["db"]
+    sigs = np.load(GOLDEN / f"{name}.sigs.npy")
+    for b in range(64):
+        assert np.array_equal(oracle.bucket_band(sigs[:, b]), db["rep"][b]), b
+
+
+@pytest.mark.parametrize("name,identity", [(s, i) for s in SETS for i in IDENTITIES[s]])
+def test_align_matches_reference(built, golden, name, identity):
+    db = golden[name]["db"]
+    pairs, s_split, s_fma, _ = load_pairs(name, identity)
+    assert np.array_equal(oracle.align_pairs(db["packed"], db["offsets"], pairs, identity,
+                                             oracle.ROUND_SPLIT), s_split)
+    assert np.array_equal(oracle.align_pairs(db["packed"], db["offsets"], pairs, identity,
+                                             oracle.ROUND_FMA), s_fma)
+
+
+@pytest.mark.parametrize("name,identity", [(s, i) for s in SETS for i in IDENTITIES[s]])
+def test_graph_matches_reference(built, golden, name, identity):
+    db = golden[name]["db"]
+    for mode, tag in ((oracle.ROUND_SPLIT, "split"), (oracle.ROUND_FMA, "fma")):
+        e, total = oracle.graph_edges(db["packed"], db["offsets"], db["lens"], db["rep"],
+                                      identity, 64, mode)
+        assert np.array_equal(e, load_edges(name, identity, tag))
+    assert total == load_pairs(name, identity)[3]
+
+
+def test_known_answer_lcs(built):
+    """Full-band cases: the banded bit-parallel LCS equals the textbook DP."""
+    z = np.load(GOLDEN / "known_answer.npz")
+    ra = np.concatenate([[0], np.cumsum(z["rep_lens"])])
+    ta = np.concatenate([[0], np.cumsum(z["tar_lens"])])
+    for k in range(len(z["lcs"])):
+        a = z["reps"][ra[k]:ra[k + 1]].tobytes()
+        b = z["tars"][ta[k]:ta[k + 1]].tobytes()
+        got = oracle.banded_lcs(oracle.pack_record(a), oracle.pack_record(b), 1)
+        assert got == z["lcs"][k], (a, b)
+
+
+def test_identity_formula(built):
+    # identical 40-residue sequences: LCS 40, identity 40*100/(40+40-40) = 100
+    s = b"ACDEFGHIKLMNPQRSTVWY" * 2
+    r = oracle.pack_record(s)
+    assert oracle.align_records(r, r, 90) == 100
+    # disjoint codes: LCS 0 -> 0
+    assert oracle.align_records(oracle.pack_record(b"A" * 40), oracle.pack_record(b"C" * 40),
+                                1) == 0
+    # code-0 residues never match, even against themselves
+    x = oracle.pack_record(b"X" * 40)
+    assert oracle.align_records(x, x, 1) == 0
+    # half of a 40-mer: LCS 20 of 40 vs 20 -> 20*100/(40+20-20) = 50
+    assert oracle.align_records(oracle.pack_record(s), oracle.pack_record(s[:20]), 40) == 50
+
+
+def test_round_modes_differ_where_expected(built):
+    # t = 0.9f: 320 - 320*t is exactly 32 after rounding the product, but
+    # slightly above 32 when fused, which moves both band edges by one block.
+    assert oracle.band_bounds(320, 320, 90, oracle.ROUND_SPLIT) == (32, 64)
+    assert oracle.band_bounds(320, 320, 90, oracle.ROUND_FMA) == (64, 65)
+    assert oracle.band_blocks(320, 320, 90, oracle.ROUND_SPLIT) < \
+        oracle.band_blocks(320, 320, 90, oracle.ROUND_FMA)
+    # at 300 the right bound differs by one residue but not in whole blocks
+    assert oracle.band_bounds(300, 300, 90, oracle.ROUND_SPLIT) == (32, 62)
+    assert oracle.band_bounds(300, 300, 90, oracle.ROUND_FMA) == (32, 63)
+    assert oracle.band_blocks(300, 300, 90, oracle.ROUND_SPLIT) == \
+        oracle.band_blocks(300, 300, 90, oracle.ROUND_FMA)
+    # the length filter rejects Lt < Lr * t
+    assert oracle.band_bounds(100, 89, 90) is None
