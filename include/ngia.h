@@ -91,6 +91,22 @@ int ngia_sketch(const uint32_t *d_packed, const uint64_t *d_rec_offsets,
 int ngia_bucket(const uint32_t *d_sigs, uint32_t n, uint32_t bands,
                 uint32_t *d_rep, void *stream);
 
+/* Same result as ngia_bucket without allocating anything, for callers that
+ * cannot allocate device memory while they run (a plugin in a host program
+ * that reserves the device up front, a loop that must never take the
+ * allocator's synchronising path, a service whose memory is capped).  No
+ * counterpart in the reference, which always allocates.
+ * Limit: n * bands <= 1,048,576 (e.g. 16,384 sequences x 64 bands); larger
+ * inputs return NGIA_ERR_ARG.  The scratch is a fixed ~16.3 MiB device array
+ * that every GPU loading this library holds until the process exits.  The
+ * first call on a device looks up that array's device address (make it before
+ * any stream capture).  All calls share the array: calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised by the
+ * caller.  Every scratch word is written before it is read, so nothing needs
+ * clearing between calls. */
+int ngia_bucket_noalloc(const uint32_t *d_sigs, uint32_t n, uint32_t bands,
+                        uint32_t *d_rep, void *stream);
+
 /* ---- stage (c): align ---------------------------------------------------------
  * Drop-in for BuildGraph::kernel_dynamic (src/buildGraph.hpp:192-253, launch
  * at :323; same kernel at src/fastClustering.hpp:183-244, launch at :313):

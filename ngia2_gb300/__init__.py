@@ -67,6 +67,8 @@ _SIGNATURES = {
     "ngia_set_round_mode": (C.c_int, [C.c_int]),
     "ngia_sketch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "ngia_bucket": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "ngia_bucket_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                      C.c_void_p]),
     "ngia_align_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                    C.c_uint32, C.c_void_p]),
     "ngia_emit_edges": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -156,6 +158,12 @@ def sketch(d_packed: int, d_offsets: int, n: int, d_sigs: int, stream: int = 0) 
 
 def bucket(d_sigs: int, n: int, bands: int, d_rep: int, stream: int = 0) -> None:
     _check(lib().ngia_bucket(d_sigs, n, bands, d_rep, stream), "ngia_bucket")
+
+
+def bucket_noalloc(d_sigs: int, n: int, bands: int, d_rep: int, stream: int = 0) -> None:
+    """ngia_bucket with its scratch in the library's fixed device array (no
+    allocation; n * bands <= 1,048,576; calls must not overlap on the GPU)."""
+    _check(lib().ngia_bucket_noalloc(d_sigs, n, bands, d_rep, stream), "ngia_bucket_noalloc")
 
 
 def align_pairs(d_packed: int, d_offsets: int, d_jobs: int, count: int, identity: int,

@@ -9,6 +9,8 @@
 // Device form: all bands are sorted together as 64 segments by the segmented
 // radix sort (sort.cu), then one coalesced pass over the sorted runs writes
 // the predecessor links.
+#include <mutex>
+
 #include "kernels.cuh"
 
 namespace ngia {
@@ -67,4 +69,59 @@ extern "C" int ngia_bucket(const uint32_t *d_sigs, uint32_t n, uint32_t bands,
   e = cudaFreeAsync(scratch, s);
   if (st == NGIA_OK && e != cudaSuccess) st = ngia::cuda_fail(e);
   return st;
+}
+
+// ---- allocation-free variant ----------------------------------------------------
+// Some callers cannot allocate device memory at call time: a plugin living in
+// a host application that reserves the whole device up front, a real-time loop
+// that must not take the synchronising allocator path, or a memory-capped
+// service that forbids allocations once it is serving.  ngia_bucket_noalloc
+// gives them the bucketing stage with its scratch in a fixed array that every
+// GPU loading this library holds until the process exits.
+
+namespace ngia {
+
+// Largest n * bands the fixed scratch serves (e.g. 16,384 sequences x 64 bands).
+constexpr uint64_t kNoAllocMaxElems = 1ull << 20;
+// bucket_scratch_bytes(n, bands) for n * bands <= kNoAllocMaxElems and
+// bands <= 64: 16 bytes per element plus the per-tile digit counts
+// (256 words per tile, at most kNoAllocMaxElems / 4096 + 64 tiles) plus slack.
+constexpr size_t kNoAllocScratchBytes =
+    16 * kNoAllocMaxElems + 1024 * (kNoAllocMaxElems / 4096 + kBands) + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Host code may not pass g_noalloc_scratch itself to a kernel (on the host it
+// names a host-side stand-in); the device address is looked up once per
+// device with that device current, and cached.
+static void *g_noalloc_ptr[128] = {};
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(void **out) {
+  int dev = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return NGIA_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    NGIA_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return NGIA_OK;
+}
+
+}  // namespace ngia
+
+extern "C" int ngia_bucket_noalloc(const uint32_t *d_sigs, uint32_t n, uint32_t bands,
+                                   uint32_t *d_rep, void *stream) {
+  using namespace ngia;
+  if (bands < 1 || bands > NGIA_BANDS) return NGIA_ERR_ARG;
+  if (n == 0) return NGIA_OK;
+  if (!d_sigs || !d_rep) return NGIA_ERR_ARG;
+  if ((uint64_t)n * bands > kNoAllocMaxElems) return NGIA_ERR_ARG;
+  if (bucket_scratch_bytes(n, bands) > kNoAllocScratchBytes) return NGIA_ERR_ARG;
+  void *scratch = nullptr;
+  NGIA_TRY(noalloc_scratch(&scratch));
+  return bucket(d_sigs, n, bands, d_rep, scratch, as_stream(stream));
 }
