@@ -1,6 +1,7 @@
 // align.cu -- alignment kernels: the drop-in job-triple kernel and the
 // length-binned batched kernels.
 #include "align.cuh"
+#include "align_lds.cuh"
 #include "kernels.cuh"
 
 namespace ngia {
@@ -54,7 +55,8 @@ align_jobs_dev_count_kernel(const uint32_t *__restrict__ packed,
   }
 }
 
-// Batched form: pairs of one width class, listed in `order[begin, end)`.
+// Batched form, register-plane window or general kernel: pairs of one width
+// class, listed in `order[begin, end)`.
 template <int W>
 __global__ void __launch_bounds__(128)
 align_class_kernel(const uint32_t *__restrict__ packed,
@@ -79,6 +81,79 @@ align_class_kernel(const uint32_t *__restrict__ packed,
   scores[p] = identity_score(lcs, lr, lt, t);
 }
 
+// Batched form, shared-memory table kernel (align_lds.cuh).
+template <int W>
+__global__ void __launch_bounds__(lds_threads(W))
+align_lds_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
+                 const uint64_t *__restrict__ offs, const uint2 *__restrict__ pairs,
+                 const uint32_t *__restrict__ order, uint32_t begin, uint32_t end,
+                 uint32_t *__restrict__ scores, float t, int fma_mode) {
+  extern __shared__ uint32_t smem[];
+  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= end) return;
+  LdsTable<W> tab{smem + (threadIdx.x >> 5) * (16 * W * 32) + (threadIdx.x & 31u)};
+  const uint32_t p = order[k];
+  const uint2 pr = pairs[p];
+  const uint32_t *rep = packed + offs[pr.x];
+  const uint64_t to = offs[pr.y];
+  const uint32_t lr = __ldg(rep), lt = __ldg(packed + to);
+  const Band b = make_band(lr, lt, t, fma_mode);
+  const uint32_t lcs = lcs_lds<W>(rep, nib + to + 1, b, tab);
+  scores[p] = identity_score(lcs, lr, lt, t);
+}
+
+// Planes -> nibbles: the same record layout, with each block's four plane
+// words replaced by four words of eight 4-bit codes (position 8k + j of the
+// record in nibble 7 - j of word k).  The length word is copied.
+__global__ void __launch_bounds__(256)
+nibble_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
+              uint32_t n, uint32_t *__restrict__ nib) {
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const uint64_t o = offs[i];
+    const uint32_t len = packed[o];
+    if (threadIdx.x == 0) nib[o] = len;
+    const uint32_t blocks = (len + 31) >> 5;
+    for (uint32_t w = threadIdx.x; w < 4 * blocks; w += blockDim.x) {
+      const uint32_t blk = w >> 2, q = w & 3u;
+      const uint32_t *pl = packed + o + 1 + 4 * blk;
+      uint32_t out = 0;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const uint32_t byte = (pl[e] >> (8 * q)) & 0xFFu;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) out |= ((byte >> j) & 1u) << (28 - 4 * j + e);
+      }
+      nib[o + 1 + w] = out;
+    }
+  }
+}
+
+int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
+                   cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t cap = (uint32_t)sms * 16;
+  nibble_kernel<<<n < cap ? n : cap, 256, 0, s>>>(packed, offs, n, nib);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+template <int W>
+static int launch_lds(const uint32_t *packed, const uint32_t *nib, const uint64_t *offs,
+                      const uint2 *pairs, const uint32_t *order, uint32_t begin, uint32_t end,
+                      uint32_t *scores, float t, int fm, cudaStream_t s) {
+  constexpr int T = lds_threads(W);
+  constexpr size_t smem = lds_smem_bytes(W);
+  NGIA_CUDA(cudaFuncSetAttribute(align_lds_kernel<W>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  align_lds_kernel<W><<<ceil_div(end - begin, (uint32_t)T), T, smem, s>>>(
+      packed, nib, offs, pairs, order, begin, end, scores, t, fm);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
 int launch_align_jobs(const uint32_t *packed, const uint64_t *offs, uint32_t *jobs,
                       uint32_t count, uint32_t identity, cudaStream_t s) {
   if (count == 0) return NGIA_OK;
@@ -100,21 +175,24 @@ int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
   return NGIA_OK;
 }
 
-int launch_align_class(int cls, const uint32_t *packed, const uint64_t *offs,
-                       const uint2 *pairs, const uint32_t *order, uint32_t begin,
-                       uint32_t end, uint32_t *scores, uint32_t identity,
+int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
+                       const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
+                       uint32_t begin, uint32_t end, uint32_t *scores, uint32_t identity,
                        cudaStream_t s) {
   if (end <= begin) return NGIA_OK;
   const float t = identity_threshold(identity);
   const int fm = round_mode();
   const uint32_t blocks = ceil_div(end - begin, 128u);
   switch (cls) {
-    case 0: align_class_kernel<4><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
-    case 1: align_class_kernel<8><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
-    case 2: align_class_kernel<12><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
-    case 3: align_class_kernel<16><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
-    case 4: align_class_kernel<24><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
-    case 5: align_class_kernel<32><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case 0: return launch_lds<4>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
+    case 1: return launch_lds<6>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
+    case 2: return launch_lds<8>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
+    case 3: return launch_lds<10>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
+    case 4: return launch_lds<12>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
+    case 5: return launch_lds<14>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
+    case 6: return launch_lds<16>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
+    case 7: align_class_kernel<24><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case 8: align_class_kernel<32><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
     case kGeneralClass: align_class_kernel<0><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
     default: return NGIA_ERR_ARG;
   }

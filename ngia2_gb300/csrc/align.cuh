@@ -36,22 +36,36 @@
 
 namespace ngia {
 
-// s[0..W) = a + b as one W-word number (W multiple of 4, carry in = cin != 0
-// when CIN).
+// One chunk of C words of a multi-word add (carry in when CIN, carry out when
+// COUT), dispatched to the PTX chains.
+template <int C, bool CIN, bool COUT>
+__device__ __forceinline__ void add_chunk(uint32_t *s, const uint32_t *a, const uint32_t *b,
+                                          uint32_t cin, uint32_t &cout) {
+#define NGIA_CHUNK(N)                                              \
+  if constexpr (C == N) {                                          \
+    if constexpr (CIN && COUT) add_chain##N##_cc(s, a, b, cin, cout); \
+    else if constexpr (CIN) add_chain##N##_cn(s, a, b, cin);       \
+    else if constexpr (COUT) add_chain##N##_zc(s, a, b, cout);     \
+    else add_chain##N##_zn(s, a, b);                               \
+  }
+  NGIA_CHUNK(2)
+  NGIA_CHUNK(4)
+  NGIA_CHUNK(8)
+#undef NGIA_CHUNK
+}
+
+// s[0..W) = a + b as one W-word number (W even; carry in = cin != 0 when CIN).
 template <int W, bool CIN>
 __device__ __forceinline__ void add_words(uint32_t *s, const uint32_t *a,
                                           const uint32_t *b, uint32_t cin) {
-  if constexpr (W == 4) {
-    if constexpr (CIN) add_chain4_cn(s, a, b, cin);
-    else add_chain4_zn(s, a, b);
-  } else if constexpr (W == 8) {
-    if constexpr (CIN) add_chain8_cn(s, a, b, cin);
-    else add_chain8_zn(s, a, b);
+  static_assert(W > 0 && W % 2 == 0, "window width must be even");
+  constexpr int C = W >= 8 ? 8 : (W >= 4 ? 4 : 2);
+  uint32_t c = 0;
+  if constexpr (W == C) {
+    add_chunk<C, CIN, false>(s, a, b, cin, c);
   } else {
-    uint32_t c;
-    if constexpr (CIN) add_chain8_cc(s, a, b, cin, c);
-    else add_chain8_zc(s, a, b, c);
-    add_words<W - 8, true>(s + 8, a + 8, b + 8, c);
+    add_chunk<C, CIN, true>(s, a, b, cin, c);
+    add_words<W - C, true>(s + C, a + C, b + C, c);
   }
 }
 
@@ -219,27 +233,26 @@ __device__ inline uint32_t lcs_general(const uint32_t *__restrict__ rep,
   return lcs;
 }
 
-// Window width classes of the batched aligner; class kGeneralClass uses
-// lcs_general.  Pairs failing the length filter get class kSkipClass.
-// Widths: 4, 8, 12, 16, 24, 32.
-constexpr int kNumWindowClasses = 6;
-constexpr int kGeneralClass = kNumWindowClasses;
-constexpr int kSkipClass = kNumWindowClasses + 1;
-constexpr int kNumClasses = kNumWindowClasses + 2;
+// Width classes of the batched aligner:
+//   0..6  shared-memory table kernel (align_lds.cuh), W = 4, 6, ..., 16
+//   7, 8  register-plane window kernel, W = 24, 32
+//   9     general kernel (any width)
+//   10    pairs failing the length filter (score 0, not launched)
+constexpr int kNumLdsClasses = 7;
+constexpr int kGeneralClass = 9;
+constexpr int kSkipClass = 10;
+constexpr int kNumClasses = 11;
 
 __host__ __device__ inline int class_width(int c) {
-  return c < 4 ? 4 * (c + 1) : (c == 4 ? 24 : 32);
+  return c < kNumLdsClasses ? 4 + 2 * c : (c == 7 ? 24 : (c == 8 ? 32 : 0));
 }
 
 __host__ __device__ inline int width_class(const Band &b) {
   if (!b.pass) return kSkipClass;
   const uint32_t w = b.width;
-  if (w <= 4) return 0;
-  if (w <= 8) return 1;
-  if (w <= 12) return 2;
-  if (w <= 16) return 3;
-  if (w <= 24) return 4;
-  if (w <= 32) return 5;
+  if (w <= 16) return w <= 4 ? 0 : (int)((w - 3) / 2);  // 5,6 -> 1; 7,8 -> 2; ...
+  if (w <= 24) return 7;
+  if (w <= 32) return 8;
   return kGeneralClass;
 }
 

@@ -14,6 +14,42 @@
 
 namespace ngia {
 
+__device__ __forceinline__ void add_chain2_zn(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm("add.cc.u32 %0, %2, %4;\n\t"
+      "addc.u32 %1, %3, %5;\n\t"
+      : "=r"(s[0]), "=r"(s[1])
+      : "r"(a[0]), "r"(a[1]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void add_chain2_zc(uint32_t *s, const uint32_t *a, const uint32_t *b, uint32_t &cout) {
+  asm("add.cc.u32 %0, %3, %5;\n\t"
+      "addc.cc.u32 %1, %4, %6;\n\t"
+      "addc.u32 %2, 0, 0;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(cout)
+      : "r"(a[0]), "r"(a[1]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void add_chain2_cn(uint32_t *s, const uint32_t *a, const uint32_t *b, uint32_t cin) {
+  asm("{\n\t.reg .u32 t;\n\t"
+      "add.cc.u32 t, %6, 0xFFFFFFFF;\n\t"
+      "addc.cc.u32 %0, %2, %4;\n\t"
+      "addc.u32 %1, %3, %5;\n\t"
+      "}"
+      : "=r"(s[0]), "=r"(s[1])
+      : "r"(a[0]), "r"(a[1]), "r"(b[0]), "r"(b[1]), "r"(cin));
+}
+
+__device__ __forceinline__ void add_chain2_cc(uint32_t *s, const uint32_t *a, const uint32_t *b, uint32_t cin, uint32_t &cout) {
+  asm("{\n\t.reg .u32 t;\n\t"
+      "add.cc.u32 t, %7, 0xFFFFFFFF;\n\t"
+      "addc.cc.u32 %0, %3, %5;\n\t"
+      "addc.cc.u32 %1, %4, %6;\n\t"
+      "addc.u32 %2, 0, 0;\n\t"
+      "}"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(cout)
+      : "r"(a[0]), "r"(a[1]), "r"(b[0]), "r"(b[1]), "r"(cin));
+}
+
 __device__ __forceinline__ void add_chain4_zn(uint32_t *s, const uint32_t *a, const uint32_t *b) {
   asm("add.cc.u32 %0, %4, %8;\n\t"
       "addc.cc.u32 %1, %5, %9;\n\t"

@@ -62,7 +62,7 @@ struct ngia_ctx {
   uint32_t n = 0;
   uint64_t packed_words = 0;
   uint32_t rep_bands = 0;
-  ngia::DevBuf packed, offs, lens, rep, sigs;
+  ngia::DevBuf packed, nib, offs, lens, rep, sigs;
   // graph build work
   ngia::DevBuf ucount, uoff, counters, pairs, scores, cls, cls_sorted, order, sort_tmp,
       emit_tmp, edges, scan_tmp, jobs;
@@ -157,11 +157,11 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   uint32_t begin[kNumClasses + 1];
   begin[0] = 0;
   for (int k = 0; k < kNumClasses; ++k) begin[k + 1] = begin[k] + hc.class_count[k];
-  const int launch_order[] = {kGeneralClass, 5, 4, 3, 2, 1, 0};
+  const int launch_order[] = {kGeneralClass, 8, 7, 6, 5, 4, 3, 2, 1, 0};
   for (int cl : launch_order)
-    NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), pairs,
-                                c->order.as<uint32_t>(), begin[cl], begin[cl + 1], scores,
-                                identity, s));
+    NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->nib.as<uint32_t>(),
+                                c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
+                                begin[cl], begin[cl + 1], scores, identity, s));
   NGIA_CUDA(cudaEventRecord(c->ev[2], s));
   // 4. emit: compact hits, sort by (rep, tar)
   NGIA_TRY(c->emit_tmp.reserve(emit_scratch_bytes(m, n)));
@@ -227,6 +227,9 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
   NGIA_CUDA(cudaMemcpyAsync(c->packed.p, h_packed, words * 4, cudaMemcpyHostToDevice, s));
   NGIA_CUDA(cudaMemcpyAsync(c->offs.p, h_offs, (size_t)n * 8, cudaMemcpyHostToDevice, s));
   NGIA_CUDA(cudaMemcpyAsync(c->lens.p, h_lens, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  NGIA_TRY(c->nib.reserve(words * 4));
+  NGIA_TRY(launch_nibbles(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), n,
+                          c->nib.as<uint32_t>(), s));
   c->n = n;
   c->packed_words = words;
   c->rep_bands = 0;
@@ -294,7 +297,7 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
 void ngia_ctx_destroy(ngia_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  ngia::DevBuf *bufs[] = {&c->packed, &c->offs,  &c->lens,       &c->rep,    &c->sigs,
+  ngia::DevBuf *bufs[] = {&c->packed, &c->nib, &c->offs,  &c->lens,       &c->rep,    &c->sigs,
                           &c->ucount, &c->uoff,  &c->counters,   &c->pairs,  &c->scores,
                           &c->cls,    &c->cls_sorted, &c->order, &c->sort_tmp,
                           &c->emit_tmp, &c->edges, &c->scan_tmp, &c->jobs};

@@ -32,10 +32,12 @@ int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
                                 uint32_t *jobs, const uint32_t *d_count,
                                 uint32_t max_count, uint32_t identity,
                                 cudaStream_t s);
-int launch_align_class(int cls, const uint32_t *packed, const uint64_t *offs,
-                       const uint2 *pairs, const uint32_t *order, uint32_t begin,
-                       uint32_t end, uint32_t *scores, uint32_t identity,
+int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
+                       const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
+                       uint32_t begin, uint32_t end, uint32_t *scores, uint32_t identity,
                        cudaStream_t s);
+int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
+                   cudaStream_t s);
 
 // pairs.cu
 int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,

@@ -85,7 +85,7 @@ def main():
             res["ref_buildgraph_sort_s"] = consuming(out, "[buildGraph]")
             m = re.search(r"compare pairs:\s*(\d+)", out)
             res["ref_compare_pairs"] = int(m.group(1)) if m else None
-        args[3] = d / f"ours_{mode}.txt"
+        args[5] = d / f"ours_{mode}.txt"
         t, out = run([ng.CLI_PATH, *args])
         res[f"ours_{mode}_s"] = t
         m = re.search(r"\[%s\]\s*([0-9.]+) s" % mode if mode == "fast" else r"\[clustering\]\s*([0-9.]+) s", out)

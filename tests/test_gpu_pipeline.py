@@ -80,6 +80,40 @@ def test_result_files_are_byte_identical(cuda, built, golden, tmp_path, name, id
         assert hashlib.sha256(out.read_bytes()).hexdigest() == want[kind], kind
 
 
+@pytest.mark.parametrize("identity", [30, 50, 70, 90, 95])
+def test_batched_aligner_on_chosen_pairs(cuda, built, identity):
+    """Arbitrary pair sets through the batched path (every width class): rep
+    rows are written so that target i's candidates are chosen partners j < i,
+    and the sorted edge list must equal the oracle's."""
+    import oracle
+    from ngia2_gb300 import synth
+    from gpu_util import build_db
+    rng = np.random.default_rng(400 + identity)
+    seqs = []
+    for k in range(120):  # families of related sequences of varied length
+        root = synth._draw(rng, synth.AMINO, synth.AMINO_FREQ,
+                           int(rng.integers(20, 3000 if k % 10 else 6000))).tobytes()
+        for _ in range(5):
+            b = bytearray(root[: max(1, int(len(root) * rng.uniform(0.88, 1.0)))])
+            for p in rng.integers(0, len(b), size=int(len(b) * rng.uniform(0, 0.12))):
+                b[int(p)] = synth.AMINO[rng.integers(0, 20)]
+            seqs.append(bytes(b))
+    seqs.sort(key=len, reverse=True)  # index order = length descending
+    packed, offs, lens = build_db(seqs)
+    n = len(seqs)
+    rep = np.tile(np.arange(n, dtype=np.uint32), (8, 1))
+    for b in range(8):
+        for i in range(1, n):
+            if rng.random() < 0.7:
+                rep[b, i] = rng.integers(max(0, i - 12), i)
+    with ng.Context() as ctx:
+        ctx.load(packed, offs, lens, rep, 8)
+        e, st = ctx.graph(identity, 8)
+    want, total = oracle.graph_edges(packed, offs, lens, rep, identity, 8, oracle.ROUND_FMA)
+    assert st["candidate_pairs"] == total
+    assert np.array_equal(as_triples(e), want)
+
+
 def test_cli_end_to_end(cuda, built, golden, tmp_path):
     packed = tmp_path / "p.packed"
     r = subprocess.run([str(ng.CLI_PATH), "-m", "makedb", "-f", str(golden["prot"]["fa"]), "-p",
