@@ -93,8 +93,8 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
   NGIA_TRY(c->rep.reserve((size_t)kBands * c->n * 4));
   NGIA_TRY(c->sort_tmp.reserve(bucket_scratch_bytes(c->n, bands)));
   NGIA_CUDA(cudaEventRecord(c->ev[0], s));
-  NGIA_TRY(launch_sketch(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
-                         c->sigs.as<uint32_t>(), s));
+  NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
+                                 c->sigs.as<uint32_t>(), s));
   NGIA_CUDA(cudaEventRecord(c->ev[1], s));
   NGIA_TRY(bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(),
                   c->sort_tmp.p, s));

@@ -9,6 +9,8 @@ namespace ngia {
 // sketch.cu
 int launch_sketch(const uint32_t *packed, const uint64_t *offs, uint32_t n,
                   uint32_t *sigs, cudaStream_t s);
+int launch_sketch_nibbles(const uint32_t *nib, const uint64_t *offs, uint32_t n,
+                          uint32_t *sigs, cudaStream_t s);
 
 // sort.cu
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs);

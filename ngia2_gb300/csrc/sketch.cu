@@ -10,11 +10,15 @@
 //
 // Mapping: one warp per record; each lane signs a contiguous run of the
 // positions and keeps all 64 running minima in registers (64 independent
-// hash chains per position give the scheduler plenty of independent work),
-// then one redux.sync min per band combines the lanes.  The workload is
-// integer-ALU bound (about 13 integer ops per band per position against half
-// a byte read per position).  Records are in length-descending index order,
-// so the longest records are scheduled first.
+// hash chains per position), then one redux.sync min per band combines the
+// lanes.  Records are in length-descending index order, so the longest are
+// scheduled first.
+//
+// The work is integer-ALU bound: 64 hashes per position against half a byte
+// read.  The integer ALU pipe retires 64 lanes per clock per SM while the
+// multiply-add pipe would otherwise sit idle, so every shift of the hash is
+// written as a multiply-high (x >> k == mulhi(x, 2^(32-k))) and every
+// multiply stays a multiply; the ALU keeps only the xors and the minimum.
 #include "kernels.cuh"
 
 namespace ngia {
@@ -27,20 +31,41 @@ __host__ __device__ constexpr uint32_t band_seed_fold(uint32_t band) {
          ((band * 0x9e3779b1u + 0x85ebca6bu) >> 16);
 }
 
+template <uint32_t K>
+__device__ __forceinline__ uint32_t shr_mul(uint32_t x) {  // x >> K on the multiply pipe
+  uint32_t r;
+  asm("mul.hi.u32 %0, %1, %2;" : "=r"(r) : "r"(x), "n"(1u << (32 - K)));
+  return r;
+}
+
+template <uint32_t C>
+__device__ __forceinline__ uint32_t mul_const(uint32_t x) {
+  uint32_t r;
+  asm("mul.lo.u32 %0, %1, %2;" : "=r"(r) : "r"(x), "n"(C));
+  return r;
+}
+
 __device__ __forceinline__ uint32_t band_hash_tail(uint32_t x) {
-  x = x * 9u;  // x + (x << 3)
-  x ^= x >> 4;
-  x *= 0x27d4eb2du;
-  x ^= x >> 15;
-  x = (x ^ (x >> 8)) * 0x9e3779b1u;
-  x ^= x >> 14;
+  x = mul_const<9u>(x);  // x + (x << 3)
+  x ^= shr_mul<4>(x);
+  x = mul_const<0x27d4eb2du>(x);
+  x ^= shr_mul<15>(x);
+  x = mul_const<0x9e3779b1u>(x ^ shr_mul<8>(x));
+  x ^= shr_mul<14>(x);
   return x;
 }
 
-struct PlaneCursor {  // decodes residue codes from a record's bit planes
+// k-mers from the bit planes of a packed record (ABI entry point).
+struct PlaneKmers {
   const uint32_t *rec;
+  __device__ static PlaneKmers make(const uint32_t *r) {
+    PlaneKmers k;
+    k.rec = r;
+    return k;
+  }
   uint32_t block = 0xFFFFFFFFu;
   uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+  uint32_t kmer = 0;
   __device__ __forceinline__ uint32_t code(uint32_t pos) {
     const uint32_t blk = pos >> 5;
     if (blk != block) {
@@ -55,17 +80,40 @@ struct PlaneCursor {  // decodes residue codes from a record's bit planes
     return ((p0 >> s) & 1u) | (((p1 >> s) & 1u) << 1) | (((p2 >> s) & 1u) << 2) |
            (((p3 >> s) & 1u) << 3);
   }
+  __device__ __forceinline__ void start(uint32_t pb) {
+    kmer = 0;
+    for (uint32_t q = pb >= 7 ? pb - 7 : 0; q < pb; ++q) kmer = (kmer << 4) | code(q);
+  }
+  __device__ __forceinline__ uint32_t at(uint32_t p) {  // positions in increasing order
+    kmer = (kmer << 4) | code(p);
+    return kmer;
+  }
 };
 
+// k-mers from the nibble layout (word k holds positions 8k..8k+7, first in the
+// high nibble): the k-mer ending at p is the 32-bit window of the stream
+// starting at position p - 7, one funnel shift.
+struct NibbleKmers {
+  const uint32_t *nib;  // the record's first code word
+  __device__ static NibbleKmers make(const uint32_t *r) { return NibbleKmers{r + 1}; }
+  __device__ __forceinline__ void start(uint32_t) {}
+  __device__ __forceinline__ uint32_t at(uint32_t p) {
+    if (p < 7) return __ldg(nib) >> (28 - 4 * p);  // short record: codes 0..p
+    const uint32_t s = p - 7, k = s >> 3, r = s & 7u;
+    const uint32_t hi = __ldg(nib + k);
+    return r ? __funnelshift_l(__ldg(nib + k + 1), hi, 4 * r) : hi;
+  }
+};
+
+template <typename Source>
 __global__ void __launch_bounds__(256)
-sketch_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
+sketch_kernel(const uint32_t *__restrict__ words, const uint64_t *__restrict__ offs,
               uint32_t n, uint32_t *__restrict__ sigs) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-    PlaneCursor cur;
-    cur.rec = packed + offs[i];
-    const uint32_t len = __ldg(cur.rec);
+    const uint32_t *rec = words + offs[i];
+    const uint32_t len = __ldg(rec);
     const uint32_t first = len >= 8 ? 7u : (len > 0 ? len - 1 : 0u);
     const uint32_t span = len - first;  // signed positions
     const uint32_t per = (span + 31u) >> 5;
@@ -77,11 +125,11 @@ sketch_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ 
     for (int k = 0; k < kBands; ++k) mn[k] = kFull;
 
     if (pb < pe) {
-      uint32_t kmer = 0;
-      for (uint32_t q = pb >= 7 ? pb - 7 : 0; q < pb; ++q) kmer = (kmer << 4) | cur.code(q);
+      Source src = Source::make(rec);
+      src.start(pb);
       for (uint32_t p = pb; p < pe; ++p) {
-        kmer = (kmer << 4) | cur.code(p);
-        const uint32_t y = kmer ^ (kmer >> 16);
+        const uint32_t kmer = src.at(p);
+        const uint32_t y = kmer ^ shr_mul<16>(kmer);
 #pragma unroll
         for (int k = 0; k < kBands; ++k)
           mn[k] = min(mn[k], band_hash_tail(y ^ band_seed_fold((uint32_t)k)));
@@ -101,17 +149,28 @@ sketch_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ 
   }
 }
 
-int launch_sketch(const uint32_t *packed, const uint64_t *offs, uint32_t n,
-                  uint32_t *sigs, cudaStream_t s) {
+template <typename Source>
+static int launch(const uint32_t *words, const uint64_t *offs, uint32_t n, uint32_t *sigs,
+                  cudaStream_t s) {
   if (n == 0) return NGIA_OK;
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u);  // 8 warps per block
   const uint32_t cap = (uint32_t)sms * 16u;
-  sketch_kernel<<<want < cap ? want : cap, 256, 0, s>>>(packed, offs, n, sigs);
+  sketch_kernel<Source><<<want < cap ? want : cap, 256, 0, s>>>(words, offs, n, sigs);
   NGIA_LAUNCHED();
   return NGIA_OK;
+}
+
+int launch_sketch(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *sigs,
+                  cudaStream_t s) {
+  return launch<PlaneKmers>(packed, offs, n, sigs, s);
+}
+
+int launch_sketch_nibbles(const uint32_t *nib, const uint64_t *offs, uint32_t n,
+                          uint32_t *sigs, cudaStream_t s) {
+  return launch<NibbleKmers>(nib, offs, n, sigs, s);
 }
 
 }  // namespace ngia
