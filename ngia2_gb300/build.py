@@ -59,7 +59,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     for src in CU_SOURCES:
         out = OBJDIR / (src + ".o")
         cmd = [nv, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-               "--expt-relaxed-constexpr", *inc, "-c", str(CSRC / src), "-o", str(out)]
+               "--expt-relaxed-constexpr", *inc, *os.environ.get("NGIA_NVCC_FLAGS", "").split(),
+               "-c", str(CSRC / src), "-o", str(out)]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         jobs.append((out, [CSRC / src, *headers], cmd))

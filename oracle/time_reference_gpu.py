@@ -30,10 +30,14 @@ def sha(p: Path) -> str:
     return hashlib.sha256(p.read_bytes()).hexdigest()
 
 
+LOGS: list = []
+
+
 def run(cmd, timeout=3600):
     t0 = time.perf_counter()
     r = subprocess.run([str(c) for c in cmd], capture_output=True, text=True, timeout=timeout)
     dt = time.perf_counter() - t0
+    LOGS.append((" ".join(str(c) for c in cmd), r.stdout))
     if r.returncode != 0:
         raise RuntimeError(f"{cmd[0]} failed ({r.returncode}):\n{r.stdout[-2000:]}{r.stderr[-2000:]}")
     return dt, r.stdout
@@ -56,6 +60,7 @@ def main():
     ap.add_argument("--identity", type=int, default=95)
     ap.add_argument("--bands", type=int, default=64)
     ap.add_argument("--out", default="")
+    ap.add_argument("--log-dir", default="", help="keep every command's stdout here")
     a = ap.parse_args()
     import ngia2_gb300 as ng
     from ngia2_gb300 import synth
@@ -93,6 +98,10 @@ def main():
         res[f"{mode}_result_identical"] = sha(d / f"ref_{mode}.txt") == sha(d / f"ours_{mode}.txt")
     line = json.dumps(res)
     print(line)
+    if a.log_dir:
+        Path(a.log_dir).mkdir(parents=True, exist_ok=True)
+        for k, (cmd, out) in enumerate(LOGS):
+            (Path(a.log_dir) / f"run{k:02d}.txt").write_text(cmd + "\n\n" + out)
     if a.out:
         Path(a.out).write_text(line + "\n")
 
