@@ -134,7 +134,10 @@ __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
 
 // Threads per block of the shared-memory aligner for width W (64*W bytes of
 // table per thread).
-__host__ __device__ constexpr int lds_threads(int W) { return W <= 8 ? 128 : (W <= 12 ? 128 : 64); }
+#ifndef NGIA_LDS_THREADS
+#define NGIA_LDS_THREADS 64
+#endif
+__host__ __device__ constexpr int lds_threads(int W) { return W > 0 ? NGIA_LDS_THREADS : 0; }
 __host__ __device__ constexpr size_t lds_smem_bytes(int W) {
   return (size_t)lds_threads(W) * 16 * W * 4;
 }

@@ -8,16 +8,16 @@
 //   with H Wang's 32-bit integer hash followed by two extra xor-shift-multiply
 //   rounds (the steps below), minimum 0xFFFFFFFF when nothing is signed.
 //
-// Mapping: one warp per record; 8 lanes share each run of positions and
-// split the 64 bands between them, 4 such runs per record; two shuffles per
-// band combine the runs.  Records are in length-descending index order, so
-// the longest are scheduled first.
+// Mapping: one warp per record; each lane signs a contiguous run of the
+// positions and keeps all 64 running minima in registers (64 independent
+// hash chains per position), then one redux.sync min per band combines the
+// lanes.  Records are in length-descending index order, so the longest are
+// scheduled first.
 //
-// The work is integer-ALU bound: 64 hashes per position against half a byte
-// read.  The integer ALU pipe retires 64 lanes per clock per SM while the
-// multiply-add pipe would otherwise sit idle, so every shift of the hash is
-// written as a multiply-high (x >> k == mulhi(x, 2^(32-k))) and every
-// multiply stays a multiply; the ALU keeps only the xors and the minimum.
+// The work is integer-bound: 64 hashes of 13 integer instructions per
+// position against half a byte read.  On this GPU the logic/shift pipe and
+// the integer multiply-add pipe draw on the same integer issue budget, and a
+// multiply-high costs two of its slots, so the shifts stay shifts.
 #include "kernels.cuh"
 
 namespace ngia {
@@ -30,31 +30,13 @@ __host__ __device__ constexpr uint32_t band_seed_fold(uint32_t band) {
          ((band * 0x9e3779b1u + 0x85ebca6bu) >> 16);
 }
 
-template <uint32_t K>
-__device__ __forceinline__ uint32_t shr_mul(uint32_t x) {  // x >> K on the multiply pipe
-#ifdef NGIA_SKETCH_ALU_SHIFTS
-  return x >> K;
-#else
-  uint32_t r;
-  asm("mul.hi.u32 %0, %1, %2;" : "=r"(r) : "r"(x), "n"(1u << (32 - K)));
-  return r;
-#endif
-}
-
-template <uint32_t C>
-__device__ __forceinline__ uint32_t mul_const(uint32_t x) {
-  uint32_t r;
-  asm("mul.lo.u32 %0, %1, %2;" : "=r"(r) : "r"(x), "n"(C));
-  return r;
-}
-
 __device__ __forceinline__ uint32_t band_hash_tail(uint32_t x) {
-  x = mul_const<9u>(x);  // x + (x << 3)
-  x ^= shr_mul<4>(x);
-  x = mul_const<0x27d4eb2du>(x);
-  x ^= shr_mul<15>(x);
-  x = mul_const<0x9e3779b1u>(x ^ shr_mul<8>(x));
-  x ^= shr_mul<14>(x);
+  x = x * 9u;  // x + (x << 3)
+  x ^= x >> 4;
+  x *= 0x27d4eb2du;
+  x ^= x >> 15;
+  x = (x ^ (x >> 8)) * 0x9e3779b1u;
+  x ^= x >> 14;
   return x;
 }
 
@@ -108,56 +90,47 @@ struct NibbleKmers {
   }
 };
 
-// Lane layout inside the warp of one record: lane = 8 * part + group; the 8
-// groups split the 64 bands (8 each), the 4 parts split the signed positions
-// into contiguous runs.  Few registers per lane (8 minima), so the SM holds
-// its full complement of warps to hide the hash chains' latency.
-constexpr int kBandGroups = 8, kBandsPerLane = kBands / kBandGroups, kParts = 32 / kBandGroups;
-
 template <typename Source>
 __global__ void __launch_bounds__(256)
 sketch_kernel(const uint32_t *__restrict__ words, const uint64_t *__restrict__ offs,
               uint32_t n, uint32_t *__restrict__ sigs) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t group = lane % kBandGroups, part = lane / kBandGroups;
-  uint32_t seed[kBandsPerLane];
-#pragma unroll
-  for (int j = 0; j < kBandsPerLane; ++j)
-    seed[j] = band_seed_fold(group * kBandsPerLane + (uint32_t)j);
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint32_t *rec = words + offs[i];
     const uint32_t len = __ldg(rec);
     const uint32_t first = len >= 8 ? 7u : (len > 0 ? len - 1 : 0u);
     const uint32_t span = len - first;  // signed positions
-    const uint32_t per = (span + kParts - 1) / kParts;
-    const uint32_t pb = first + part * per;
+    const uint32_t per = (span + 31u) >> 5;
+    const uint32_t pb = first + lane * per;
     const uint32_t pe = min(pb + per, len);
 
-    uint32_t mn[kBandsPerLane];
+    uint32_t mn[kBands];
 #pragma unroll
-    for (int j = 0; j < kBandsPerLane; ++j) mn[j] = kFull;
+    for (int k = 0; k < kBands; ++k) mn[k] = kFull;
+
     if (pb < pe) {
       Source src = Source::make(rec);
       src.start(pb);
-#pragma unroll 2
       for (uint32_t p = pb; p < pe; ++p) {
         const uint32_t kmer = src.at(p);
-        const uint32_t y = kmer ^ shr_mul<16>(kmer);
+        const uint32_t y = kmer ^ (kmer >> 16);
 #pragma unroll
-        for (int j = 0; j < kBandsPerLane; ++j) mn[j] = min(mn[j], band_hash_tail(y ^ seed[j]));
+        for (int k = 0; k < kBands; ++k)
+          mn[k] = min(mn[k], band_hash_tail(y ^ band_seed_fold((uint32_t)k)));
       }
     }
+    uint32_t lo = kFull, hi = kFull;
 #pragma unroll
-    for (int j = 0; j < kBandsPerLane; ++j) {  // min over the 4 parts
-      mn[j] = min(mn[j], __shfl_xor_sync(kFull, mn[j], 8));
-      mn[j] = min(mn[j], __shfl_xor_sync(kFull, mn[j], 16));
+    for (int k = 0; k < kBands; ++k) {
+      const uint32_t r = __reduce_min_sync(kFull, mn[k]);
+      if ((uint32_t)(k & 31) == lane) {
+        if (k < 32) lo = r;
+        else hi = r;
+      }
     }
-    if (part == 0) {
-#pragma unroll
-      for (int j = 0; j < kBandsPerLane; ++j)
-        sigs[(size_t)(group * kBandsPerLane + j) * n + i] = mn[j];
-    }
+    sigs[(size_t)lane * n + i] = lo;
+    sigs[(size_t)(lane + 32) * n + i] = hi;
   }
 }
 
