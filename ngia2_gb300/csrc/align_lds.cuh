@@ -38,24 +38,31 @@ struct LdsTable {
     for (int c = 1; c < 16; ++c) p[c * kCodeStride] = 0u;
   }
   // masks of one row block from its four bit planes
-  __device__ __forceinline__ void fill(uint32_t s, const uint32_t *rb) const {
-    const uint32_t p0 = __ldg(rb), p1 = __ldg(rb + 1), p2 = __ldg(rb + 2), p3 = __ldg(rb + 3);
-    const uint32_t lo[4] = {~p0 & ~p1, p0 & ~p1, ~p0 & p1, p0 & p1};
-    const uint32_t hi[4] = {~p2 & ~p3, p2 & ~p3, ~p2 & p3, p2 & p3};
+  __device__ __forceinline__ void fill(uint32_t s, const uint4 &pl) const {
+    const uint32_t lo[4] = {~pl.x & ~pl.y, pl.x & ~pl.y, ~pl.x & pl.y, pl.x & pl.y};
+    const uint32_t hi[4] = {~pl.z & ~pl.w, pl.z & ~pl.w, ~pl.z & pl.w, pl.z & pl.w};
     uint32_t *p = slot(s);
 #pragma unroll
     for (int c = 1; c < 16; ++c) p[c * kCodeStride] = lo[c & 3] & hi[c >> 2];
   }
 };
 
+__device__ __forceinline__ uint4 load4(const uint32_t *p) {
+  return make_uint4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
+}
+
 // 32 column steps of one column block with the window rotated by R.
 template <int W, int R>
 __device__ __forceinline__ void lds_columns(uint32_t (&V)[W], const uint32_t *tab,
-                                            const uint32_t *__restrict__ nib) {
+                                            const uint4 &nib) {
+  uint32_t w0 = nib.x, w1 = nib.y, w2 = nib.z, w3 = nib.w;
 #pragma unroll 1
   for (int q = 0; q < 4; ++q) {
-    uint32_t x = __ldg(nib + q);
-#pragma unroll 4
+    uint32_t x = w0;  // the code words move down one per 8 columns
+    w0 = w1;
+    w1 = w2;
+    w2 = w3;
+#pragma unroll 8
     for (int k = 0; k < 8; ++k) {
       uint32_t code;
       asm("mul.hi.u32 %0, %1, 16;" : "=r"(code) : "r"(x));
@@ -75,20 +82,29 @@ __device__ __forceinline__ void lds_columns(uint32_t (&V)[W], const uint32_t *ta
   }
 }
 
+// Rows entering the band at this column block, with the planes of the one
+// row that was prefetched during the previous block.
+struct Entering {
+  uint32_t act;     // rows loaded so far
+  uint32_t j1;      // rows to have loaded after this block
+  uint32_t pf_row;  // row whose planes are in pf
+  uint4 pf;
+};
+
 // One column block at rotation R: retire the row leaving the band, load the
 // rows entering it, then the 32 column steps.
 template <int W, int R>
 __device__ __forceinline__ void lds_block(uint32_t (&V)[W], const LdsTable<W> &tab,
-                                          const uint32_t *__restrict__ rep,
-                                          const uint32_t *__restrict__ nib, bool retire,
-                                          uint32_t &act, uint32_t j1, uint32_t &lcs) {
+                                          const uint32_t *__restrict__ rep, const uint4 &nib,
+                                          bool retire, Entering &in, uint32_t &lcs) {
   if (retire) {
     constexpr int out = (R + W - 1) % W;
     lcs += __popc(~V[out]);
     V[out] = kFull;
     tab.clear(out);
   }
-  for (; act < j1; ++act) tab.fill(act % W, rep + 1 + 4 * act);
+  for (; in.act < in.j1; ++in.act)
+    tab.fill(in.act % W, in.act == in.pf_row ? in.pf : load4(rep + 1 + 4 * in.act));
   lds_columns<W, R>(V, tab.base, nib);
 }
 
@@ -96,19 +112,21 @@ template <int W, int R = 0>
 __device__ __forceinline__ void lds_dispatch(uint32_t rot, uint32_t (&V)[W],
                                              const LdsTable<W> &tab,
                                              const uint32_t *__restrict__ rep,
-                                             const uint32_t *__restrict__ nib, bool retire,
-                                             uint32_t &act, uint32_t j1, uint32_t &lcs) {
+                                             const uint4 &nib, bool retire, Entering &in,
+                                             uint32_t &lcs) {
   if constexpr (R < W) {
     if (rot == R) {
-      lds_block<W, R>(V, tab, rep, nib, retire, act, j1, lcs);
+      lds_block<W, R>(V, tab, rep, nib, retire, in, lcs);
       return;
     }
-    lds_dispatch<W, R + 1>(rot, V, tab, rep, nib, retire, act, j1, lcs);
+    lds_dispatch<W, R + 1>(rot, V, tab, rep, nib, retire, in, lcs);
   }
 }
 
 // LCS of the banded computation; requires b.width <= W.  tar_nib points at
-// the target's nibble words (position 8k..8k+7 in word k).
+// the target's nibble words (position 8k..8k+7 in word k).  The next column
+// block's code words and the next entering row's planes are loaded one block
+// ahead so that their latency hides behind the current block's steps.
 template <int W>
 __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
                                    const uint32_t *__restrict__ tar_nib, const Band &b,
@@ -121,11 +139,25 @@ __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
   uint32_t V[W];
 #pragma unroll
   for (int m = 0; m < W; ++m) V[m] = kFull;
-  uint32_t lcs = 0, act = 0;
+  uint32_t lcs = 0;
+  Entering in{0u, 0u, kFull, make_uint4(0u, 0u, 0u, 0u)};
+  uint4 cur = b.nc ? load4(tar_nib) : make_uint4(0u, 0u, 0u, 0u);
   for (uint32_t i = 0; i < b.nc; ++i) {
     const uint32_t j0 = i > b.ls ? i - b.ls : 0;
-    const uint32_t j1 = (i + b.rs < b.nr) ? i + b.rs : b.nr;
-    lds_dispatch<W>(j0 % W, V, tab, rep, tar_nib + 4 * i, i > b.ls, act, j1, lcs);
+    in.j1 = (i + b.rs < b.nr) ? i + b.rs : b.nr;
+    const uint32_t j1n = (i + 1 + b.rs < b.nr) ? i + 1 + b.rs : b.nr;
+    const bool more = i + 1 < b.nc;
+    const uint4 nxt = more ? load4(tar_nib + 4 * (i + 1)) : cur;
+    uint4 pf_next = in.pf;
+    uint32_t pf_row_next = in.pf_row;
+    if (more && j1n > in.j1) {
+      pf_row_next = j1n - 1;
+      pf_next = load4(rep + 1 + 4 * pf_row_next);
+    }
+    lds_dispatch<W>(j0 % W, V, tab, rep, cur, i > b.ls, in, lcs);
+    cur = nxt;
+    in.pf = pf_next;
+    in.pf_row = pf_row_next;
   }
 #pragma unroll
   for (int m = 0; m < W; ++m) lcs += __popc(~V[m]);
