@@ -100,11 +100,16 @@ def make_database(n_seqs: int, n_families: int, seed: int, workdir: Path):
     import ngia2_gb300 as ng
     from ngia2_gb300 import synth
     t0 = time.time()
-    s = synth.dna_families(n_seqs, n_families, seed)
+    # NGIA_BENCH_CACHE=<dir> keeps the generated workload between runs
+    cache = os.environ.get("NGIA_BENCH_CACHE")
+    if cache:
+        workdir = Path(cache) / f"dna_{n_seqs}_{n_families}_{seed}"
+        workdir.mkdir(parents=True, exist_ok=True)
     fasta = workdir / "workload.fa"
-    s.write_fasta(fasta)
     packed = workdir / "workload.packed"
-    ng.makedb(fasta, packed)
+    if not (cache and fasta.exists() and packed.exists()):
+        synth.dna_families(n_seqs, n_families, seed).write_fasta(fasta)
+        ng.makedb(fasta, packed)
     db = ng.read_packed(packed)
     log(f"workload: {db['n']} sequences, {int(db['lens'].sum())} residues "
         f"({time.time() - t0:.1f} s to generate + makedb)")

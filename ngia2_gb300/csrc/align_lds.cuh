@@ -25,7 +25,16 @@
 
 #include "align.cuh"
 
+#ifndef NGIA_LDS_UNROLL
+#define NGIA_LDS_UNROLL 4  // column steps unrolled per loop trip
+#endif
+#ifndef NGIA_LDS_PREFETCH
+#define NGIA_LDS_PREFETCH 1  // load the next block's words one block ahead
+#endif
+
 namespace ngia {
+
+constexpr int kLdsUnroll = NGIA_LDS_UNROLL;
 
 template <int W>
 struct LdsTable {
@@ -62,7 +71,7 @@ __device__ __forceinline__ void lds_columns(uint32_t (&V)[W], const uint32_t *ta
     w0 = w1;
     w1 = w2;
     w2 = w3;
-#pragma unroll 8
+#pragma unroll kLdsUnroll
     for (int k = 0; k < 8; ++k) {
       uint32_t code;
       asm("mul.hi.u32 %0, %1, 16;" : "=r"(code) : "r"(x));
@@ -146,7 +155,7 @@ __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
     const uint32_t j0 = i > b.ls ? i - b.ls : 0;
     in.j1 = (i + b.rs < b.nr) ? i + b.rs : b.nr;
     const uint32_t j1n = (i + 1 + b.rs < b.nr) ? i + 1 + b.rs : b.nr;
-    const bool more = i + 1 < b.nc;
+    const bool more = NGIA_LDS_PREFETCH && i + 1 < b.nc;
     const uint4 nxt = more ? load4(tar_nib + 4 * (i + 1)) : cur;
     uint4 pf_next = in.pf;
     uint32_t pf_row_next = in.pf_row;
@@ -154,6 +163,7 @@ __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
       pf_row_next = j1n - 1;
       pf_next = load4(rep + 1 + 4 * pf_row_next);
     }
+    if (!NGIA_LDS_PREFETCH) cur = load4(tar_nib + 4 * i);
     lds_dispatch<W>(j0 % W, V, tab, rep, cur, i > b.ls, in, lcs);
     cur = nxt;
     in.pf = pf_next;
