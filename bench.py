@@ -43,7 +43,9 @@ N_SEQS, N_FAMILIES, SEED = 200_000, 20_000, 2
 WORKLOAD = "dna_200k_seqs_20k_families_id95_64bands"
 DATA = ("synthetic: seeded DNA families (uniform roots 200-3000 nt, GC 0.45, 1-10% subs, "
         "1% indels mean 2), 10 members per family")
-ALIGN_OPS_PER_WORD_STEP = 5  # AND, add with carry in, carry out, and-not, or
+# Irreducible integer work of the bit-parallel LCS update per 32 cells (one
+# row word, one column): t = V & M; s = V + t + carry; V = s | (V ^ t).
+ALIGN_OPS_PER_WORD_STEP = 3
 
 
 def log(*a):

@@ -82,16 +82,17 @@ align_class_kernel(const uint32_t *__restrict__ packed,
 }
 
 // Batched form, shared-memory table kernel (align_lds.cuh).
-template <int W>
+template <int W, int K>
 __global__ void __launch_bounds__(lds_threads(W))
 align_lds_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
-                 const uint64_t *__restrict__ offs, const uint2 *__restrict__ pairs,
-                 const uint32_t *__restrict__ order, uint32_t begin, uint32_t end,
-                 uint32_t *__restrict__ scores, float t, int fma_mode) {
+                 uint64_t inv, const uint64_t *__restrict__ offs,
+                 const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,
+                 uint32_t begin, uint32_t end, uint32_t *__restrict__ scores, float t,
+                 int fma_mode) {
   extern __shared__ uint32_t smem[];
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= end) return;
-  LdsTable<W> tab{smem + (threadIdx.x >> 5) * (16 * W * 32) + (threadIdx.x & 31u)};
+  const LdsTable<W, K> tab{smem + (threadIdx.x >> 5) * (K * W * 32) + (threadIdx.x & 31u), inv};
   const uint32_t p = order[k];
   const uint2 pr = pairs[p];
   const uint32_t *rep = packed + offs[pr.x];
@@ -107,7 +108,11 @@ align_lds_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict
 // record in nibble 7 - j of word k).  The length word is copied.
 __global__ void __launch_bounds__(256)
 nibble_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
-              uint32_t n, uint32_t *__restrict__ nib) {
+              uint32_t n, uint32_t *__restrict__ nib, uint32_t *__restrict__ presence) {
+  __shared__ uint32_t seen;
+  if (threadIdx.x == 0) seen = 0;
+  __syncthreads();
+  uint32_t mine = 0;  // bit c set when code c occurs
   for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
     const uint64_t o = offs[i];
     const uint32_t len = packed[o];
@@ -124,32 +129,81 @@ nibble_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ 
         for (int j = 0; j < 8; ++j) out |= ((byte >> j) & 1u) << (28 - 4 * j + e);
       }
       nib[o + 1 + w] = out;
+      const uint32_t valid = len - 8 * w < 8 ? len - 8 * w : 8;  // codes of real residues
+#pragma unroll
+      for (uint32_t j = 0; j < 8; ++j)
+        if (j < valid) mine |= 1u << ((out >> (28 - 4 * j)) & 15u);
+    }
+  }
+  if (mine) atomicOr(&seen, mine);
+  __syncthreads();
+  if (threadIdx.x == 0 && seen) atomicOr(presence, seen);
+}
+
+// Rewrites nibble codes through a 16-entry map (map nibble c = new code of c).
+__global__ void __launch_bounds__(256)
+recode_kernel(const uint32_t *__restrict__ nib, const uint64_t *__restrict__ offs, uint32_t n,
+              uint64_t map, uint32_t *__restrict__ out) {
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const uint64_t o = offs[i];
+    const uint32_t len = nib[o];
+    if (threadIdx.x == 0) out[o] = len;
+    const uint32_t words = ((len + 31) >> 5) * 4;
+    for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) {
+      const uint32_t x = nib[o + 1 + w];
+      uint32_t y = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) y |= (uint32_t)((map >> (4 * ((x >> (4 * j)) & 15u))) & 15u) << (4 * j);
+      out[o + 1 + w] = y;
     }
   }
 }
 
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
-                   cudaStream_t s) {
+                   uint32_t *presence, cudaStream_t s) {
   if (n == 0) return NGIA_OK;
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t cap = (uint32_t)sms * 16;
-  nibble_kernel<<<n < cap ? n : cap, 256, 0, s>>>(packed, offs, n, nib);
+  NGIA_CUDA(cudaMemsetAsync(presence, 0, sizeof(uint32_t), s));
+  nibble_kernel<<<n < cap ? n : cap, 256, 0, s>>>(packed, offs, n, nib, presence);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
+                  uint32_t *out, cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t cap = (uint32_t)sms * 16;
+  recode_kernel<<<n < cap ? n : cap, 256, 0, s>>>(nib, offs, n, map, out);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
 
 template <int W>
-static int launch_lds(const uint32_t *packed, const uint32_t *nib, const uint64_t *offs,
-                      const uint2 *pairs, const uint32_t *order, uint32_t begin, uint32_t end,
-                      uint32_t *scores, float t, int fm, cudaStream_t s) {
+static int launch_lds(const uint32_t *packed, const uint32_t *nib, const Alphabet &ab,
+                      const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
+                      uint32_t begin, uint32_t end, uint32_t *scores, float t, int fm,
+                      cudaStream_t s) {
   constexpr int T = lds_threads(W);
-  constexpr size_t smem = lds_smem_bytes(W);
-  NGIA_CUDA(cudaFuncSetAttribute(align_lds_kernel<W>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  align_lds_kernel<W><<<ceil_div(end - begin, (uint32_t)T), T, smem, s>>>(
-      packed, nib, offs, pairs, order, begin, end, scores, t, fm);
+  const uint32_t blocks = ceil_div(end - begin, (uint32_t)T);
+  if (ab.K == 8) {
+    constexpr size_t smem = lds_smem_bytes(W, 8);
+    NGIA_CUDA(cudaFuncSetAttribute(align_lds_kernel<W, 8>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    align_lds_kernel<W, 8><<<blocks, T, smem, s>>>(packed, nib, ab.inv, offs, pairs, order,
+                                                   begin, end, scores, t, fm);
+  } else {
+    constexpr size_t smem = lds_smem_bytes(W, 16);
+    NGIA_CUDA(cudaFuncSetAttribute(align_lds_kernel<W, 16>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    align_lds_kernel<W, 16><<<blocks, T, smem, s>>>(packed, nib, ab.inv, offs, pairs, order,
+                                                    begin, end, scores, t, fm);
+  }
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
@@ -176,21 +230,24 @@ int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
 }
 
 int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
-                       const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
-                       uint32_t begin, uint32_t end, uint32_t *scores, uint32_t identity,
-                       cudaStream_t s) {
+                       const Alphabet &ab, const uint64_t *offs, const uint2 *pairs,
+                       const uint32_t *order, uint32_t begin, uint32_t end,
+                       uint32_t *scores, uint32_t identity, cudaStream_t s) {
   if (end <= begin) return NGIA_OK;
   const float t = identity_threshold(identity);
   const int fm = round_mode();
   const uint32_t blocks = ceil_div(end - begin, 128u);
+#define NGIA_LDS_CASE(C, W) \
+  case C: return launch_lds<W>(packed, nib, ab, offs, pairs, order, begin, end, scores, t, fm, s);
   switch (cls) {
-    case 0: return launch_lds<4>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
-    case 1: return launch_lds<6>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
-    case 2: return launch_lds<8>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
-    case 3: return launch_lds<10>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
-    case 4: return launch_lds<12>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
-    case 5: return launch_lds<14>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
-    case 6: return launch_lds<16>(packed, nib, offs, pairs, order, begin, end, scores, t, fm, s);
+    NGIA_LDS_CASE(0, 4)
+    NGIA_LDS_CASE(1, 6)
+    NGIA_LDS_CASE(2, 8)
+    NGIA_LDS_CASE(3, 10)
+    NGIA_LDS_CASE(4, 12)
+    NGIA_LDS_CASE(5, 14)
+    NGIA_LDS_CASE(6, 16)
+#undef NGIA_LDS_CASE
     case 7: align_class_kernel<24><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
     case 8: align_class_kernel<32><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
     case kGeneralClass: align_class_kernel<0><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;

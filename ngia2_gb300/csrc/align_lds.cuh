@@ -29,30 +29,44 @@
 #define NGIA_LDS_UNROLL 4  // column steps unrolled per loop trip
 #endif
 #ifndef NGIA_LDS_PREFETCH
-#define NGIA_LDS_PREFETCH 1  // load the next block's words one block ahead
+#define NGIA_LDS_PREFETCH 0  // 1: load the next block's words one block ahead
 #endif
 
 namespace ngia {
 
 constexpr int kLdsUnroll = NGIA_LDS_UNROLL;
 
-template <int W>
+// K = entries per row block: 16 (all residue codes) or 8 when the database
+// uses at most 7 nonzero codes and the targets were recoded densely (the
+// table, and so the shared memory per thread, halves; nucleotides).
+template <int W, int K = 16>
 struct LdsTable {
   uint32_t *base;  // this thread's column of the warp's table
+  uint64_t inv;    // nibble d = residue code that aligner code d stands for
   __device__ __forceinline__ uint32_t *slot(uint32_t s) const { return base + s * 32; }
   static constexpr uint32_t kCodeStride = W * 32;  // words between codes
   __device__ __forceinline__ void clear(uint32_t s) const {
     uint32_t *p = slot(s);
 #pragma unroll
-    for (int c = 1; c < 16; ++c) p[c * kCodeStride] = 0u;
+    for (int c = 1; c < K; ++c) p[c * kCodeStride] = 0u;
   }
   // masks of one row block from its four bit planes
   __device__ __forceinline__ void fill(uint32_t s, const uint4 &pl) const {
-    const uint32_t lo[4] = {~pl.x & ~pl.y, pl.x & ~pl.y, ~pl.x & pl.y, pl.x & pl.y};
-    const uint32_t hi[4] = {~pl.z & ~pl.w, pl.z & ~pl.w, ~pl.z & pl.w, pl.z & pl.w};
     uint32_t *p = slot(s);
+    if constexpr (K == 16) {
+      const uint32_t lo[4] = {~pl.x & ~pl.y, pl.x & ~pl.y, ~pl.x & pl.y, pl.x & pl.y};
+      const uint32_t hi[4] = {~pl.z & ~pl.w, pl.z & ~pl.w, ~pl.z & pl.w, pl.z & pl.w};
 #pragma unroll
-    for (int c = 1; c < 16; ++c) p[c * kCodeStride] = lo[c & 3] & hi[c >> 2];
+      for (int c = 1; c < 16; ++c) p[c * kCodeStride] = lo[c & 3] & hi[c >> 2];
+    } else {
+#pragma unroll
+      for (int d = 1; d < K; ++d) {
+        const uint32_t c = (uint32_t)(inv >> (4 * d)) & 15u;
+        p[d * kCodeStride] = ((c & 1u) ? pl.x : ~pl.x) & ((c & 2u) ? pl.y : ~pl.y) &
+                             ((c & 4u) ? pl.z : ~pl.z) & ((c & 8u) ? pl.w : ~pl.w) &
+                             (c ? kFull : 0u);
+      }
+    }
   }
 };
 
@@ -102,8 +116,8 @@ struct Entering {
 
 // One column block at rotation R: retire the row leaving the band, load the
 // rows entering it, then the 32 column steps.
-template <int W, int R>
-__device__ __forceinline__ void lds_block(uint32_t (&V)[W], const LdsTable<W> &tab,
+template <int W, int R, typename Tab>
+__device__ __forceinline__ void lds_block(uint32_t (&V)[W], const Tab &tab,
                                           const uint32_t *__restrict__ rep, const uint4 &nib,
                                           bool retire, Entering &in, uint32_t &lcs) {
   if (retire) {
@@ -117,9 +131,8 @@ __device__ __forceinline__ void lds_block(uint32_t (&V)[W], const LdsTable<W> &t
   lds_columns<W, R>(V, tab.base, nib);
 }
 
-template <int W, int R = 0>
-__device__ __forceinline__ void lds_dispatch(uint32_t rot, uint32_t (&V)[W],
-                                             const LdsTable<W> &tab,
+template <int W, typename Tab, int R = 0>
+__device__ __forceinline__ void lds_dispatch(uint32_t rot, uint32_t (&V)[W], const Tab &tab,
                                              const uint32_t *__restrict__ rep,
                                              const uint4 &nib, bool retire, Entering &in,
                                              uint32_t &lcs) {
@@ -128,7 +141,7 @@ __device__ __forceinline__ void lds_dispatch(uint32_t rot, uint32_t (&V)[W],
       lds_block<W, R>(V, tab, rep, nib, retire, in, lcs);
       return;
     }
-    lds_dispatch<W, R + 1>(rot, V, tab, rep, nib, retire, in, lcs);
+    lds_dispatch<W, Tab, R + 1>(rot, V, tab, rep, nib, retire, in, lcs);
   }
 }
 
@@ -136,10 +149,10 @@ __device__ __forceinline__ void lds_dispatch(uint32_t rot, uint32_t (&V)[W],
 // the target's nibble words (position 8k..8k+7 in word k).  The next column
 // block's code words and the next entering row's planes are loaded one block
 // ahead so that their latency hides behind the current block's steps.
-template <int W>
+template <int W, typename Tab>
 __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
                                    const uint32_t *__restrict__ tar_nib, const Band &b,
-                                   const LdsTable<W> &tab) {
+                                   const Tab &tab) {
 #pragma unroll 1
   for (uint32_t s = 0; s < (uint32_t)W; ++s) {
     tab.clear(s);
@@ -180,8 +193,8 @@ __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
 #define NGIA_LDS_THREADS 64
 #endif
 __host__ __device__ constexpr int lds_threads(int W) { return W > 0 ? NGIA_LDS_THREADS : 0; }
-__host__ __device__ constexpr size_t lds_smem_bytes(int W) {
-  return (size_t)lds_threads(W) * 16 * W * 4;
+__host__ __device__ constexpr size_t lds_smem_bytes(int W, int K) {
+  return (size_t)lds_threads(W) * K * W * 4;
 }
 
 }  // namespace ngia

@@ -63,6 +63,11 @@ struct ngia_ctx {
   uint64_t packed_words = 0;
   uint32_t rep_bands = 0;
   ngia::DevBuf packed, nib, offs, lens, rep, sigs;
+  // targets as the aligner reads them: densely recoded when the database uses
+  // at most 7 nonzero residue codes (aligner tables of 8 entries), else `nib`
+  ngia::DevBuf nib_dense, presence;
+  const uint32_t *align_nib = nullptr;
+  ngia::Alphabet ab{16, 0xFEDCBA9876543210ull};
   // graph build work
   ngia::DevBuf ucount, uoff, counters, pairs, scores, cls, cls_sorted, order, sort_tmp,
       emit_tmp, edges, scan_tmp, jobs;
@@ -159,7 +164,7 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   for (int k = 0; k < kNumClasses; ++k) begin[k + 1] = begin[k] + hc.class_count[k];
   const int launch_order[] = {kGeneralClass, 8, 7, 6, 5, 4, 3, 2, 1, 0};
   for (int cl : launch_order)
-    NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->nib.as<uint32_t>(),
+    NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->align_nib, c->ab,
                                 c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
                                 begin[cl], begin[cl + 1], scores, identity, s));
   NGIA_CUDA(cudaEventRecord(c->ev[2], s));
@@ -228,8 +233,32 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
   NGIA_CUDA(cudaMemcpyAsync(c->offs.p, h_offs, (size_t)n * 8, cudaMemcpyHostToDevice, s));
   NGIA_CUDA(cudaMemcpyAsync(c->lens.p, h_lens, (size_t)n * 4, cudaMemcpyHostToDevice, s));
   NGIA_TRY(c->nib.reserve(words * 4));
+  NGIA_TRY(c->presence.reserve(sizeof(uint32_t)));
   NGIA_TRY(launch_nibbles(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), n,
-                          c->nib.as<uint32_t>(), s));
+                          c->nib.as<uint32_t>(), c->presence.as<uint32_t>(), s));
+  uint32_t present = 0;
+  NGIA_CUDA(cudaMemcpyAsync(&present, c->presence.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  // Dense recoding of the residue codes in use (code 0 stays 0): equality of
+  // codes, all the aligner looks at, is unchanged by a bijection.
+  c->align_nib = c->nib.as<uint32_t>();
+  c->ab = Alphabet{16, 0xFEDCBA9876543210ull};
+  if (__builtin_popcount(present & ~1u) <= 7) {
+    uint64_t map = 0, inv = 0;
+    int next = 1;
+    for (int code = 1; code < 16; ++code) {
+      if (!((present >> code) & 1u)) continue;
+      map |= (uint64_t)next << (4 * code);
+      inv |= (uint64_t)code << (4 * next);
+      ++next;
+    }
+    NGIA_TRY(c->nib_dense.reserve(words * 4));
+    NGIA_TRY(launch_recode(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), n, map,
+                           c->nib_dense.as<uint32_t>(), s));
+    c->align_nib = c->nib_dense.as<uint32_t>();
+    c->ab = Alphabet{8, inv};
+  }
   c->n = n;
   c->packed_words = words;
   c->rep_bands = 0;
@@ -297,7 +326,7 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
 void ngia_ctx_destroy(ngia_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  ngia::DevBuf *bufs[] = {&c->packed, &c->nib, &c->offs,  &c->lens,       &c->rep,    &c->sigs,
+  ngia::DevBuf *bufs[] = {&c->packed, &c->nib, &c->nib_dense, &c->presence, &c->offs,  &c->lens,       &c->rep,    &c->sigs,
                           &c->ucount, &c->uoff,  &c->counters,   &c->pairs,  &c->scores,
                           &c->cls,    &c->cls_sorted, &c->order, &c->sort_tmp,
                           &c->emit_tmp, &c->edges, &c->scan_tmp, &c->jobs};

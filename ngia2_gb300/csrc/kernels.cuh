@@ -34,12 +34,21 @@ int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
                                 uint32_t *jobs, const uint32_t *d_count,
                                 uint32_t max_count, uint32_t identity,
                                 cudaStream_t s);
+// Alphabet of the target codes the aligner reads: codes 1..K-1 in use;
+// inv packs, per code d < K, the residue code whose match mask d stands for
+// (identity when the codes were not recoded).
+struct Alphabet {
+  int K;         // 8 or 16 table entries per row block
+  uint64_t inv;  // nibble d = residue code of aligner code d
+};
 int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
-                       const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
-                       uint32_t begin, uint32_t end, uint32_t *scores, uint32_t identity,
-                       cudaStream_t s);
+                       const Alphabet &ab, const uint64_t *offs, const uint2 *pairs,
+                       const uint32_t *order, uint32_t begin, uint32_t end,
+                       uint32_t *scores, uint32_t identity, cudaStream_t s);
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
-                   cudaStream_t s);
+                   uint32_t *presence, cudaStream_t s);
+int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
+                  uint32_t *out, cudaStream_t s);
 
 // pairs.cu
 int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
