@@ -143,6 +143,10 @@ typedef struct ngia_stats {
   uint64_t aligned_cells;   /* 1024 x 32x32 blocks visited over unique pairs */
   uint64_t edges;           /* emitted edges (sorted, unique) */
   double ms_sketch, ms_bucket, ms_pairs, ms_align, ms_emit; /* device time */
+  uint64_t computed_cells;  /* cells the aligners updated: window words (a
+                               little wider than the band) times the column
+                               blocks processed before a pair's score was
+                               settled (see the early exit in common.cuh) */
 } ngia_stats;
 
 int ngia_ctx_create(ngia_ctx **ctx, void *stream);

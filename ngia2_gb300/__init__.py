@@ -48,7 +48,8 @@ class Stats(C.Structure):
     _fields_ = [("candidate_pairs", C.c_uint64), ("unique_pairs", C.c_uint64),
                 ("aligned_cells", C.c_uint64), ("edges", C.c_uint64),
                 ("ms_sketch", C.c_double), ("ms_bucket", C.c_double),
-                ("ms_pairs", C.c_double), ("ms_align", C.c_double), ("ms_emit", C.c_double)]
+                ("ms_pairs", C.c_double), ("ms_align", C.c_double), ("ms_emit", C.c_double),
+                ("computed_cells", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

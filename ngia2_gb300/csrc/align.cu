@@ -11,10 +11,17 @@ namespace ngia {
 // src/buildGraph.hpp:323).  The window width is picked per pair at run time.
 __device__ __forceinline__ uint32_t lcs_any(const uint32_t *rep, const uint32_t *tar,
                                             const Band &b, uint32_t *lines) {
-  if (b.width <= 4) return lcs_window<4>(rep, tar, b);
-  if (b.width <= 8) return lcs_window<8>(rep, tar, b);
-  if (b.width <= 16) return lcs_window<16>(rep, tar, b);
-  return lcs_general(rep, tar, b, lines);
+  uint32_t blocks;
+  if (b.width <= 4) return lcs_window<4>(rep, tar, b, blocks);
+  if (b.width <= 8) return lcs_window<8>(rep, tar, b, blocks);
+  if (b.width <= 16) return lcs_window<16>(rep, tar, b, blocks);
+  return lcs_general(rep, tar, b, lines, blocks);
+}
+
+// Adds the warp's computed 32x32 blocks (row words x column blocks) to *work.
+__device__ __forceinline__ void count_work(uint32_t blocks, unsigned long long *work) {
+  const uint32_t sum = __reduce_add_sync(kFull, blocks);
+  if ((threadIdx.x & 31u) == 0 && sum) atomicAdd(work, (unsigned long long)sum);
 }
 
 __global__ void __launch_bounds__(128)
@@ -62,23 +69,29 @@ __global__ void __launch_bounds__(128)
 align_class_kernel(const uint32_t *__restrict__ packed,
                    const uint64_t *__restrict__ offs, const uint2 *__restrict__ pairs,
                    const uint32_t *__restrict__ order, uint32_t begin, uint32_t end,
-                   uint32_t *__restrict__ scores, float t, int fma_mode) {
+                   uint32_t *__restrict__ scores, float t, int fma_mode,
+                   unsigned long long *__restrict__ work) {
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= end) return;
-  const uint32_t p = order[k];
-  const uint2 pr = pairs[p];
-  const uint32_t *rep = packed + offs[pr.x];
-  const uint32_t *tar = packed + offs[pr.y];
-  const uint32_t lr = __ldg(rep), lt = __ldg(tar);
-  const Band b = make_band(lr, lt, t, fma_mode);
-  uint32_t lcs;
-  if constexpr (W > 0) {
-    lcs = lcs_window<W>(rep, tar, b);
-  } else {
-    uint32_t lines[kMaxRowBlocks];
-    lcs = lcs_general(rep, tar, b, lines);
+  uint32_t done = 0;
+  if (k < end) {
+    const uint32_t p = order[k];
+    const uint2 pr = pairs[p];
+    const uint32_t *rep = packed + offs[pr.x];
+    const uint32_t *tar = packed + offs[pr.y];
+    const uint32_t lr = __ldg(rep), lt = __ldg(tar);
+    const Band b = make_band(lr, lt, t, fma_mode);
+    uint32_t lcs, blocks;
+    if constexpr (W > 0) {
+      lcs = lcs_window<W>(rep, tar, b, blocks);
+      done = blocks * W;
+    } else {
+      uint32_t lines[kMaxRowBlocks];
+      lcs = lcs_general(rep, tar, b, lines, blocks);
+      done = blocks * ((b.width + 7u) & ~7u);
+    }
+    scores[p] = identity_score(lcs, lr, lt, t);
   }
-  scores[p] = identity_score(lcs, lr, lt, t);
+  count_work(done, work);
 }
 
 // Batched form, shared-memory table kernel (align_lds.cuh).
@@ -88,19 +101,25 @@ align_lds_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict
                  uint64_t inv, const uint64_t *__restrict__ offs,
                  const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,
                  uint32_t begin, uint32_t end, uint32_t *__restrict__ scores, float t,
-                 int fma_mode) {
+                 int fma_mode, unsigned long long *__restrict__ work) {
   extern __shared__ uint32_t smem[];
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= end) return;
-  const LdsTable<W, K> tab{smem + (threadIdx.x >> 5) * (K * W * 32) + (threadIdx.x & 31u), inv};
-  const uint32_t p = order[k];
-  const uint2 pr = pairs[p];
-  const uint32_t *rep = packed + offs[pr.x];
-  const uint64_t to = offs[pr.y];
-  const uint32_t lr = __ldg(rep), lt = __ldg(packed + to);
-  const Band b = make_band(lr, lt, t, fma_mode);
-  const uint32_t lcs = lcs_lds<W>(rep, nib + to + 1, b, tab);
-  scores[p] = identity_score(lcs, lr, lt, t);
+  uint32_t done = 0;
+  if (k < end) {
+    const LdsTable<W, K> tab{smem + (threadIdx.x >> 5) * (K * W * 32) + (threadIdx.x & 31u),
+                             inv};
+    const uint32_t p = order[k];
+    const uint2 pr = pairs[p];
+    const uint32_t *rep = packed + offs[pr.x];
+    const uint64_t to = offs[pr.y];
+    const uint32_t lr = __ldg(rep), lt = __ldg(packed + to);
+    const Band b = make_band(lr, lt, t, fma_mode);
+    uint32_t blocks;
+    const uint32_t lcs = lcs_lds<W>(rep, nib + to + 1, b, tab, blocks);
+    scores[p] = identity_score(lcs, lr, lt, t);
+    done = blocks * W;
+  }
+  count_work(done, work);
 }
 
 // Planes -> nibbles: the same record layout, with each block's four plane
@@ -188,7 +207,7 @@ template <int W>
 static int launch_lds(const uint32_t *packed, const uint32_t *nib, const Alphabet &ab,
                       const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
                       uint32_t begin, uint32_t end, uint32_t *scores, float t, int fm,
-                      cudaStream_t s) {
+                      unsigned long long *work, cudaStream_t s) {
   constexpr int T = lds_threads(W);
   const uint32_t blocks = ceil_div(end - begin, (uint32_t)T);
   if (ab.K == 8) {
@@ -196,13 +215,13 @@ static int launch_lds(const uint32_t *packed, const uint32_t *nib, const Alphabe
     NGIA_CUDA(cudaFuncSetAttribute(align_lds_kernel<W, 8>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     align_lds_kernel<W, 8><<<blocks, T, smem, s>>>(packed, nib, ab.inv, offs, pairs, order,
-                                                   begin, end, scores, t, fm);
+                                                   begin, end, scores, t, fm, work);
   } else {
     constexpr size_t smem = lds_smem_bytes(W, 16);
     NGIA_CUDA(cudaFuncSetAttribute(align_lds_kernel<W, 16>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     align_lds_kernel<W, 16><<<blocks, T, smem, s>>>(packed, nib, ab.inv, offs, pairs, order,
-                                                    begin, end, scores, t, fm);
+                                                    begin, end, scores, t, fm, work);
   }
   NGIA_LAUNCHED();
   return NGIA_OK;
@@ -232,13 +251,16 @@ int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
 int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const Alphabet &ab, const uint64_t *offs, const uint2 *pairs,
                        const uint32_t *order, uint32_t begin, uint32_t end,
-                       uint32_t *scores, uint32_t identity, cudaStream_t s) {
+                       uint32_t *scores, uint32_t identity, unsigned long long *work,
+                       cudaStream_t s) {
   if (end <= begin) return NGIA_OK;
   const float t = identity_threshold(identity);
   const int fm = round_mode();
   const uint32_t blocks = ceil_div(end - begin, 128u);
-#define NGIA_LDS_CASE(C, W) \
-  case C: return launch_lds<W>(packed, nib, ab, offs, pairs, order, begin, end, scores, t, fm, s);
+#define NGIA_LDS_CASE(C, W)                                                               \
+  case C:                                                                                 \
+    return launch_lds<W>(packed, nib, ab, offs, pairs, order, begin, end, scores, t, fm, \
+                         work, s);
   switch (cls) {
     NGIA_LDS_CASE(0, 4)
     NGIA_LDS_CASE(1, 6)
@@ -248,9 +270,9 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
     NGIA_LDS_CASE(5, 14)
     NGIA_LDS_CASE(6, 16)
 #undef NGIA_LDS_CASE
-    case 7: align_class_kernel<24><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
-    case 8: align_class_kernel<32><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
-    case kGeneralClass: align_class_kernel<0><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm); break;
+    case 7: align_class_kernel<24><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm, work); break;
+    case 8: align_class_kernel<32><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm, work); break;
+    case kGeneralClass: align_class_kernel<0><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm, work); break;
     default: return NGIA_ERR_ARG;
   }
   NGIA_LAUNCHED();

@@ -127,8 +127,11 @@ __device__ __forceinline__ void window_step(uint32_t (&V)[W], const uint32_t (&P
 
 // LCS of the banded computation, window form; requires b.width <= W.
 template <int W>
+// `blocks` receives the column blocks processed (fewer than b.nc after an
+// early exit).
 __device__ inline uint32_t lcs_window(const uint32_t *__restrict__ rep,
-                               const uint32_t *__restrict__ tar, const Band &b) {
+                                      const uint32_t *__restrict__ tar, const Band &b,
+                                      uint32_t &blocks) {
   uint32_t V[W], P0[W], P1[W], P2[W], P3[W];
 #pragma unroll
   for (int m = 0; m < W; ++m) {
@@ -170,9 +173,17 @@ __device__ inline uint32_t lcs_window(const uint32_t *__restrict__ rep,
     ColumnPlanes col(tar + 1 + 4 * i);
 #pragma unroll 4
     for (int k = 0; k < 32; ++k) window_step<W>(V, P0, P1, P2, P3, col.next());
+    uint32_t z = lcs;
+#pragma unroll
+    for (int m = 0; m < W; ++m) z += __popc(~V[m]);
+    if (!may_reach_threshold(z, 32 * (i + 1), b)) {  // score 0 already certain
+      blocks = i + 1;
+      return 0;
+    }
   }
 #pragma unroll
   for (int m = 0; m < W; ++m) lcs += __popc(~V[m]);
+  blocks = b.nc;
   return lcs;
 }
 
@@ -184,12 +195,17 @@ constexpr uint32_t kMaxRowBlocks = (NGIA_MAX_READ + 31) / 32;  // 2048
 
 __device__ inline uint32_t lcs_general(const uint32_t *__restrict__ rep,
                                 const uint32_t *__restrict__ tar, const Band &b,
-                                uint32_t *lines) {
+                                uint32_t *lines, uint32_t &blocks) {
   for (uint32_t w = 0; w < b.nr; ++w) lines[w] = kFull;
+  uint32_t zeros = 0;  // running LCS: zero bits over all row blocks
   for (uint32_t i = 0; i < b.nc; ++i) {
     const uint32_t j0 = i > b.ls ? i - b.ls : 0;
     const uint32_t j1 = (i + b.rs < b.nr) ? i + b.rs : b.nr;
     const uint32_t *tb = tar + 1 + 4 * i;
+    if (i > 0 && !may_reach_threshold(zeros, 32 * i, b)) {  // score 0 certain
+      blocks = i;
+      return 0;
+    }
     uint32_t cin_word = 0;  // carries into the current chunk, bit k = column k
     for (uint32_t j = j0; j < j1; j += 8) {
       uint32_t V[8], P0[8], P1[8], P2[8], P3[8];
@@ -224,13 +240,15 @@ __device__ inline uint32_t lcs_general(const uint32_t *__restrict__ rep,
       }
 #pragma unroll
       for (int m = 0; m < 8; ++m)
-        if (j + m < j1) lines[j + m] = V[m];
+        if (j + m < j1) {
+          zeros += __popc(~V[m]) - __popc(~lines[j + m]);
+          lines[j + m] = V[m];
+        }
       cin_word = cout_word;
     }
   }
-  uint32_t lcs = 0;
-  for (uint32_t w = 0; w < b.nr; ++w) lcs += __popc(~lines[w]);
-  return lcs;
+  blocks = b.nc;
+  return zeros;
 }
 
 // Width classes of the batched aligner:

@@ -152,7 +152,7 @@ __device__ __forceinline__ void lds_dispatch(uint32_t rot, uint32_t (&V)[W], con
 template <int W, typename Tab>
 __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
                                    const uint32_t *__restrict__ tar_nib, const Band &b,
-                                   const Tab &tab) {
+                                   const Tab &tab, uint32_t &blocks) {
 #pragma unroll 1
   for (uint32_t s = 0; s < (uint32_t)W; ++s) {
     tab.clear(s);
@@ -181,9 +181,17 @@ __device__ inline uint32_t lcs_lds(const uint32_t *__restrict__ rep,
     cur = nxt;
     in.pf = pf_next;
     in.pf_row = pf_row_next;
+    uint32_t z = lcs;
+#pragma unroll
+    for (int m = 0; m < W; ++m) z += __popc(~V[m]);
+    if (!may_reach_threshold(z, 32 * (i + 1), b)) {  // score 0 already certain
+      blocks = i + 1;
+      return 0;
+    }
   }
 #pragma unroll
   for (int m = 0; m < W; ++m) lcs += __popc(~V[m]);
+  blocks = b.nc;
   return lcs;
 }
 

@@ -51,6 +51,8 @@ struct Band {
   uint32_t ls, rs, nr, nc;
   uint32_t width;  // max live row blocks = min(ls + rs, nr)
   bool pass;       // the length filter Lt >= Lr*t (src/buildGraph.hpp:201)
+  uint32_t lr, lt;
+  float t;
 };
 
 __host__ __device__ inline float identity_threshold(uint32_t identity) {
@@ -67,6 +69,9 @@ __host__ __device__ inline uint32_t ceil_to_u32(float v) {
 __host__ __device__ inline Band make_band(uint32_t lr, uint32_t lt, float t,
                                           int fma_mode) {
   Band b;
+  b.lr = lr;
+  b.lt = lt;
+  b.t = t;
   if (lr > NGIA_MAX_READ || lt > NGIA_MAX_READ) {
     // makedb never writes such records; refusing them keeps every row index
     // of the alignment inside its 2048-word bound.
@@ -133,6 +138,21 @@ __host__ __device__ inline uint32_t identity_score(uint32_t lcs, uint32_t lr,
   const bool hit = (float)lcs > (float)den * t;
 #endif
   return hit ? lcs * 100u / den : 0u;
+}
+
+// Early exit.  One column step raises the number of zero bits of the row
+// vector (the running LCS) by at most one, and the score test
+// lcs > (Lr + Lt - lcs) * t is monotone in lcs.  So once
+//   lcs_so_far + columns_left
+// fails the test, the pair's score is 0 whatever the remaining columns hold,
+// and the alignment can stop: the score is exactly the reference's.
+__host__ __device__ inline bool may_reach_threshold(uint32_t lcs_so_far, uint32_t cols_done,
+                                                    const Band &b) {
+  const uint32_t left = b.lt > cols_done ? b.lt - cols_done : 0u;
+  uint32_t ub = lcs_so_far + left;
+  const uint32_t cap = b.lr < b.lt ? b.lr : b.lt;
+  if (ub > cap) ub = cap;
+  return identity_score(ub, b.lr, b.lt, b.t) > 0;
 }
 
 template <typename T>

@@ -82,6 +82,7 @@ struct Counters {  // device-side counters of one graph build
   uint64_t unique_total;
   unsigned int class_count[kNumClasses];
   uint32_t fast_count;
+  unsigned long long work;  // 32x32 blocks the aligners computed
 };
 
 static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
@@ -166,7 +167,7 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   for (int cl : launch_order)
     NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->align_nib, c->ab,
                                 c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
-                                begin[cl], begin[cl + 1], scores, identity, s));
+                                begin[cl], begin[cl + 1], scores, identity, &dc->work, s));
   NGIA_CUDA(cudaEventRecord(c->ev[2], s));
   // 4. emit: compact hits, sort by (rep, tar)
   NGIA_TRY(c->emit_tmp.reserve(emit_scratch_bytes(m, n)));
@@ -178,9 +179,12 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   c->n_edges = ne;
   if (h_n_edges) *h_n_edges = ne;
   if (st) {
+    unsigned long long work = 0;
+    NGIA_CUDA(cudaMemcpy(&work, &dc->work, sizeof(work), cudaMemcpyDeviceToHost));
     st->candidate_pairs = hc.cand_total;
     st->unique_pairs = total;
     st->aligned_cells = hc.cells;
+    st->computed_cells = work * 1024ull;
     st->edges = ne;
     st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
     st->ms_align = ev_ms(c->ev[1], c->ev[2]);

@@ -44,7 +44,8 @@ struct Alphabet {
 int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const Alphabet &ab, const uint64_t *offs, const uint2 *pairs,
                        const uint32_t *order, uint32_t begin, uint32_t end,
-                       uint32_t *scores, uint32_t identity, cudaStream_t s);
+                       uint32_t *scores, uint32_t identity, unsigned long long *work,
+                       cudaStream_t s);
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
                    uint32_t *presence, cudaStream_t s);
 int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
