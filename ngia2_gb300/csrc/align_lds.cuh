@@ -26,10 +26,10 @@
 #include "align.cuh"
 
 #ifndef NGIA_LDS_UNROLL
-#define NGIA_LDS_UNROLL 4  // column steps unrolled per loop trip
+#define NGIA_LDS_UNROLL 2  // column steps unrolled per loop trip
 #endif
 #ifndef NGIA_LDS_PREFETCH
-#define NGIA_LDS_PREFETCH 0  // 1: load the next block's words one block ahead
+#define NGIA_LDS_PREFETCH 1  // 1: load the next block's words one block ahead
 #endif
 
 namespace ngia {
