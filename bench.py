@@ -46,6 +46,19 @@ DATA = ("synthetic: seeded DNA families (uniform roots 200-3000 nt, GC 0.45, 1-1
 # Irreducible integer work of the bit-parallel LCS update per 32 cells (one
 # row word, one column): t = V & M; s = V + t + carry; V = s | (V ^ t).
 ALIGN_OPS_PER_WORD_STEP = 3
+# Logic/shift-pipe work of one band hash in the sketch (per signed position and
+# band): the seed xor, four shift+xor pairs, the running min.  Its three
+# multiplies issue to the multiply-add pipe alongside and are not counted.
+SKETCH_ALU_OPS_PER_HASH = 10
+# DRAM bytes (read + write) per unit, from ncu captures of the kernels on the
+# 20,000-sequence case of the same generator (profiles/*_dna20k.txt); scaled
+# to a full launch by the units it processes.
+SKETCH_DRAM_BYTES_PER_POSITION = None
+ALIGN_DRAM_BYTES_PER_CELL = None
+# The reference's host code clusters about 650 families (6,500 sequences) of
+# this generator per second on 16 Grace cores; samples are sized from that.
+CPU_FAMILIES_PER_S = 650
+CPU_SAMPLE_FAMILIES = 6500
 
 
 def log(*a):
@@ -55,13 +68,13 @@ def log(*a):
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--n-seqs", type=int, default=N_SEQS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--ref-families", type=int, default=0,
-                   help="families in the reference arm's sample (default: sized to ~10 s)")
+                   help="families in the CPU samples (default: sized from CPU_FAMILIES_PER_S)")
     return p.parse_args()
 
 
@@ -118,6 +131,14 @@ def make_database(n_seqs: int, n_families: int, seed: int, workdir: Path):
     return db, fasta, packed
 
 
+def signed_positions(lens) -> int:
+    """Positions the sketch hashes: L - 7 per record of length L >= 8, one for
+    a shorter non-empty record (its whole sequence is the k-mer)."""
+    import numpy as np
+    lens = np.asarray(lens, dtype=np.int64)
+    return int(np.where(lens >= 8, lens - 7, (lens > 0).astype(np.int64)).sum())
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
 
@@ -138,6 +159,12 @@ class ClockSampler:
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        # wait (bounded) for the first sample so that sampling covers the timed region
+        t0 = time.time()
+        while self.proc is not None and time.time() - t0 < 5.0:
+            if self.proc.poll() is not None or self.path.stat().st_size > 0:
+                break
+            time.sleep(0.05)
         return self
 
     def __exit__(self, *exc):
@@ -340,16 +367,34 @@ def run_ours(args, world, rank, local, pg):
         ctx.close()
         return None
     int_peak = ng.int32_peak(stream.cuda_stream)
-    align_ops = cells / 32 * ALIGN_OPS_PER_WORD_STEP
-    achieved = align_ops / (align_ms * 1e-3)
-    traffic = None
-    tfile = ROOT / "profiles" / "align_traffic.json"
-    if tfile.exists():
-        try:
-            traffic = json.loads(tfile.read_text()).get("bytes_per_cell")
-            traffic = traffic * cells if traffic else None
-        except ValueError:
-            traffic = None
+    sketch_ms = statistics.mean(s["ms_sketch"] for s in stats)
+    positions = signed_positions(db["lens"])
+    hbm = peaks().get("hbm_gbs")
+
+    def roof(kernel, ops, ms, units, unit_name, bytes_per_unit, algo_bytes, launches_):
+        achieved = ops / (ms * 1e-3)
+        return {"bound": "int32_alu", "kernel": kernel, "achieved": achieved / 1e12,
+                "peak": int_peak / 1e12, "unit": "Tops/s (32-bit lane ops)",
+                "frac": achieved / int_peak, "peak_source":
+                "measured: ngia_int32_peak (lop3 chains on all SMs, the logic/shift pipe)",
+                "units": {unit_name: units}, "launches": launches_, "ms": ms,
+                "traffic": bytes_per_unit * units / launches_ if bytes_per_unit else None,
+                "algorithmic_bytes": algo_bytes / launches_,
+                "hbm_frac_of_measured": (algo_bytes / (ms * 1e-3) / (hbm * 1e9)) if hbm else None}
+
+    rs = {
+        "sketch": roof("sketch_kernel<NibbleKmers>", positions * BANDS * SKETCH_ALU_OPS_PER_HASH,
+                       sketch_ms, positions, "signed_positions", SKETCH_DRAM_BYTES_PER_POSITION,
+                       # nibble codes read (half a byte per residue) + 64 signatures written
+                       int(db["lens"].sum()) / 2 + 4 * BANDS * n, 1),
+        # the align phase: one launch per populated width class, timed as a whole
+        "align": roof("align phase (align_lds_kernel / align_class_kernel per width class)",
+                      cells / 32 * ALIGN_OPS_PER_WORD_STEP, align_ms, cells, "computed_cells",
+                      ALIGN_DRAM_BYTES_PER_CELL,
+                      # the pair list and scores once + every record's codes once
+                      st["unique_pairs"] * 12 + int(db["lens"].sum()) / 2, 1),
+    }
+    dominant = max(rs, key=lambda k: rs[k]["ms"])
     line = {
         "metric": "seqs clustered/s", "value": world * n / (mean_ms_max * 1e-3),
         "unit": "seqs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -365,12 +410,8 @@ def run_ours(args, world, rank, local, pg):
                       for k in ("ms_sketch", "ms_bucket", "ms_pairs", "ms_align", "ms_emit")},
         "work": {"candidate_pairs": st["candidate_pairs"], "unique_pairs": st["unique_pairs"],
                  "band_cells": band_cells, "computed_cells": cells, "edges": st["edges"]},
-        "roofline": {"bound": "int32_alu", "kernel": "align (width-class kernels, one phase)",
-                     "achieved": achieved / 1e12, "peak": int_peak / 1e12,
-                     "unit": "Tops/s (32-bit lane ops)", "frac": achieved / int_peak,
-                     "ops_per_32_cells": ALIGN_OPS_PER_WORD_STEP,
-                     "peak_source": "measured: ngia_int32_peak (lop3 chains, all SMs)",
-                     "traffic": traffic},
+        "roofline": dict(rs[dominant], name=dominant),
+        "rooflines": rs,
         "e2e": {"value": world * n / (e2e_mean * 1e-3), "unit": "seqs/s",
                 "ms_per_step": e2e_mean, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches // max(1, args.steps) * args.steps,
@@ -380,7 +421,8 @@ def run_ours(args, world, rank, local, pg):
     ctx.close()
     if world == 1 and not args.no_cpu_baseline:
         try:
-            fam = args.ref_families or 400
+            # about 10 s of the reference's host code on all cores
+            fam = args.ref_families or CPU_SAMPLE_FAMILIES
             line["cpu_baseline"] = run_cpu_baseline(workdir, 1, 0, fam)
         except Exception as e:  # reported, never silently dropped
             line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
@@ -391,7 +433,10 @@ def run_reference(args, world, rank):
     if rank != 0:
         return None
     workdir = Path(tempfile.mkdtemp(prefix="ngia_ref_"))
-    fam = args.ref_families or 1000
+    # each pass a sample sized so that warm-up + timed passes take about two minutes
+    per_pass_s = 120.0 / max(1, args.steps + args.warmup)
+    fam = args.ref_families or int(min(CPU_SAMPLE_FAMILIES,
+                                       max(50, per_pass_s * CPU_FAMILIES_PER_S)))
     base = run_cpu_baseline(workdir, args.steps, args.warmup, fam)
     return {
         "metric": "seqs clustered/s", "value": base["value"], "unit": "seqs/s",
