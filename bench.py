@@ -429,14 +429,18 @@ def run_ours(args, world, rank, local, pg):
     return line
 
 
+def reference_sample_families(steps: int, warmup: int) -> int:
+    """Families per pass of the reference arm: warm-up + timed passes take
+    about two minutes of the reference's host code."""
+    per_pass_s = 120.0 / max(1, steps + warmup)
+    return int(min(CPU_SAMPLE_FAMILIES, max(50, per_pass_s * CPU_FAMILIES_PER_S)))
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
     workdir = Path(tempfile.mkdtemp(prefix="ngia_ref_"))
-    # each pass a sample sized so that warm-up + timed passes take about two minutes
-    per_pass_s = 120.0 / max(1, args.steps + args.warmup)
-    fam = args.ref_families or int(min(CPU_SAMPLE_FAMILIES,
-                                       max(50, per_pass_s * CPU_FAMILIES_PER_S)))
+    fam = args.ref_families or reference_sample_families(args.steps, args.warmup)
     base = run_cpu_baseline(workdir, args.steps, args.warmup, fam)
     return {
         "metric": "seqs clustered/s", "value": base["value"], "unit": "seqs/s",
