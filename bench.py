@@ -51,10 +51,10 @@ ALIGN_OPS_PER_WORD_STEP = 3
 # multiplies issue to the multiply-add pipe alongside and are not counted.
 SKETCH_ALU_OPS_PER_HASH = 10
 # DRAM bytes (read + write) per unit, from ncu captures of the kernels on the
-# 20,000-sequence case of the same generator (profiles/*_dna20k.txt); scaled
-# to a full launch by the units it processes.
-SKETCH_DRAM_BYTES_PER_POSITION = None
-ALIGN_DRAM_BYTES_PER_CELL = None
+# 100,000-sequence case of the same generator (profiles/*_dna100k.txt); scaled
+# to a full launch by the units it processes (both grow in proportion).
+SKETCH_DRAM_BYTES_PER_POSITION = 0.553
+ALIGN_DRAM_BYTES_PER_CELL = 5.9e-4
 # The reference's host code clusters about 650 families (6,500 sequences) of
 # this generator per second on 16 Grace cores; samples are sized from that.
 CPU_FAMILIES_PER_S = 650
@@ -400,7 +400,9 @@ def run_ours(args, world, rank, local, pg):
         "unit": "seqs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": mean_ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": DATA,
-        "config": {"workload": WORKLOAD, "n_seqs": n, "families": n_fam, "identity": IDENTITY,
+        "config": {"workload": WORKLOAD if n == N_SEQS else
+                   f"dna_{n}_seqs_{n_fam}_families_id{IDENTITY}_{BANDS}bands",
+                   "n_seqs": n, "families": n_fam, "identity": IDENTITY,
                    "bands": BANDS, "stages": "sketch+bucket+candidates+align+emit",
                    "l2": "flushed before every timed step (256 MiB write)",
                    "parallelism": f"replicas x{world}"},
