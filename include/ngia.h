@@ -181,6 +181,23 @@ int ngia_ctx_group_align(ngia_ctx *ctx, uint32_t identity, uint32_t bands,
 /* Copy the last graph's edges to the host (cap entries at most). */
 int ngia_ctx_edges(ngia_ctx *ctx, ngia_edge *h_edges, uint64_t cap);
 
+/* Batched alignment of caller-given pairs on the resident database: the same
+ * scores as ngia_align_pairs (the kernel_dynamic contract, src/buildGraph.hpp
+ * :192-253; 0 for pairs failing the length filter), computed by the
+ * length-binned persistent kernels: pairs are binned by band width, each bin
+ * is queued longest first and taken by a persistent grid -- one pair per lane
+ * for narrow bands, one pair per group of 16 or 32 lanes for wide ones.
+ * d_pairs: count (rep, tar) u32 index pairs on the device, every index below
+ * the loaded record count (not checked); d_scores: count u32 out.  The
+ * context's own pair scratch is not touched.  Synchronises. */
+int ngia_ctx_align_pairs(ngia_ctx *ctx, const uint32_t *d_pairs, uint32_t count,
+                         uint32_t identity, uint32_t *d_scores, ngia_stats *stats);
+
+/* Same from host arrays (indices checked, NGIA_ERR_ARG when one is out of
+ * range); uses the context's pair buffers. */
+int ngia_ctx_align_pairs_host(ngia_ctx *ctx, const uint32_t *h_pairs, uint32_t count,
+                              uint32_t identity, uint32_t *h_scores, ngia_stats *stats);
+
 /* Fast greedy clustering (src/fastClustering.hpp:249-352): per band, targets
  * not yet assigned are aligned against their rep and assigned on a hit;
  * h_cluster[i] = root index.  Synchronises. */

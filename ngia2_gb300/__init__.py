@@ -86,6 +86,10 @@ _SIGNATURES = {
     "ngia_ctx_group_align": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32,
                                        C.POINTER(C.c_uint64), C.POINTER(Stats)]),
     "ngia_ctx_edges": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "ngia_ctx_align_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                       C.c_void_p, C.POINTER(Stats)]),
+    "ngia_ctx_align_pairs_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                            C.c_void_p, C.POINTER(Stats)]),
     "ngia_int32_peak": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ngia_ctx_fast_cluster": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.POINTER(Stats)]),
@@ -260,6 +264,25 @@ class Context:
     def graph(self, identity: int, bands: int = BANDS) -> tuple[np.ndarray, dict]:
         m, st = self.build_graph(identity, bands)
         return self.edges(m), st
+
+    def align_pairs(self, pairs: np.ndarray, identity: int) -> tuple[np.ndarray, dict]:
+        """Batched alignment of (rep, tar) index pairs [count, 2] from host
+        memory; returns the u32 scores and the stats."""
+        pairs = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1, 2)
+        out = np.zeros(len(pairs), np.uint32)
+        st = Stats()
+        _check(lib().ngia_ctx_align_pairs_host(self._h, _ptr(pairs), len(pairs), identity,
+                                               _ptr(out), C.byref(st)),
+               "ngia_ctx_align_pairs_host")
+        return out, st.as_dict()
+
+    def align_pairs_device(self, d_pairs: int, count: int, identity: int,
+                           d_scores: int) -> dict:
+        """Batched alignment of `count` device (rep, tar) pairs into d_scores."""
+        st = Stats()
+        _check(lib().ngia_ctx_align_pairs(self._h, d_pairs, count, identity, d_scores,
+                                          C.byref(st)), "ngia_ctx_align_pairs")
+        return st.as_dict()
 
     def fast_cluster(self, identity: int, bands: int = BANDS) -> np.ndarray:
         out = np.empty(self.n, np.uint32)

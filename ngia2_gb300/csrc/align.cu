@@ -1,7 +1,11 @@
 // align.cu -- alignment kernels: the drop-in job-triple kernel and the
 // length-binned batched kernels.
+#include <mutex>
+#include <vector>
+
 #include "align.cuh"
-#include "align_lds.cuh"
+#include "align_group.cuh"
+#include "align_stream.cuh"
 #include "kernels.cuh"
 
 namespace ngia {
@@ -20,8 +24,11 @@ __device__ __forceinline__ uint32_t lcs_any(const uint32_t *rep, const uint32_t 
 
 // Adds the warp's computed 32x32 blocks (row words x column blocks) to *work.
 __device__ __forceinline__ void count_work(uint32_t blocks, unsigned long long *work) {
-  const uint32_t sum = __reduce_add_sync(kFull, blocks);
-  if ((threadIdx.x & 31u) == 0 && sum) atomicAdd(work, (unsigned long long)sum);
+  // two 16-bit halves, so that a warp's sum cannot overflow
+  const uint32_t lo = __reduce_add_sync(kFull, blocks & 0xFFFFu);
+  const uint32_t hi = __reduce_add_sync(kFull, blocks >> 16);
+  const unsigned long long sum = ((unsigned long long)hi << 16) + lo;
+  if ((threadIdx.x & 31u) == 0 && sum) atomicAdd(work, sum);
 }
 
 __global__ void __launch_bounds__(128)
@@ -94,31 +101,35 @@ align_class_kernel(const uint32_t *__restrict__ packed,
   count_work(done, work);
 }
 
-// Batched form, shared-memory table kernel (align_lds.cuh).
-template <int W, int K>
-__global__ void __launch_bounds__(lds_threads(W))
-align_lds_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
-                 uint64_t inv, const uint64_t *__restrict__ offs,
-                 const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,
-                 uint32_t begin, uint32_t end, uint32_t *__restrict__ scores, float t,
-                 int fma_mode, unsigned long long *__restrict__ work) {
+// Batched form, group kernel (align_group.cuh): a persistent grid whose groups
+// of G lanes take pairs of one class from its queue.
+template <int G, int K, int KC>
+__global__ void __launch_bounds__(kGroupThreads)
+align_group_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
+                   uint64_t inv, const uint64_t *__restrict__ offs,
+                   const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,
+                   uint32_t begin, uint32_t end, unsigned int *__restrict__ cursor,
+                   uint32_t *__restrict__ scores, float t, int fma_mode,
+                   unsigned long long *__restrict__ work) {
   extern __shared__ uint32_t smem[];
-  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t done = 0;
-  if (k < end) {
-    const LdsTable<W, K> tab{smem + (threadIdx.x >> 5) * (K * W * 32) + (threadIdx.x & 31u),
-                             inv};
-    const uint32_t p = order[k];
-    const uint2 pr = pairs[p];
-    const uint32_t *rep = packed + offs[pr.x];
-    const uint64_t to = offs[pr.y];
-    const uint32_t lr = __ldg(rep), lt = __ldg(packed + to);
-    const Band b = make_band(lr, lt, t, fma_mode);
-    uint32_t blocks;
-    const uint32_t lcs = lcs_lds<W>(rep, nib + to + 1, b, tab, blocks);
-    scores[p] = identity_score(lcs, lr, lt, t);
-    done = blocks * W;
-  }
+  const uint32_t done = align_group<G, K, KC>(packed, nib, inv, offs, pairs, order, begin, end,
+                                              cursor, scores, t, fma_mode, smem);
+  count_work(done, work);
+}
+
+// Batched form, streaming shared-memory table kernel (align_stream.cuh):
+// a persistent grid whose lanes take pairs of one class from its queue.
+template <int W, int K>
+__global__ void __launch_bounds__(kStreamThreads)
+align_stream_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
+                    uint64_t inv, const uint64_t *__restrict__ offs,
+                    const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,
+                    uint32_t begin, uint32_t end, unsigned int *__restrict__ cursor,
+                    uint32_t *__restrict__ scores, float t, int fma_mode,
+                    unsigned long long *__restrict__ work) {
+  extern __shared__ uint32_t smem[];
+  const uint32_t done = align_stream<W, K>(packed, nib, inv, offs, pairs, order, begin, end,
+                                           cursor, scores, t, fma_mode, smem);
   count_work(done, work);
 }
 
@@ -203,28 +214,95 @@ int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_
   return NGIA_OK;
 }
 
-template <int W>
-static int launch_lds(const uint32_t *packed, const uint32_t *nib, const Alphabet &ab,
-                      const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
-                      uint32_t begin, uint32_t end, uint32_t *scores, float t, int fm,
-                      unsigned long long *work, cudaStream_t s) {
-  constexpr int T = lds_threads(W);
-  const uint32_t blocks = ceil_div(end - begin, (uint32_t)T);
-  if (ab.K == 8) {
-    constexpr size_t smem = lds_smem_bytes(W, 8);
-    NGIA_CUDA(cudaFuncSetAttribute(align_lds_kernel<W, 8>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    align_lds_kernel<W, 8><<<blocks, T, smem, s>>>(packed, nib, ab.inv, offs, pairs, order,
-                                                   begin, end, scores, t, fm, work);
-  } else {
-    constexpr size_t smem = lds_smem_bytes(W, 16);
-    NGIA_CUDA(cudaFuncSetAttribute(align_lds_kernel<W, 16>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    align_lds_kernel<W, 16><<<blocks, T, smem, s>>>(packed, nib, ab.inv, offs, pairs, order,
-                                                    begin, end, scores, t, fm, work);
+// Blocks of a persistent launch: as many as fit on the device at once, and no
+// more than `want`.  Occupancy is looked up once per (kernel, device).
+struct OccEntry {
+  const void *func;
+  int dev, per_sm, sms;
+};
+static std::mutex g_occ_mu;
+static std::vector<OccEntry> g_occ;
+
+template <typename F>
+static int persistent_grid(F func, int threads, size_t smem, uint32_t want, uint32_t *grid) {
+  int dev = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  const void *key = reinterpret_cast<const void *>(func);
+  std::lock_guard<std::mutex> lock(g_occ_mu);
+  const OccEntry *hit = nullptr;
+  for (const OccEntry &e : g_occ)
+    if (e.func == key && e.dev == dev) hit = &e;
+  if (!hit) {
+    OccEntry e{key, dev, 0, 0};
+    NGIA_CUDA(cudaDeviceGetAttribute(&e.sms, cudaDevAttrMultiProcessorCount, dev));
+    NGIA_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NGIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e.per_sm, func, threads, smem));
+    if (e.per_sm < 1) e.per_sm = 1;
+    g_occ.push_back(e);
+    hit = &g_occ.back();
   }
+  const uint32_t cap = (uint32_t)(hit->per_sm * hit->sms);
+  *grid = want < cap ? want : cap;
+  return NGIA_OK;
+}
+
+template <int W, int K>
+static int launch_stream_k(const uint32_t *packed, const uint32_t *nib, uint64_t inv,
+                           const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
+                           uint32_t begin, uint32_t end, unsigned int *cursor,
+                           uint32_t *scores, float t, int fm, unsigned long long *work,
+                           cudaStream_t s) {
+  constexpr size_t smem = stream_smem_bytes(W, K);
+  uint32_t grid = 0;
+  NGIA_TRY(persistent_grid(align_stream_kernel<W, K>, kStreamThreads, smem,
+                           ceil_div(end - begin, (uint32_t)kStreamThreads), &grid));
+  align_stream_kernel<W, K><<<grid, kStreamThreads, smem, s>>>(
+      packed, nib, inv, offs, pairs, order, begin, end, cursor, scores, t, fm, work);
   NGIA_LAUNCHED();
   return NGIA_OK;
+}
+
+template <int G, int K, int KC>
+static int launch_group_k(const uint32_t *packed, const uint32_t *nib, uint64_t inv,
+                          const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
+                          uint32_t begin, uint32_t end, unsigned int *cursor,
+                          uint32_t *scores, float t, int fm, unsigned long long *work,
+                          cudaStream_t s) {
+  constexpr size_t smem = group_smem_bytes(K, KC);
+  constexpr uint32_t groups_per_block = kGroupThreads / G;
+  uint32_t grid = 0;
+  NGIA_TRY(persistent_grid(align_group_kernel<G, K, KC>, kGroupThreads, smem,
+                           ceil_div(end - begin, groups_per_block), &grid));
+  align_group_kernel<G, K, KC><<<grid, kGroupThreads, smem, s>>>(
+      packed, nib, inv, offs, pairs, order, begin, end, cursor, scores, t, fm, work);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+template <int G, int K>
+static int launch_group(const uint32_t *packed, const uint32_t *nib, const Alphabet &ab,
+                        const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
+                        uint32_t begin, uint32_t end, unsigned int *cursor,
+                        uint32_t *scores, float t, int fm, unsigned long long *work,
+                        cudaStream_t s) {
+  if (ab.K == 8)
+    return launch_group_k<G, K, 8>(packed, nib, ab.inv, offs, pairs, order, begin, end,
+                                   cursor, scores, t, fm, work, s);
+  return launch_group_k<G, K, 16>(packed, nib, ab.inv, offs, pairs, order, begin, end, cursor,
+                                  scores, t, fm, work, s);
+}
+
+template <int W>
+static int launch_stream(const uint32_t *packed, const uint32_t *nib, const Alphabet &ab,
+                         const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
+                         uint32_t begin, uint32_t end, unsigned int *cursor,
+                         uint32_t *scores, float t, int fm, unsigned long long *work,
+                         cudaStream_t s) {
+  if (ab.K == 8)
+    return launch_stream_k<W, 8>(packed, nib, ab.inv, offs, pairs, order, begin, end, cursor,
+                                 scores, t, fm, work, s);
+  return launch_stream_k<W, 16>(packed, nib, ab.inv, offs, pairs, order, begin, end, cursor,
+                                scores, t, fm, work, s);
 }
 
 int launch_align_jobs(const uint32_t *packed, const uint64_t *offs, uint32_t *jobs,
@@ -252,15 +330,15 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const Alphabet &ab, const uint64_t *offs, const uint2 *pairs,
                        const uint32_t *order, uint32_t begin, uint32_t end,
                        uint32_t *scores, uint32_t identity, unsigned long long *work,
-                       cudaStream_t s) {
+                       unsigned int *cursor, cudaStream_t s) {
   if (end <= begin) return NGIA_OK;
   const float t = identity_threshold(identity);
   const int fm = round_mode();
   const uint32_t blocks = ceil_div(end - begin, 128u);
-#define NGIA_LDS_CASE(C, W)                                                               \
-  case C:                                                                                 \
-    return launch_lds<W>(packed, nib, ab, offs, pairs, order, begin, end, scores, t, fm, \
-                         work, s);
+#define NGIA_LDS_CASE(C, W)                                                          \
+  case C:                                                                            \
+    return launch_stream<W>(packed, nib, ab, offs, pairs, order, begin, end, cursor, \
+                            scores, t, fm, work, s);
   switch (cls) {
     NGIA_LDS_CASE(0, 4)
     NGIA_LDS_CASE(1, 6)
@@ -270,8 +348,17 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
     NGIA_LDS_CASE(5, 14)
     NGIA_LDS_CASE(6, 16)
 #undef NGIA_LDS_CASE
-    case 7: align_class_kernel<24><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm, work); break;
-    case 8: align_class_kernel<32><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm, work); break;
+#define NGIA_GROUP_CASE(C)                                                              \
+  case C:                                                                               \
+    return launch_group<group_shape(C).G, group_shape(C).K>(                            \
+        packed, nib, ab, offs, pairs, order, begin, end, cursor, scores, t, fm, work, s);
+    NGIA_GROUP_CASE(7)
+    NGIA_GROUP_CASE(8)
+    NGIA_GROUP_CASE(9)
+    NGIA_GROUP_CASE(10)
+    NGIA_GROUP_CASE(11)
+    NGIA_GROUP_CASE(12)
+#undef NGIA_GROUP_CASE
     case kGeneralClass: align_class_kernel<0><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm, work); break;
     default: return NGIA_ERR_ARG;
   }

@@ -252,26 +252,72 @@ __device__ inline uint32_t lcs_general(const uint32_t *__restrict__ rep,
 }
 
 // Width classes of the batched aligner:
-//   0..6  shared-memory table kernel (align_lds.cuh), W = 4, 6, ..., 16
-//   7, 8  register-plane window kernel, W = 24, 32
-//   9     general kernel (any width)
-//   10    pairs failing the length filter (score 0, not launched)
+//   0..6   streaming shared-memory table kernel (align_stream.cuh), one pair
+//          per lane, W = 4, 6, ..., 16 words by stream_width
+//   7..12  group kernel (align_group.cuh), one pair per group of G lanes with
+//          K words per lane: (16,1) (32,1) (32,2) (32,4) (32,8) (32,16)
+//   13     general kernel, one pair per thread (any width)
+//   14     pairs failing the length filter (score 0, not launched)
 constexpr int kNumLdsClasses = 7;
-constexpr int kGeneralClass = 9;
-constexpr int kSkipClass = 10;
-constexpr int kNumClasses = 11;
+constexpr int kFirstGroupClass = 7;
+constexpr int kNumGroupClasses = 6;
+constexpr int kGeneralClass = 13;
+constexpr int kSkipClass = 14;
+constexpr int kNumClasses = 15;
+
+struct GroupShape {
+  int G, K;
+};
+__host__ __device__ constexpr GroupShape group_shape(int c) {
+  return c == 7 ? GroupShape{16, 1}
+       : c == 8 ? GroupShape{32, 1}
+       : c == 9 ? GroupShape{32, 2}
+       : c == 10 ? GroupShape{32, 4}
+       : c == 11 ? GroupShape{32, 8}
+                 : GroupShape{32, 16};
+}
 
 __host__ __device__ inline int class_width(int c) {
-  return c < kNumLdsClasses ? 4 + 2 * c : (c == 7 ? 24 : (c == 8 ? 32 : 0));
+  return c < kNumLdsClasses ? 4 + 2 * c : 0;
+}
+
+// Window a streaming kernel needs for a pair: the live rows of block i,
+// [max(i - ls, 0), min(i + rs, nr)), inside [i - ls, i - ls + W).
+__host__ __device__ inline uint32_t stream_width(const Band &b) {
+  return b.ls + (b.rs < b.nr ? b.rs : b.nr);
+}
+
+// A group of G lanes with K words per lane holds at most one live slice per
+// lane when the rep has at most G slices or ls + rs <= (G - 1)K + G.
+__host__ __device__ inline bool group_fits(const Band &b, int G, int K) {
+  const uint32_t ns = (b.nr + K - 1) / K;
+  return ns <= (uint32_t)G || b.ls + b.rs <= (uint32_t)((G - 1) * K + G);
 }
 
 __host__ __device__ inline int width_class(const Band &b) {
   if (!b.pass) return kSkipClass;
-  const uint32_t w = b.width;
-  if (w <= 16) return w <= 4 ? 0 : (int)((w - 3) / 2);  // 5,6 -> 1; 7,8 -> 2; ...
-  if (w <= 24) return 7;
-  if (w <= 32) return 8;
+  const uint32_t ws = stream_width(b);
+  if (ws <= 16) return ws <= 4 ? 0 : (int)((ws - 3) / 2);  // 5,6 -> 1; 7,8 -> 2; ...
+  for (int c = kFirstGroupClass; c < kFirstGroupClass + kNumGroupClasses; ++c)
+    if (group_fits(b, group_shape(c).G, group_shape(c).K)) return c;
   return kGeneralClass;
 }
+
+// Queue order inside a class: longest targets first.  The sort key of a pair
+// is class-major, then 15 - floor(2 log2 nc) (column blocks in half-octaves,
+// capped at 15), one 8-bit radix pass.
+__host__ __device__ inline uint32_t class_sort_key(int cls, const Band &b) {
+  uint32_t h = 0;
+  if (b.nc > 1) {
+#ifdef __CUDA_ARCH__
+    const uint32_t lg = 31u - (uint32_t)__clz(b.nc);  // floor(log2 nc)
+#else
+    const uint32_t lg = 31u - (uint32_t)__builtin_clz(b.nc);
+#endif
+    h = 2 * lg + ((uint64_t)b.nc * b.nc >= (2ull << (2 * lg)) ? 1u : 0u);
+  }
+  return ((uint32_t)cls << 4) | (15u - (h < 15u ? h : 15u));
+}
+constexpr int kClassKeyBits = 8;
 
 }  // namespace ngia

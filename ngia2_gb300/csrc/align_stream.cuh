@@ -1,0 +1,176 @@
+// align_stream.cuh -- persistent shared-memory aligner: each lane of a warp
+// aligns its own stream of pairs (internal header).
+//
+// Same recurrence, tables and column steps as align_lds.cuh.  What changes is
+// how the 32 lanes of a warp share the instruction stream.  With one pair per
+// lane for the whole launch, lanes whose pairs are shorter, or whose score is
+// settled early, idle until the warp's slowest pair ends, and lanes whose
+// bands start at different row offsets rotate their windows differently, so
+// the rotation switch diverges.  Here:
+//
+// Virtual rows.  A pair's window holds rows j0v .. j0v + W - 1 with
+// j0v = i - ls at column block i; rows below 0 are virtual (all ones, zero
+// masks): they pass a zero carry up unchanged, which is exactly the band's
+// zero carry into its lowest live row J0 = max(i - ls, 0).  Row r lives in
+// slot (base + r) % W with base = (g0 + ls) % W, g0 being the warp step at
+// which the pair's first column block runs.  At warp step g the window's
+// lowest row then sits in slot g % W in every lane: the rotation is uniform
+// across the warp whatever each lane's pair is.  The window covers every live
+// row [J0, J1) when ls + min(rs, nr) <= W, the width these classes are
+// binned by.
+//
+// Streams.  A lane whose pair ends (last column block, or a score of 0
+// already certain) writes the score, resets its window and takes the next
+// pair from the class's queue (one atomic per warp for all lanes that need
+// one), so the lanes stay busy until the queue drains.  Pairs are queued
+// longest first.
+#pragma once
+
+#include "align_lds.cuh"
+
+namespace ngia {
+
+// Threads per block of the streaming kernels (each warp owns its tables).
+constexpr int kStreamThreads = 64;
+
+__host__ __device__ constexpr size_t stream_smem_bytes(int W, int K) {
+  return (size_t)kStreamThreads * K * W * 4;
+}
+
+// One lane's pair.
+struct StreamPair {
+  const uint32_t *rep;  // rep record (length word, then bit planes)
+  const uint32_t *tar;  // target's nibble code words
+  uint32_t p;           // pair index (score slot)
+  uint32_t i;           // current column block
+  uint32_t nc, nr, rs;
+  uint32_t act;         // rows entered so far
+  uint32_t in_slot;     // slot of row `act`
+  uint32_t lcs;         // zeros of the retired rows
+  uint32_t lr, lt;
+  uint4 cur;            // code words of block i
+  bool active;
+};
+
+// One column block at warp rotation R: retire the row leaving the window,
+// enter the rows reaching the band, 32 column steps.
+template <int W, int R, typename Tab>
+__device__ __forceinline__ void stream_block(uint32_t (&V)[W], const Tab &tab,
+                                             StreamPair &sp) {
+  constexpr int out = (R + W - 1) % W;
+  sp.lcs += __popc(~V[out]);
+  V[out] = kFull;
+  tab.clear(out);
+  const uint32_t j1 = sp.i + sp.rs < sp.nr ? sp.i + sp.rs : sp.nr;
+  for (; sp.act < j1; ++sp.act) {
+    tab.fill(sp.in_slot, load4(sp.rep + 1 + 4 * sp.act));
+    sp.in_slot = sp.in_slot + 1 == (uint32_t)W ? 0u : sp.in_slot + 1;
+  }
+  lds_columns<W, R>(V, tab.base, sp.cur);
+}
+
+template <int W, typename Tab, int R = 0>
+__device__ __forceinline__ void stream_dispatch(uint32_t rot, uint32_t (&V)[W],
+                                                const Tab &tab, StreamPair &sp) {
+  if constexpr (R < W) {
+    if (rot == R) {
+      if (sp.active) stream_block<W, R>(V, tab, sp);
+      return;
+    }
+    stream_dispatch<W, Tab, R + 1>(rot, V, tab, sp);
+  }
+}
+
+// The persistent kernel body of one width class.  `order[begin, end)` lists
+// the class's pairs; `cursor` counts the pairs taken (zero at launch).
+// Returns the column blocks x W computed by this lane.
+template <int W, int K>
+__device__ inline uint32_t align_stream(const uint32_t *__restrict__ packed,
+                                        const uint32_t *__restrict__ nib, uint64_t inv,
+                                        const uint64_t *__restrict__ offs,
+                                        const uint2 *__restrict__ pairs,
+                                        const uint32_t *__restrict__ order, uint32_t begin,
+                                        uint32_t end, unsigned int *__restrict__ cursor,
+                                        uint32_t *__restrict__ scores, float t,
+                                        int fma_mode, uint32_t *smem) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const LdsTable<W, K> tab{smem + (threadIdx.x >> 5) * (K * W * 32) + lane, inv};
+#pragma unroll 1
+  for (uint32_t s = 0; s < (uint32_t)W; ++s) {
+    tab.clear(s);
+    tab.slot(s)[0] = 0u;  // code 0 matches nothing
+  }
+  uint32_t V[W];
+#pragma unroll
+  for (int m = 0; m < W; ++m) V[m] = kFull;
+  StreamPair sp;
+  sp.active = false;
+  bool drained = false;
+  uint32_t done = 0, g = 0;
+  for (;;) {
+    // lanes without a pair take the next ones from the queue
+    const uint32_t need = __ballot_sync(kFull, !sp.active && !drained);
+    if (need) {
+      const uint32_t leader = __ffs(need) - 1;
+      uint32_t first = 0;
+      if (lane == leader) first = atomicAdd(cursor, (unsigned int)__popc(need));
+      first = __shfl_sync(kFull, first, leader);
+      if (!sp.active && !drained) {
+        const uint32_t k = begin + first + __popc(need & ((1u << lane) - 1u));
+        if (k < end) {
+          const uint32_t p = order[k];
+          const uint2 pr = pairs[p];
+          const uint64_t to = offs[pr.y];
+          sp.rep = packed + offs[pr.x];
+          sp.tar = nib + to + 1;
+          sp.lr = __ldg(sp.rep);
+          sp.lt = __ldg(packed + to);
+          const Band b = make_band(sp.lr, sp.lt, t, fma_mode);
+          if (b.nc == 0) {
+            scores[p] = identity_score(0u, sp.lr, sp.lt, t);
+          } else {
+            sp.p = p;
+            sp.i = 0;
+            sp.nc = b.nc;
+            sp.nr = b.nr;
+            sp.rs = b.rs;
+            sp.act = 0;
+            sp.in_slot = (g + b.ls) % (uint32_t)W;
+            sp.lcs = 0;
+            sp.cur = load4(sp.tar);
+            sp.active = true;
+          }
+        } else {
+          drained = true;
+        }
+      }
+    }
+    if (!__any_sync(kFull, sp.active)) {
+      if (__all_sync(kFull, drained)) break;
+      continue;
+    }
+    stream_dispatch<W>(g % (uint32_t)W, V, tab, sp);
+    ++g;
+    if (sp.active) {
+      ++sp.i;
+      done += W;
+      uint32_t z = sp.lcs;
+#pragma unroll
+      for (int m = 0; m < W; ++m) z += __popc(~V[m]);
+      const bool last = sp.i >= sp.nc;
+      if (last || !stream_may_reach(z, 32 * sp.i, sp.lr, sp.lt, t)) {
+        scores[sp.p] = last ? identity_score(z, sp.lr, sp.lt, t) : 0u;
+        sp.active = false;
+#pragma unroll
+        for (int m = 0; m < W; ++m) V[m] = kFull;
+#pragma unroll 1
+        for (uint32_t s = 0; s < (uint32_t)W; ++s) tab.clear(s);
+      } else {
+        sp.cur = load4(sp.tar + 4 * sp.i);
+      }
+    }
+  }
+  return done;
+}
+
+}  // namespace ngia

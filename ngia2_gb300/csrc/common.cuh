@@ -146,13 +146,18 @@ __host__ __device__ inline uint32_t identity_score(uint32_t lcs, uint32_t lr,
 //   lcs_so_far + columns_left
 // fails the test, the pair's score is 0 whatever the remaining columns hold,
 // and the alignment can stop: the score is exactly the reference's.
+__host__ __device__ inline bool stream_may_reach(uint32_t lcs_so_far, uint32_t cols_done,
+                                                 uint32_t lr, uint32_t lt, float t) {
+  const uint32_t left = lt > cols_done ? lt - cols_done : 0u;
+  uint32_t ub = lcs_so_far + left;
+  const uint32_t cap = lr < lt ? lr : lt;
+  if (ub > cap) ub = cap;
+  return identity_score(ub, lr, lt, t) > 0;
+}
+
 __host__ __device__ inline bool may_reach_threshold(uint32_t lcs_so_far, uint32_t cols_done,
                                                     const Band &b) {
-  const uint32_t left = b.lt > cols_done ? b.lt - cols_done : 0u;
-  uint32_t ub = lcs_so_far + left;
-  const uint32_t cap = b.lr < b.lt ? b.lr : b.lt;
-  if (ub > cap) ub = cap;
-  return identity_score(ub, b.lr, b.lt, b.t) > 0;
+  return stream_may_reach(lcs_so_far, cols_done, b.lr, b.lt, b.t);
 }
 
 template <typename T>

@@ -83,6 +83,7 @@ struct Counters {  // device-side counters of one graph build
   unsigned int class_count[kNumClasses];
   uint32_t fast_count;
   unsigned long long work;  // 32x32 blocks the aligners computed
+  unsigned int cursor[kNumClasses];  // pairs taken from each class's queue
 };
 
 static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
@@ -111,6 +112,40 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
     st->ms_sketch = ev_ms(c->ev[0], c->ev[1]);
     st->ms_bucket = ev_ms(c->ev[1], c->ev[2]);
   }
+  return NGIA_OK;
+}
+
+// The batched aligner over m pairs on the device: width classes (classify),
+// class-major queue order with the longest targets first (one radix pass),
+// scores zeroed, then one persistent launch per class, widest first.  Records
+// event ev_first (classification start is the caller's) after the class
+// counts reach the host and ev_first + 1 after the last launch.
+static int align_batched(ngia_ctx *c, const uint2 *pairs, uint32_t m, uint32_t identity,
+                         uint32_t *scores, Counters *dc, Counters *hc, int ev_first) {
+  cudaStream_t s = c->stream;
+  NGIA_TRY(c->cls.reserve((size_t)(m ? m : 1) * 4));
+  NGIA_TRY(c->cls_sorted.reserve((size_t)(m ? m : 1) * 4));
+  NGIA_TRY(c->order.reserve((size_t)(m ? m : 1) * 4));
+  NGIA_TRY(c->sort_tmp.reserve(radix_sort_scratch_bytes(m, 1)));
+  NGIA_TRY(classify(c->lens.as<uint32_t>(), pairs, m, identity, c->cls.as<uint32_t>(),
+                    dc->class_count, &dc->cells, s));
+  NGIA_TRY(radix_sort_pairs(c->cls.as<uint32_t>(), nullptr, c->cls_sorted.as<uint32_t>(),
+                            c->order.as<uint32_t>(), m, 1, 0, kClassKeyBits, c->sort_tmp.p,
+                            s));
+  NGIA_CUDA(cudaMemsetAsync(scores, 0, (size_t)(m ? m : 1) * 4, s));
+  NGIA_CUDA(cudaMemcpyAsync(hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaEventRecord(c->ev[ev_first], s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  uint32_t begin[kNumClasses + 1];
+  begin[0] = 0;
+  for (int k = 0; k < kNumClasses; ++k) begin[k + 1] = begin[k] + hc->class_count[k];
+  const int launch_order[] = {kGeneralClass, 12, 11, 10, 9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
+  for (int cl : launch_order)
+    NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->align_nib, c->ab,
+                                c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
+                                begin[cl], begin[cl + 1], scores, identity, &dc->work,
+                                &dc->cursor[cl], s));
+  NGIA_CUDA(cudaEventRecord(c->ev[ev_first + 1], s));
   return NGIA_OK;
 }
 
@@ -143,32 +178,11 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   const uint32_t m = (uint32_t)total;
   NGIA_TRY(c->pairs.reserve((size_t)(m ? m : 1) * 8));
   NGIA_TRY(c->scores.reserve((size_t)(m ? m : 1) * 4));
-  NGIA_TRY(c->cls.reserve((size_t)(m ? m : 1) * 4));
-  NGIA_TRY(c->cls_sorted.reserve((size_t)(m ? m : 1) * 4));
-  NGIA_TRY(c->order.reserve((size_t)(m ? m : 1) * 4));
-  NGIA_TRY(c->sort_tmp.reserve(radix_sort_scratch_bytes(m, 1)));
   uint2 *pairs = c->pairs.as<uint2>();
   uint32_t *scores = c->scores.as<uint32_t>();
   NGIA_TRY(collect_write(rep, lens, n, bands, identity, c->uoff.as<uint64_t>(), pairs, s));
-  // 2. width classes, stably ordered (target order kept inside a class)
-  NGIA_TRY(classify(lens, pairs, m, identity, c->cls.as<uint32_t>(), dc->class_count,
-                    &dc->cells, s));
-  NGIA_TRY(radix_sort_pairs(c->cls.as<uint32_t>(), nullptr, c->cls_sorted.as<uint32_t>(),
-                            c->order.as<uint32_t>(), m, 1, 0, 8, c->sort_tmp.p, s));
-  NGIA_CUDA(cudaMemsetAsync(scores, 0, (size_t)(m ? m : 1) * 4, s));
-  NGIA_CUDA(cudaMemcpyAsync(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
-  NGIA_CUDA(cudaEventRecord(c->ev[1], s));
-  NGIA_CUDA(cudaStreamSynchronize(s));
-  // 3. align, one launch per width class, widest first
-  uint32_t begin[kNumClasses + 1];
-  begin[0] = 0;
-  for (int k = 0; k < kNumClasses; ++k) begin[k + 1] = begin[k] + hc.class_count[k];
-  const int launch_order[] = {kGeneralClass, 8, 7, 6, 5, 4, 3, 2, 1, 0};
-  for (int cl : launch_order)
-    NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->align_nib, c->ab,
-                                c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
-                                begin[cl], begin[cl + 1], scores, identity, &dc->work, s));
-  NGIA_CUDA(cudaEventRecord(c->ev[2], s));
+  // 2-3. width classes, then one persistent launch per class
+  NGIA_TRY(align_batched(c, pairs, m, identity, scores, dc, &hc, 1));
   // 4. emit: compact hits, sort by (rep, tar)
   NGIA_TRY(c->emit_tmp.reserve(emit_scratch_bytes(m, n)));
   NGIA_TRY(c->edges.reserve((size_t)(m ? m : 1) * sizeof(ngia_edge)));
@@ -189,6 +203,35 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
     st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
     st->ms_align = ev_ms(c->ev[1], c->ev[2]);
     st->ms_emit = ev_ms(c->ev[2], c->ev[3]);
+  }
+  return NGIA_OK;
+}
+
+// The batched aligner on caller-given pairs (device arrays) of the resident
+// database.  Every index must be below the record count.
+int ctx_align_pairs(ngia_ctx *c, const uint2 *d_pairs, uint32_t m, uint32_t identity,
+                    uint32_t *d_scores, ngia_stats *st) {
+  if (c->n == 0) return NGIA_ERR_STATE;
+  if (identity < 1 || identity > 99) return NGIA_ERR_ARG;
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (m == 0) return NGIA_OK;
+  cudaStream_t s = c->stream;
+  NGIA_TRY(c->counters.reserve(sizeof(Counters)));
+  Counters *dc = c->counters.as<Counters>();
+  NGIA_CUDA(cudaMemsetAsync(dc, 0, sizeof(Counters), s));
+  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  Counters hc;
+  NGIA_TRY(align_batched(c, d_pairs, m, identity, d_scores, dc, &hc, 1));
+  NGIA_CUDA(cudaEventSynchronize(c->ev[2]));
+  if (st) {
+    unsigned long long work = 0;
+    NGIA_CUDA(cudaMemcpy(&work, &dc->work, sizeof(work), cudaMemcpyDeviceToHost));
+    st->candidate_pairs = m;
+    st->unique_pairs = m;
+    st->aligned_cells = hc.cells;
+    st->computed_cells = work * 1024ull;
+    st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
+    st->ms_align = ev_ms(c->ev[1], c->ev[2]);
   }
   return NGIA_OK;
 }
@@ -392,6 +435,35 @@ int ngia_ctx_edges(ngia_ctx *c, ngia_edge *h_edges, uint64_t cap) {
   if (m == 0) return NGIA_OK;
   NGIA_CUDA(cudaMemcpyAsync(h_edges, c->edges.p, m * sizeof(ngia_edge),
                             cudaMemcpyDeviceToHost, c->stream));
+  NGIA_CUDA(cudaStreamSynchronize(c->stream));
+  return NGIA_OK;
+}
+
+int ngia_ctx_align_pairs(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count,
+                         uint32_t identity, uint32_t *d_scores, ngia_stats *stats) {
+  if (!c || (count && (!d_pairs || !d_scores))) return NGIA_ERR_ARG;
+  return ngia::ctx_align_pairs(c, reinterpret_cast<const uint2 *>(d_pairs), count, identity,
+                               d_scores, stats);
+}
+
+int ngia_ctx_align_pairs_host(ngia_ctx *c, const uint32_t *h_pairs, uint32_t count,
+                              uint32_t identity, uint32_t *h_scores, ngia_stats *stats) {
+  if (!c || (count && (!h_pairs || !h_scores))) return NGIA_ERR_ARG;
+  if (c->n == 0) return NGIA_ERR_STATE;
+  for (uint64_t j = 0; j < 2ull * count; ++j)
+    if (h_pairs[j] >= c->n) return NGIA_ERR_ARG;
+  if (count == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return NGIA_OK;
+  }
+  NGIA_TRY(c->pairs.reserve((size_t)count * 8));
+  NGIA_TRY(c->scores.reserve((size_t)count * 4));
+  NGIA_CUDA(cudaMemcpyAsync(c->pairs.p, h_pairs, (size_t)count * 8, cudaMemcpyHostToDevice,
+                            c->stream));
+  NGIA_TRY(ngia::ctx_align_pairs(c, c->pairs.as<uint2>(), count, identity,
+                                 c->scores.as<uint32_t>(), stats));
+  NGIA_CUDA(cudaMemcpyAsync(h_scores, c->scores.p, (size_t)count * 4, cudaMemcpyDeviceToHost,
+                            c->stream));
   NGIA_CUDA(cudaStreamSynchronize(c->stream));
   return NGIA_OK;
 }

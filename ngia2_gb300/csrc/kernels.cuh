@@ -41,11 +41,13 @@ struct Alphabet {
   int K;         // 8 or 16 table entries per row block
   uint64_t inv;  // nibble d = residue code of aligner code d
 };
+// One width class of the batched aligner over order[begin, end).  `cursor`
+// (device, zero before the launch) is the queue head of the streaming classes.
 int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const Alphabet &ab, const uint64_t *offs, const uint2 *pairs,
                        const uint32_t *order, uint32_t begin, uint32_t end,
                        uint32_t *scores, uint32_t identity, unsigned long long *work,
-                       cudaStream_t s);
+                       unsigned int *cursor, cudaStream_t s);
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
                    uint32_t *presence, cudaStream_t s);
 int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,

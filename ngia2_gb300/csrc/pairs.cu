@@ -138,7 +138,7 @@ classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pai
     const uint2 pr = pairs[p];
     const Band b = make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode);
     const int c = width_class(b);
-    cls[p] = (uint32_t)c;
+    cls[p] = class_sort_key(c, b);
     atomicAdd(&sc[c], 1u);
     my_cells += band_blocks(b);
   }
