@@ -193,6 +193,12 @@ int ngia_ctx_edges(ngia_ctx *ctx, ngia_edge *h_edges, uint64_t cap);
 int ngia_ctx_align_pairs(ngia_ctx *ctx, const uint32_t *d_pairs, uint32_t count,
                          uint32_t identity, uint32_t *d_scores, ngia_stats *stats);
 
+/* Whether ngia_ctx_align_pairs captures its round (classification, queue
+ * sort and every class launch) as a CUDA graph and replays it while the
+ * pair/score addresses, count, identity and rounding stay the same (default
+ * on).  Returns the previous setting (0/1), or NGIA_ERR_ARG. */
+int ngia_ctx_use_graphs(ngia_ctx *ctx, int on);
+
 /* Same from host arrays (indices checked, NGIA_ERR_ARG when one is out of
  * range); uses the context's pair buffers. */
 int ngia_ctx_align_pairs_host(ngia_ctx *ctx, const uint32_t *h_pairs, uint32_t count,

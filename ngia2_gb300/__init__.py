@@ -90,6 +90,7 @@ _SIGNATURES = {
                                        C.c_void_p, C.POINTER(Stats)]),
     "ngia_ctx_align_pairs_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                             C.c_void_p, C.POINTER(Stats)]),
+    "ngia_ctx_use_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "ngia_int32_peak": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ngia_ctx_fast_cluster": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.POINTER(Stats)]),
@@ -275,6 +276,13 @@ class Context:
                                                _ptr(out), C.byref(st)),
                "ngia_ctx_align_pairs_host")
         return out, st.as_dict()
+
+    def use_graphs(self, on: bool) -> bool:
+        """Capture/replay the batched round as a CUDA graph; returns the old setting."""
+        r = lib().ngia_ctx_use_graphs(self._h, 1 if on else 0)
+        if r < 0:
+            _check(r, "ngia_ctx_use_graphs")
+        return bool(r)
 
     def align_pairs_device(self, d_pairs: int, count: int, identity: int,
                            d_scores: int) -> dict:

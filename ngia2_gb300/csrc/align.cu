@@ -69,33 +69,32 @@ align_jobs_dev_count_kernel(const uint32_t *__restrict__ packed,
   }
 }
 
-// Batched form, register-plane window or general kernel: pairs of one width
-// class, listed in `order[begin, end)`.
-template <int W>
+// The batched kernels read their class's range of the queue order from
+// device memory (bounds[cls] .. bounds[cls + 1], written by the classifier),
+// so that a round needs no host round trip and can be captured as a graph.
+
+// Batched form, general kernel: one pair per thread, grid-stride over the
+// class's range.
 __global__ void __launch_bounds__(128)
-align_class_kernel(const uint32_t *__restrict__ packed,
-                   const uint64_t *__restrict__ offs, const uint2 *__restrict__ pairs,
-                   const uint32_t *__restrict__ order, uint32_t begin, uint32_t end,
-                   uint32_t *__restrict__ scores, float t, int fma_mode,
-                   unsigned long long *__restrict__ work) {
-  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+align_general_kernel(const uint32_t *__restrict__ packed,
+                     const uint64_t *__restrict__ offs, const uint2 *__restrict__ pairs,
+                     const uint32_t *__restrict__ order, const uint32_t *__restrict__ bounds,
+                     int cls, uint32_t *__restrict__ scores, float t, int fma_mode,
+                     unsigned long long *__restrict__ work) {
+  const uint32_t begin = bounds[cls], end = bounds[cls + 1];
   uint32_t done = 0;
-  if (k < end) {
+  for (uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x; k < end;
+       k += gridDim.x * blockDim.x) {
     const uint32_t p = order[k];
     const uint2 pr = pairs[p];
     const uint32_t *rep = packed + offs[pr.x];
     const uint32_t *tar = packed + offs[pr.y];
     const uint32_t lr = __ldg(rep), lt = __ldg(tar);
     const Band b = make_band(lr, lt, t, fma_mode);
-    uint32_t lcs, blocks;
-    if constexpr (W > 0) {
-      lcs = lcs_window<W>(rep, tar, b, blocks);
-      done = blocks * W;
-    } else {
-      uint32_t lines[kMaxRowBlocks];
-      lcs = lcs_general(rep, tar, b, lines, blocks);
-      done = blocks * ((b.width + 7u) & ~7u);
-    }
+    uint32_t lines[kMaxRowBlocks];
+    uint32_t blocks;
+    const uint32_t lcs = lcs_general(rep, tar, b, lines, blocks);
+    done += blocks * ((b.width + 7u) & ~7u);
     scores[p] = identity_score(lcs, lr, lt, t);
   }
   count_work(done, work);
@@ -108,12 +107,13 @@ __global__ void __launch_bounds__(kGroupThreads)
 align_group_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
                    uint64_t inv, const uint64_t *__restrict__ offs,
                    const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,
-                   uint32_t begin, uint32_t end, unsigned int *__restrict__ cursor,
-                   uint32_t *__restrict__ scores, float t, int fma_mode,
-                   unsigned long long *__restrict__ work) {
+                   const uint32_t *__restrict__ bounds, int cls,
+                   unsigned int *__restrict__ cursor, uint32_t *__restrict__ scores, float t,
+                   int fma_mode, unsigned long long *__restrict__ work) {
   extern __shared__ uint32_t smem[];
-  const uint32_t done = align_group<G, K, KC>(packed, nib, inv, offs, pairs, order, begin, end,
-                                              cursor, scores, t, fma_mode, smem);
+  const uint32_t done = align_group<G, K, KC>(packed, nib, inv, offs, pairs, order,
+                                              bounds[cls], bounds[cls + 1], cursor, scores, t,
+                                              fma_mode, smem);
   count_work(done, work);
 }
 
@@ -124,12 +124,12 @@ __global__ void __launch_bounds__(kStreamThreads)
 align_stream_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
                     uint64_t inv, const uint64_t *__restrict__ offs,
                     const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,
-                    uint32_t begin, uint32_t end, unsigned int *__restrict__ cursor,
-                    uint32_t *__restrict__ scores, float t, int fma_mode,
-                    unsigned long long *__restrict__ work) {
+                    const uint32_t *__restrict__ bounds, int cls,
+                    unsigned int *__restrict__ cursor, uint32_t *__restrict__ scores, float t,
+                    int fma_mode, unsigned long long *__restrict__ work) {
   extern __shared__ uint32_t smem[];
-  const uint32_t done = align_stream<W, K>(packed, nib, inv, offs, pairs, order, begin, end,
-                                           cursor, scores, t, fma_mode, smem);
+  const uint32_t done = align_stream<W, K>(packed, nib, inv, offs, pairs, order, bounds[cls],
+                                           bounds[cls + 1], cursor, scores, t, fma_mode, smem);
   count_work(done, work);
 }
 
@@ -246,63 +246,56 @@ static int persistent_grid(F func, int threads, size_t smem, uint32_t want, uint
   return NGIA_OK;
 }
 
+// Launch arguments shared by every class of one batched round.
+struct RoundArgs {
+  const uint32_t *packed, *nib;
+  uint64_t inv;
+  const uint64_t *offs;
+  const uint2 *pairs;
+  const uint32_t *order, *bounds;
+  uint32_t *scores;
+  float t;
+  int fm;
+  unsigned long long *work;
+};
+
 template <int W, int K>
-static int launch_stream_k(const uint32_t *packed, const uint32_t *nib, uint64_t inv,
-                           const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
-                           uint32_t begin, uint32_t end, unsigned int *cursor,
-                           uint32_t *scores, float t, int fm, unsigned long long *work,
+static int launch_stream_k(const RoundArgs &a, int cls, unsigned int *cursor,
                            cudaStream_t s) {
   constexpr size_t smem = stream_smem_bytes(W, K);
   uint32_t grid = 0;
-  NGIA_TRY(persistent_grid(align_stream_kernel<W, K>, kStreamThreads, smem,
-                           ceil_div(end - begin, (uint32_t)kStreamThreads), &grid));
+  NGIA_TRY(persistent_grid(align_stream_kernel<W, K>, kStreamThreads, smem, kFull, &grid));
   align_stream_kernel<W, K><<<grid, kStreamThreads, smem, s>>>(
-      packed, nib, inv, offs, pairs, order, begin, end, cursor, scores, t, fm, work);
+      a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls, cursor, a.scores, a.t,
+      a.fm, a.work);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
 
 template <int G, int K, int KC>
-static int launch_group_k(const uint32_t *packed, const uint32_t *nib, uint64_t inv,
-                          const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
-                          uint32_t begin, uint32_t end, unsigned int *cursor,
-                          uint32_t *scores, float t, int fm, unsigned long long *work,
-                          cudaStream_t s) {
+static int launch_group_k(const RoundArgs &a, int cls, unsigned int *cursor, cudaStream_t s) {
   constexpr size_t smem = group_smem_bytes(K, KC);
-  constexpr uint32_t groups_per_block = kGroupThreads / G;
   uint32_t grid = 0;
-  NGIA_TRY(persistent_grid(align_group_kernel<G, K, KC>, kGroupThreads, smem,
-                           ceil_div(end - begin, groups_per_block), &grid));
+  NGIA_TRY(persistent_grid(align_group_kernel<G, K, KC>, kGroupThreads, smem, kFull, &grid));
   align_group_kernel<G, K, KC><<<grid, kGroupThreads, smem, s>>>(
-      packed, nib, inv, offs, pairs, order, begin, end, cursor, scores, t, fm, work);
+      a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls, cursor, a.scores, a.t,
+      a.fm, a.work);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
 
-template <int G, int K>
-static int launch_group(const uint32_t *packed, const uint32_t *nib, const Alphabet &ab,
-                        const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
-                        uint32_t begin, uint32_t end, unsigned int *cursor,
-                        uint32_t *scores, float t, int fm, unsigned long long *work,
-                        cudaStream_t s) {
-  if (ab.K == 8)
-    return launch_group_k<G, K, 8>(packed, nib, ab.inv, offs, pairs, order, begin, end,
-                                   cursor, scores, t, fm, work, s);
-  return launch_group_k<G, K, 16>(packed, nib, ab.inv, offs, pairs, order, begin, end, cursor,
-                                  scores, t, fm, work, s);
+template <int W>
+static int launch_stream(const RoundArgs &a, int K, int cls, unsigned int *cursor,
+                         cudaStream_t s) {
+  return K == 8 ? launch_stream_k<W, 8>(a, cls, cursor, s)
+                : launch_stream_k<W, 16>(a, cls, cursor, s);
 }
 
-template <int W>
-static int launch_stream(const uint32_t *packed, const uint32_t *nib, const Alphabet &ab,
-                         const uint64_t *offs, const uint2 *pairs, const uint32_t *order,
-                         uint32_t begin, uint32_t end, unsigned int *cursor,
-                         uint32_t *scores, float t, int fm, unsigned long long *work,
-                         cudaStream_t s) {
-  if (ab.K == 8)
-    return launch_stream_k<W, 8>(packed, nib, ab.inv, offs, pairs, order, begin, end, cursor,
-                                 scores, t, fm, work, s);
-  return launch_stream_k<W, 16>(packed, nib, ab.inv, offs, pairs, order, begin, end, cursor,
-                                scores, t, fm, work, s);
+template <int G, int K>
+static int launch_group(const RoundArgs &a, int KC, int cls, unsigned int *cursor,
+                        cudaStream_t s) {
+  return KC == 8 ? launch_group_k<G, K, 8>(a, cls, cursor, s)
+                 : launch_group_k<G, K, 16>(a, cls, cursor, s);
 }
 
 int launch_align_jobs(const uint32_t *packed, const uint64_t *offs, uint32_t *jobs,
@@ -328,30 +321,21 @@ int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
 
 int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const Alphabet &ab, const uint64_t *offs, const uint2 *pairs,
-                       const uint32_t *order, uint32_t begin, uint32_t end,
-                       uint32_t *scores, uint32_t identity, unsigned long long *work,
-                       unsigned int *cursor, cudaStream_t s) {
-  if (end <= begin) return NGIA_OK;
-  const float t = identity_threshold(identity);
-  const int fm = round_mode();
-  const uint32_t blocks = ceil_div(end - begin, 128u);
-#define NGIA_LDS_CASE(C, W)                                                          \
-  case C:                                                                            \
-    return launch_stream<W>(packed, nib, ab, offs, pairs, order, begin, end, cursor, \
-                            scores, t, fm, work, s);
+                       const uint32_t *order, const uint32_t *bounds, uint32_t *scores,
+                       uint32_t identity, unsigned long long *work, unsigned int *cursor,
+                       cudaStream_t s) {
+  const RoundArgs a{packed, nib, ab.inv, offs, pairs, order, bounds, scores,
+                    identity_threshold(identity), round_mode(), work};
   switch (cls) {
-    NGIA_LDS_CASE(0, 4)
-    NGIA_LDS_CASE(1, 6)
-    NGIA_LDS_CASE(2, 8)
-    NGIA_LDS_CASE(3, 10)
-    NGIA_LDS_CASE(4, 12)
-    NGIA_LDS_CASE(5, 14)
-    NGIA_LDS_CASE(6, 16)
-#undef NGIA_LDS_CASE
-#define NGIA_GROUP_CASE(C)                                                              \
-  case C:                                                                               \
-    return launch_group<group_shape(C).G, group_shape(C).K>(                            \
-        packed, nib, ab, offs, pairs, order, begin, end, cursor, scores, t, fm, work, s);
+    case 0: return launch_stream<4>(a, ab.K, cls, cursor, s);
+    case 1: return launch_stream<6>(a, ab.K, cls, cursor, s);
+    case 2: return launch_stream<8>(a, ab.K, cls, cursor, s);
+    case 3: return launch_stream<10>(a, ab.K, cls, cursor, s);
+    case 4: return launch_stream<12>(a, ab.K, cls, cursor, s);
+    case 5: return launch_stream<14>(a, ab.K, cls, cursor, s);
+    case 6: return launch_stream<16>(a, ab.K, cls, cursor, s);
+#define NGIA_GROUP_CASE(C) \
+  case C: return launch_group<group_shape(C).G, group_shape(C).K>(a, ab.K, cls, cursor, s);
     NGIA_GROUP_CASE(7)
     NGIA_GROUP_CASE(8)
     NGIA_GROUP_CASE(9)
@@ -359,11 +343,16 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
     NGIA_GROUP_CASE(11)
     NGIA_GROUP_CASE(12)
 #undef NGIA_GROUP_CASE
-    case kGeneralClass: align_class_kernel<0><<<blocks, 128, 0, s>>>(packed, offs, pairs, order, begin, end, scores, t, fm, work); break;
+    case kGeneralClass: {
+      uint32_t grid = 0;
+      NGIA_TRY(persistent_grid(align_general_kernel, 128, 0, kFull, &grid));
+      align_general_kernel<<<grid, 128, 0, s>>>(packed, offs, pairs, order, bounds, cls, scores,
+                                                a.t, a.fm, work);
+      NGIA_LAUNCHED();
+      return NGIA_OK;
+    }
     default: return NGIA_ERR_ARG;
   }
-  NGIA_LAUNCHED();
-  return NGIA_OK;
 }
 
 }  // namespace ngia

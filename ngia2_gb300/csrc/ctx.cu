@@ -25,6 +25,10 @@ int round_mode() { return g_round_mode; }
 static std::atomic<unsigned long long> g_launches(0);
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+// Every device (re)allocation of the contexts bumps this, so that a captured
+// graph, whose nodes hold buffer addresses, is known to be stale.
+static std::atomic<uint64_t> g_alloc_gen{0};
+
 // Grow-only device buffer.
 struct DevBuf {
   void *p = nullptr;
@@ -34,6 +38,7 @@ struct DevBuf {
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
+    ++g_alloc_gen;
     if (want == 0) return NGIA_OK;
     cudaError_t e = cudaMalloc(&p, want);
     if (e != cudaSuccess) {
@@ -72,6 +77,20 @@ struct ngia_ctx {
   ngia::DevBuf ucount, uoff, counters, pairs, scores, cls, cls_sorted, order, sort_tmp,
       emit_tmp, edges, scan_tmp, jobs;
   uint64_t n_edges = 0;
+  // the batched round of ngia_ctx_align_pairs as a CUDA graph, replayed while
+  // its inputs (addresses, count, identity, rounding, allocations) match
+  bool use_graphs = true;
+  cudaGraphExec_t round_exec = nullptr;
+  struct RoundKey {
+    const void *pairs, *scores, *nib;
+    uint32_t m, identity;
+    int round_mode;
+    uint64_t alloc_gen;
+    bool operator==(const RoundKey &o) const {
+      return pairs == o.pairs && scores == o.scores && nib == o.nib && m == o.m &&
+             identity == o.identity && round_mode == o.round_mode && alloc_gen == o.alloc_gen;
+    }
+  } round_key{};
 };
 
 namespace ngia {
@@ -84,6 +103,7 @@ struct Counters {  // device-side counters of one graph build
   uint32_t fast_count;
   unsigned long long work;  // 32x32 blocks the aligners computed
   unsigned int cursor[kNumClasses];  // pairs taken from each class's queue
+  uint32_t bounds[kNumClasses + 1];  // class ranges of the queue order
 };
 
 static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
@@ -115,37 +135,40 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
   return NGIA_OK;
 }
 
-// The batched aligner over m pairs on the device: width classes (classify),
-// class-major queue order with the longest targets first (one radix pass),
-// scores zeroed, then one persistent launch per class, widest first.  Records
-// event ev_first (classification start is the caller's) after the class
-// counts reach the host and ev_first + 1 after the last launch.
-static int align_batched(ngia_ctx *c, const uint2 *pairs, uint32_t m, uint32_t identity,
-                         uint32_t *scores, Counters *dc, Counters *hc, int ev_first) {
-  cudaStream_t s = c->stream;
+// Scratch of a batched round over m pairs (reserved before any capture).
+static int align_reserve(ngia_ctx *c, uint32_t m) {
+  NGIA_TRY(c->counters.reserve(sizeof(Counters)));
   NGIA_TRY(c->cls.reserve((size_t)(m ? m : 1) * 4));
   NGIA_TRY(c->cls_sorted.reserve((size_t)(m ? m : 1) * 4));
   NGIA_TRY(c->order.reserve((size_t)(m ? m : 1) * 4));
-  NGIA_TRY(c->sort_tmp.reserve(radix_sort_scratch_bytes(m, 1)));
+  NGIA_TRY(c->sort_tmp.reserve(radix_sort_scratch_bytes(m ? m : 1, 1)));
+  return NGIA_OK;
+}
+
+// The batched aligner over m pairs on the device, all stream-ordered with no
+// host round trip (capturable): width classes and their bounds (classify),
+// class-major queue order with the longest targets first (one radix pass),
+// scores zeroed, then one persistent launch per class, widest first; empty
+// classes' grids find their queue empty and return.  ev_first >= 0 records
+// events ev_first (classified) and ev_first + 1 (aligned).  *dc must be zero.
+static int align_batched(ngia_ctx *c, const uint2 *pairs, uint32_t m, uint32_t identity,
+                         uint32_t *scores, Counters *dc, int ev_first) {
+  cudaStream_t s = c->stream;
   NGIA_TRY(classify(c->lens.as<uint32_t>(), pairs, m, identity, c->cls.as<uint32_t>(),
-                    dc->class_count, &dc->cells, s));
+                    dc->class_count, &dc->cells, dc->bounds, s));
   NGIA_TRY(radix_sort_pairs(c->cls.as<uint32_t>(), nullptr, c->cls_sorted.as<uint32_t>(),
                             c->order.as<uint32_t>(), m, 1, 0, kClassKeyBits, c->sort_tmp.p,
                             s));
   NGIA_CUDA(cudaMemsetAsync(scores, 0, (size_t)(m ? m : 1) * 4, s));
-  NGIA_CUDA(cudaMemcpyAsync(hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
-  NGIA_CUDA(cudaEventRecord(c->ev[ev_first], s));
-  NGIA_CUDA(cudaStreamSynchronize(s));
-  uint32_t begin[kNumClasses + 1];
-  begin[0] = 0;
-  for (int k = 0; k < kNumClasses; ++k) begin[k + 1] = begin[k] + hc->class_count[k];
+  if (ev_first >= 0) NGIA_CUDA(cudaEventRecord(c->ev[ev_first], s));
   const int launch_order[] = {kGeneralClass, 12, 11, 10, 9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
-  for (int cl : launch_order)
-    NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->align_nib, c->ab,
-                                c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
-                                begin[cl], begin[cl + 1], scores, identity, &dc->work,
-                                &dc->cursor[cl], s));
-  NGIA_CUDA(cudaEventRecord(c->ev[ev_first + 1], s));
+  if (m > 0)
+    for (int cl : launch_order)
+      NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->align_nib, c->ab,
+                                  c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
+                                  dc->bounds, scores, identity, &dc->work, &dc->cursor[cl],
+                                  s));
+  if (ev_first >= 0) NGIA_CUDA(cudaEventRecord(c->ev[ev_first + 1], s));
   return NGIA_OK;
 }
 
@@ -182,7 +205,8 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   uint32_t *scores = c->scores.as<uint32_t>();
   NGIA_TRY(collect_write(rep, lens, n, bands, identity, c->uoff.as<uint64_t>(), pairs, s));
   // 2-3. width classes, then one persistent launch per class
-  NGIA_TRY(align_batched(c, pairs, m, identity, scores, dc, &hc, 1));
+  NGIA_TRY(align_reserve(c, m));
+  NGIA_TRY(align_batched(c, pairs, m, identity, scores, dc, 1));
   // 4. emit: compact hits, sort by (rep, tar)
   NGIA_TRY(c->emit_tmp.reserve(emit_scratch_bytes(m, n)));
   NGIA_TRY(c->edges.reserve((size_t)(m ? m : 1) * sizeof(ngia_edge)));
@@ -193,12 +217,11 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   c->n_edges = ne;
   if (h_n_edges) *h_n_edges = ne;
   if (st) {
-    unsigned long long work = 0;
-    NGIA_CUDA(cudaMemcpy(&work, &dc->work, sizeof(work), cudaMemcpyDeviceToHost));
+    NGIA_CUDA(cudaMemcpy(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost));
     st->candidate_pairs = hc.cand_total;
     st->unique_pairs = total;
     st->aligned_cells = hc.cells;
-    st->computed_cells = work * 1024ull;
+    st->computed_cells = hc.work * 1024ull;
     st->edges = ne;
     st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
     st->ms_align = ev_ms(c->ev[1], c->ev[2]);
@@ -208,7 +231,9 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
 }
 
 // The batched aligner on caller-given pairs (device arrays) of the resident
-// database.  Every index must be below the record count.
+// database.  Every index must be below the record count.  With graphs on, the
+// round is captured once per (pairs, scores, count, identity, rounding,
+// allocations) and replayed.
 int ctx_align_pairs(ngia_ctx *c, const uint2 *d_pairs, uint32_t m, uint32_t identity,
                     uint32_t *d_scores, ngia_stats *st) {
   if (c->n == 0) return NGIA_ERR_STATE;
@@ -216,22 +241,56 @@ int ctx_align_pairs(ngia_ctx *c, const uint2 *d_pairs, uint32_t m, uint32_t iden
   if (st) std::memset(st, 0, sizeof(*st));
   if (m == 0) return NGIA_OK;
   cudaStream_t s = c->stream;
-  NGIA_TRY(c->counters.reserve(sizeof(Counters)));
+  NGIA_TRY(align_reserve(c, m));
   Counters *dc = c->counters.as<Counters>();
-  NGIA_CUDA(cudaMemsetAsync(dc, 0, sizeof(Counters), s));
-  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
-  Counters hc;
-  NGIA_TRY(align_batched(c, d_pairs, m, identity, d_scores, dc, &hc, 1));
+  if (c->use_graphs) {
+    const ngia_ctx::RoundKey key{d_pairs, d_scores, c->align_nib, m, identity, round_mode(),
+                                 g_alloc_gen.load()};
+    if (!c->round_exec || !(key == c->round_key)) {
+      if (c->round_exec) cudaGraphExecDestroy(c->round_exec);
+      c->round_exec = nullptr;
+      NGIA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+      int rc = NGIA_OK;
+      const cudaError_t e0 = cudaMemsetAsync(dc, 0, sizeof(Counters), s);
+      if (e0 != cudaSuccess) rc = cuda_fail(e0);
+      if (rc == NGIA_OK) rc = align_batched(c, d_pairs, m, identity, d_scores, dc, -1);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e1 = cudaStreamEndCapture(s, &graph);
+      if (rc == NGIA_OK && e1 != cudaSuccess) rc = cuda_fail(e1);
+      if (rc == NGIA_OK) {
+        const cudaError_t e2 = cudaGraphInstantiate(&c->round_exec, graph, 0);
+        if (e2 != cudaSuccess) rc = cuda_fail(e2);
+      }
+      if (graph) cudaGraphDestroy(graph);
+      if (rc != NGIA_OK) {
+        c->round_exec = nullptr;
+        return rc;
+      }
+      c->round_key = key;
+    }
+    NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+    NGIA_CUDA(cudaGraphLaunch(c->round_exec, s));
+    NGIA_CUDA(cudaEventRecord(c->ev[2], s));
+    NGIA_CUDA(cudaEventRecord(c->ev[1], s));  // no split inside a graph
+  } else {
+    NGIA_CUDA(cudaMemsetAsync(dc, 0, sizeof(Counters), s));
+    NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+    NGIA_TRY(align_batched(c, d_pairs, m, identity, d_scores, dc, 1));
+  }
   NGIA_CUDA(cudaEventSynchronize(c->ev[2]));
   if (st) {
-    unsigned long long work = 0;
-    NGIA_CUDA(cudaMemcpy(&work, &dc->work, sizeof(work), cudaMemcpyDeviceToHost));
+    Counters hc;
+    NGIA_CUDA(cudaMemcpy(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost));
     st->candidate_pairs = m;
     st->unique_pairs = m;
     st->aligned_cells = hc.cells;
-    st->computed_cells = work * 1024ull;
-    st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
-    st->ms_align = ev_ms(c->ev[1], c->ev[2]);
+    st->computed_cells = hc.work * 1024ull;
+    if (c->use_graphs) {
+      st->ms_align = ev_ms(c->ev[0], c->ev[2]);
+    } else {
+      st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
+      st->ms_align = ev_ms(c->ev[1], c->ev[2]);
+    }
   }
   return NGIA_OK;
 }
@@ -378,6 +437,7 @@ void ngia_ctx_destroy(ngia_ctx *c) {
                           &c->cls,    &c->cls_sorted, &c->order, &c->sort_tmp,
                           &c->emit_tmp, &c->edges, &c->scan_tmp, &c->jobs};
   for (ngia::DevBuf *b : bufs) b->release();
+  if (c->round_exec) cudaGraphExecDestroy(c->round_exec);
   for (int k = 0; k < 8; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -444,6 +504,13 @@ int ngia_ctx_align_pairs(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count,
   if (!c || (count && (!d_pairs || !d_scores))) return NGIA_ERR_ARG;
   return ngia::ctx_align_pairs(c, reinterpret_cast<const uint2 *>(d_pairs), count, identity,
                                d_scores, stats);
+}
+
+int ngia_ctx_use_graphs(ngia_ctx *c, int on) {
+  if (!c) return NGIA_ERR_ARG;
+  const int old = c->use_graphs ? 1 : 0;
+  c->use_graphs = on != 0;
+  return old;
 }
 
 int ngia_ctx_align_pairs_host(ngia_ctx *c, const uint32_t *h_pairs, uint32_t count,

@@ -41,13 +41,14 @@ struct Alphabet {
   int K;         // 8 or 16 table entries per row block
   uint64_t inv;  // nibble d = residue code of aligner code d
 };
-// One width class of the batched aligner over order[begin, end).  `cursor`
-// (device, zero before the launch) is the queue head of the streaming classes.
+// One width class of the batched aligner: a persistent launch over
+// order[bounds[cls], bounds[cls + 1]) (device bounds, from classify).  `cursor`
+// (device, zero before the launch) is the class's queue head.
 int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const Alphabet &ab, const uint64_t *offs, const uint2 *pairs,
-                       const uint32_t *order, uint32_t begin, uint32_t end,
-                       uint32_t *scores, uint32_t identity, unsigned long long *work,
-                       unsigned int *cursor, cudaStream_t s);
+                       const uint32_t *order, const uint32_t *bounds, uint32_t *scores,
+                       uint32_t identity, unsigned long long *work, unsigned int *cursor,
+                       cudaStream_t s);
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
                    uint32_t *presence, cudaStream_t s);
 int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
@@ -60,9 +61,13 @@ int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_
 int collect_write(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
                   uint32_t identity, const uint64_t *offsets, uint2 *pairs,
                   cudaStream_t s);
+// Width class sort keys of `count` pairs, per-class counts (added to
+// class_count), band cells (added to *cells) and the class bounds of the
+// class-major order (bounds[c] = pairs in classes below c; kNumClasses + 1
+// entries, written after the counts are complete).
 int classify(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t identity,
              uint32_t *cls, unsigned int *class_count, unsigned long long *cells,
-             cudaStream_t s);
+             uint32_t *bounds, cudaStream_t s);
 int bits_for(uint32_t max_value);
 size_t emit_scratch_bytes(uint32_t count, uint32_t n_nodes);
 int emit_sorted(const uint2 *pairs, const uint32_t *scores, uint32_t count,

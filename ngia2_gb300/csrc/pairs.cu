@@ -148,17 +148,32 @@ classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pai
   if (threadIdx.x == 0 && scells) atomicAdd(cells, scells * 1024ull);
 }
 
+__global__ void class_bounds_kernel(const unsigned int *__restrict__ class_count,
+                                    uint32_t *__restrict__ bounds) {
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int c = 0; c < kNumClasses; ++c) {
+      bounds[c] = run;
+      run += class_count[c];
+    }
+    bounds[kNumClasses] = run;
+  }
+}
+
 int classify(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t identity,
              uint32_t *cls, unsigned int *class_count, unsigned long long *cells,
-             cudaStream_t s) {
-  if (count == 0) return NGIA_OK;
-  int dev = 0, sms = 0;
-  NGIA_CUDA(cudaGetDevice(&dev));
-  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const uint32_t want = ceil_div(count, 256u), cap = (uint32_t)sms * 8;
-  classify_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
-      lens, pairs, count, identity_threshold(identity), round_mode(), cls, class_count,
-      cells);
+             uint32_t *bounds, cudaStream_t s) {
+  if (count > 0) {
+    int dev = 0, sms = 0;
+    NGIA_CUDA(cudaGetDevice(&dev));
+    NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const uint32_t want = ceil_div(count, 256u), cap = (uint32_t)sms * 8;
+    classify_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
+        lens, pairs, count, identity_threshold(identity), round_mode(), cls, class_count,
+        cells);
+    NGIA_LAUNCHED();
+  }
+  class_bounds_kernel<<<1, 32, 0, s>>>(class_count, bounds);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

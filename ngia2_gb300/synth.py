@@ -72,8 +72,9 @@ def _draw(rng, alphabet, freqs, k):
 
 
 def _mutate_chunk(rng, roots, root_lens, per_family, alphabet, freqs, sub_lo, sub_hi,
-                  indel_rate, indel_mean):
-    """Members of a chunk of families; returns (residues, lens, family ids)."""
+                  indel_rate, indel_mean, with_root=False):
+    """Members of a chunk of families; returns (residues, lens, family ids).
+    with_root: member 0 of every family is the root itself."""
     fam = np.repeat(np.arange(len(root_lens)), per_family)
     mlen = root_lens[fam]
     root_start = np.concatenate([[0], np.cumsum(root_lens)[:-1]])
@@ -82,12 +83,17 @@ def _mutate_chunk(rng, roots, root_lens, per_family, alphabet, freqs, sub_lo, su
     member_start = np.concatenate([[0], np.cumsum(mlen)[:-1]])
     pos_in = np.arange(total) - member_start[member_of]
     base = roots[root_start[fam][member_of] + pos_in]
+    first = np.concatenate([[True], fam[1:] != fam[:-1]])  # member 0 of each family
     # substitutions
     rate = rng.uniform(sub_lo, sub_hi, size=len(fam)).astype(np.float32)
+    ind = np.full(len(fam), indel_rate, dtype=np.float32)
+    if with_root:
+        rate[first] = 0.0
+        ind[first] = 0.0
     sub = rng.random(total, dtype=np.float32) < rate[member_of]
     base[sub] = _draw(rng, alphabet, freqs, int(sub.sum()))
     # indel events
-    ev = np.flatnonzero(rng.random(total, dtype=np.float32) < indel_rate)
+    ev = np.flatnonzero(rng.random(total, dtype=np.float32) < ind[member_of])
     is_del = rng.random(len(ev)) < 0.5
     length = rng.geometric(1.0 / indel_mean, size=len(ev))
     member_end = (member_start + mlen)[member_of]
@@ -114,7 +120,8 @@ def _mutate_chunk(rng, roots, root_lens, per_family, alphabet, freqs, sub_lo, su
 
 
 def families(n_seqs, n_families, alphabet, freqs, root_len_fn, sub_lo, sub_hi, indel_rate,
-             indel_mean, seed, chunk_families=2000, prefix=b"fam") -> SeqSet:
+             indel_mean, seed, chunk_families=2000, prefix=b"fam",
+             with_root=False) -> SeqSet:
     rng = np.random.default_rng(seed)
     per = np.full(n_families, n_seqs // n_families, dtype=np.int64)
     per[: n_seqs - int(per.sum())] += 1
@@ -124,7 +131,7 @@ def families(n_seqs, n_families, alphabet, freqs, root_len_fn, sub_lo, sub_hi, i
         rl = root_len_fn(rng, f1 - f0).astype(np.int64)
         roots = _draw(rng, alphabet, freqs, int(rl.sum()))
         out, lens, fam = _mutate_chunk(rng, roots, rl, per[f0:f1], alphabet, freqs, sub_lo,
-                                       sub_hi, indel_rate, indel_mean)
+                                       sub_hi, indel_rate, indel_mean, with_root)
         res_parts.append(out)
         len_parts.append(lens)
         fam_parts.append(fam + f0)
@@ -169,3 +176,68 @@ def protein_families(n_seqs=20_000, n_families=2_000, seed=1) -> SeqSet:
 def dna_families(n_seqs=200_000, n_families=20_000, seed=2) -> SeqSet:
     return families(n_seqs, n_families, NUCLEO, NUCLEO_FREQ, _uniform_roots(200, 3000),
                     0.01, 0.10, 0.01, 2.0, seed, prefix=b"dna")
+
+
+def _heavy_tailed_roots(rng, k):
+    """80 % log-normal (median 250, sigma 0.5, at least 10), 19 % uniform
+    1,000-5,000, 1 % uniform 5,000-35,000."""
+    u = rng.random(k)
+    out = np.clip(np.round(rng.lognormal(np.log(250), 0.5, size=k)), 10, 5000)
+    mid = (u >= 0.80) & (u < 0.99)
+    out[mid] = rng.integers(1000, 5001, size=int(mid.sum()))
+    top = u >= 0.99
+    out[top] = rng.integers(5000, 35001, size=int(top.sum()))
+    return out
+
+
+class PairSet:
+    """A database in index order (length descending, as makedb orders it) and
+    candidate pairs (rep, tar) of indices with rep < tar."""
+
+    def __init__(self, seqs: SeqSet, pairs: np.ndarray, related: np.ndarray):
+        self.seqs = seqs
+        self.pairs = pairs
+        self.related = related
+
+
+def protein_pairs(n_pairs=2_000_000, seed=3, family_size=5, window=64) -> PairSet:
+    """Heavy-tailed protein candidate pairs: half are pairs within one family
+    (the root and members at 50-99 % identity to it: 1-50 % substitutions,
+    1 % indels of mean length 2; every pair of the family's sequences), half
+    pair unrelated sequences of similar length (a random partner within
+    `window` places in length order, from another family)."""
+    rng = np.random.default_rng(seed)
+    per_family = family_size * (family_size - 1) // 2
+    n_fam = max(1, (n_pairs // 2 + per_family - 1) // per_family)
+    fams = families(n_fam * family_size, n_fam, AMINO, AMINO_FREQ, _heavy_tailed_roots,
+                    0.01, 0.50, 0.01, 2.0, seed, prefix=b"pair", with_root=True)
+    fam_of = np.array([int(nm[5:].split(b"_")[0]) for nm in fams.names], dtype=np.int64)
+    # index order: length descending, stable in generation order
+    order = np.argsort(-fams.lens, kind="stable")
+    idx = _gather_runs(fams.starts[order], fams.lens[order])
+    seqs = SeqSet(fams.residues[idx], fams.lens[order], [fams.names[i] for i in order])
+    fam = fam_of[order]
+    # related pairs: every pair of members of a family
+    by_fam = np.argsort(fam, kind="stable")
+    members = by_fam.reshape(n_fam, family_size)
+    a, b = np.triu_indices(family_size, 1)
+    rel = np.stack([members[:, a].reshape(-1), members[:, b].reshape(-1)], axis=1)
+    rel = rel[: n_pairs // 2]
+    # unrelated pairs: neighbours in length order from other families
+    n_un = n_pairs - len(rel)
+    i = rng.integers(0, len(seqs), size=n_un)
+    j = np.clip(i + rng.integers(1, window + 1, size=n_un) * rng.choice([-1, 1], size=n_un),
+                0, len(seqs) - 1)
+    ok = (fam[i] != fam[j]) & (i != j)
+    while not ok.all():  # redraw inside the window around i
+        bad = np.flatnonzero(~ok)
+        lo = np.maximum(i[bad] - window, 0)
+        hi = np.minimum(i[bad] + window, len(seqs) - 1)
+        j[bad] = lo + (rng.random(len(bad)) * (hi - lo + 1)).astype(np.int64)
+        ok = (fam[i] != fam[j]) & (i != j)
+    un = np.stack([i, j], axis=1)
+    pairs = np.concatenate([rel, un])
+    pairs.sort(axis=1)  # rep = the lower index = the longer record
+    related = np.concatenate([np.ones(len(rel), bool), np.zeros(n_un, bool)])
+    perm = rng.permutation(len(pairs))
+    return PairSet(seqs, pairs[perm].astype(np.uint32), related[perm])

@@ -76,9 +76,14 @@ def test_batched_pairs_match_oracle(cuda, built, identity):
     want = oracle.align_pairs(packed, offs, pairs, identity, oracle.ROUND_FMA)
     with ng.Context() as ctx:
         ctx.load(packed, offs, lens)
-        got, st = ctx.align_pairs(pairs, identity)
-        # twice: the queues and counters start over on every call
+        got, st = ctx.align_pairs(pairs, identity)  # captures the round as a graph
+        # replayed with other contents: queues and counters start over
         again, _ = ctx.align_pairs(pairs[::-1], identity)
+        ctx.use_graphs(False)
+        eager, st_eager = ctx.align_pairs(pairs, identity)
+    assert np.array_equal(eager, got)
+    assert st_eager["computed_cells"] == st["computed_cells"]
+    assert st_eager["aligned_cells"] == st["aligned_cells"]
     classes = {width_class(int(lens[r]), int(lens[t]), identity) for r, t in pairs}
     bad = np.nonzero(got != want)[0]
     assert len(bad) == 0, [(int(pairs[i, 0]), int(pairs[i, 1]), int(lens[pairs[i, 0]]),
