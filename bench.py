@@ -19,6 +19,10 @@ e2e     the same through ngia_ctx_run_host on pinned host buffers: H2D of the
         path (makedb pack+sketch+group, buildGraph candidates+align+emit;
         the reference code built as a host OpenMP program) on a bounded
         sample of the workload with all host cores.
+pairs   (one GPU) aligned cells/s of the batched aligner against the plain
+        one-thread-per-pair form launched once per group, on 2,000,000
+        heavy-tailed protein candidate pairs at identity 90, scores compared
+        bit for bit (--pairs N to resize, 0 to skip; --pairs-only).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -83,6 +87,10 @@ def parse():
                    help="pairs of the batched-vs-plain leg (0 = skip it)")
     p.add_argument("--pairs-only", action="store_true",
                    help="run only the batched-vs-plain leg and print its object")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="batched leg with the default binning plan")
+    p.add_argument("--no-plain", action="store_true",
+                   help="skip the plain arm of the batched leg (profiling)")
     return p.parse_args()
 
 
@@ -429,6 +437,9 @@ def run_ours(args, world, rank, local, pg):
         "hbm_peak_gbs": peaks().get("hbm_gbs"),
     }
     ctx.close()
+    if world == 1 and args.pairs > 0:
+        # the batched-vs-plain leg on heavy-tailed protein pairs (one GPU)
+        line["pairs"] = run_pairs(args)
     if world == 1 and not args.no_cpu_baseline:
         try:
             # about 10 s of the reference's host code on all cores
@@ -544,22 +555,38 @@ def run_pairs(args) -> dict:
 
     steps = max(1, min(args.steps, PAIRS_MAX_STEPS))
     warm = max(1, min(args.warmup, 3))
+    # the default binning plan, then the one the autotuner picks on this round
+    # (a round's time hangs on its few longest pairs, so a sample misleads)
+    default_plan = ctx.plan()
+    for _ in range(warm):
+        batched()
+    t_default = min(timed(batched)[0] for _ in range(steps))
+    sample = m
+    t0 = time.time()
+    plan = default_plan
+    if not args.no_autotune:
+        plan, _ = ctx.autotune(d_pairs.data_ptr(), sample, PAIRS_IDENTITY, 2)
+    tune_s = time.time() - t0
     for _ in range(warm):
         batched()
     tb, st = [], None
     for _ in range(steps):
         t, st = timed(batched)
         tb.append(t)
-    plain()  # warm-up
     tp = []
-    for _ in range(min(steps, 3)):
-        t, _ = timed(plain)
-        tp.append(t)
+    if not args.no_plain:
+        plain()  # warm-up
+        for _ in range(min(steps, 3)):
+            t, _ = timed(plain)
+            tp.append(t)
     torch.cuda.synchronize()
     got = d_scores.cpu().numpy().view(np.uint32)
     ref = d_jobs.cpu().numpy().view(np.uint32).reshape(-1, 3)[:, 2]
     cells = st["aligned_cells"]
-    ms_b, ms_p = statistics.mean(tb), statistics.mean(tp)
+    ms_b = statistics.mean(tb)
+    ms_p = statistics.mean(tp) if tp else None
+    int_peak = ng.int32_peak(stream.cuda_stream)
+    ops = st["computed_cells"] / 32 * ALIGN_OPS_PER_WORD_STEP
     ctx.close()
     return {
         "workload": f"protein_pairs_{m}_heavy_tailed_id{PAIRS_IDENTITY}",
@@ -568,12 +595,19 @@ def run_pairs(args) -> dict:
                 "half the pairs within a family, half unrelated neighbours in length order",
         "metric": "aligned cells/s", "unit": "cells/s",
         "band_cells": cells, "computed_cells": st["computed_cells"],
-        "batched": {"value": cells / (ms_b * 1e-3), "ms": ms_b, "ms_classify": st["ms_pairs"],
-                    "ms_align": st["ms_align"], "steps": steps},
-        "plain": {"value": cells / (ms_p * 1e-3), "ms": ms_p, "launches": groups,
-                  "steps": len(tp)},
-        "batched_over_plain": ms_p / ms_b,
-        "scores_identical": bool(np.array_equal(got, ref)),
+        "batched": {"value": cells / (ms_b * 1e-3), "ms": ms_b, "steps": steps,
+                    "cuda_graph": True, "plan": plan, "autotune_s": tune_s,
+                    "autotune_sample_pairs": sample,
+                    "ms_default_plan": t_default, "default_plan": default_plan},
+        "plain": {"value": cells / (ms_p * 1e-3) if ms_p else None, "ms": ms_p,
+                  "launches": groups, "steps": len(tp)},
+        "batched_over_plain": ms_p / ms_b if ms_p else None,
+        "roofline": {"bound": "int32_alu", "kernel": "batched round (all width classes)",
+                     "achieved": ops / (ms_b * 1e-3) / 1e12, "peak": int_peak / 1e12,
+                     "unit": "Tops/s (32-bit lane ops)",
+                     "frac": ops / (ms_b * 1e-3) / int_peak,
+                     "units": {"computed_cells": st["computed_cells"]}},
+        "scores_identical": bool(np.array_equal(got, ref)) if tp else None,
         "hits": int((got > 0).sum()),
     }
 

@@ -193,6 +193,32 @@ int ngia_ctx_edges(ngia_ctx *ctx, ngia_edge *h_edges, uint64_t cap);
 int ngia_ctx_align_pairs(ngia_ctx *ctx, const uint32_t *d_pairs, uint32_t count,
                          uint32_t identity, uint32_t *d_scores, ngia_stats *stats);
 
+/* How the batched aligner bins pairs (what ngia_ctx_autotune picks).  Width
+ * classes: one pair per lane with a window of W = 4, 6, ..., 16 words for
+ * pairs whose window ls + min(rs, nr) (in 32-residue blocks) is at most
+ * stream_max; otherwise the first group class -- G lanes per pair with K
+ * words per lane: (16,1) (16,2) (16,4) (32,4) (32,8) (32,16) -- whose
+ * group_limit admits the band (ls + rs <= group_limit, or a rep of at most G
+ * slices); otherwise one pair per thread.  group_limit 0 leaves a class
+ * unused; a limit above (G-1)K + G is refused.  Scores never depend on the
+ * plan. */
+#define NGIA_GROUP_CLASSES 6
+typedef struct ngia_plan {
+  uint32_t stream_max; /* 4..16 */
+  uint32_t group_limit[NGIA_GROUP_CLASSES];
+} ngia_plan;
+
+int ngia_ctx_get_plan(ngia_ctx *ctx, ngia_plan *plan);
+int ngia_ctx_set_plan(ngia_ctx *ctx, const ngia_plan *plan);
+
+/* Times the batched round on the given device pairs (reps runs per
+ * candidate, the best kept) for plans around the current one -- the widest
+ * one-pair-per-lane window and each group class on or off -- by coordinate
+ * descent, and keeps the fastest as the context's plan.  *best_ms receives
+ * its time.  Synchronises. */
+int ngia_ctx_autotune(ngia_ctx *ctx, const uint32_t *d_pairs, uint32_t count,
+                      uint32_t identity, int reps, ngia_plan *best, double *best_ms);
+
 /* Whether ngia_ctx_align_pairs captures its round (classification, queue
  * sort and every class launch) as a CUDA graph and replays it while the
  * pair/score addresses, count, identity and rounding stay the same (default

@@ -55,6 +55,27 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+GROUP_SHAPES = [(16, 1), (16, 2), (16, 4), (32, 4), (32, 8), (32, 16)]  # (lanes, words)
+
+
+class Plan(C.Structure):
+    """ngia_plan: the widest one-pair-per-lane window and the widest band each
+    group class (GROUP_SHAPES) takes (0 = unused)."""
+    _fields_ = [("stream_max", C.c_uint32), ("group_limit", C.c_uint32 * len(GROUP_SHAPES))]
+
+    def as_dict(self) -> dict:
+        return {"stream_max": int(self.stream_max),
+                "group_limit": [int(x) for x in self.group_limit]}
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "Plan":
+        p = cls()
+        p.stream_max = int(d["stream_max"])
+        for g, v in enumerate(d["group_limit"]):
+            p.group_limit[g] = int(v)
+        return p
+
+
 _lib = None
 u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
@@ -91,6 +112,10 @@ _SIGNATURES = {
     "ngia_ctx_align_pairs_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                             C.c_void_p, C.POINTER(Stats)]),
     "ngia_ctx_use_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+    "ngia_ctx_get_plan": (C.c_int, [C.c_void_p, C.POINTER(Plan)]),
+    "ngia_ctx_set_plan": (C.c_int, [C.c_void_p, C.POINTER(Plan)]),
+    "ngia_ctx_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,
+                                    C.POINTER(Plan), C.POINTER(C.c_double)]),
     "ngia_int32_peak": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ngia_ctx_fast_cluster": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.POINTER(Stats)]),
@@ -276,6 +301,22 @@ class Context:
                                                _ptr(out), C.byref(st)),
                "ngia_ctx_align_pairs_host")
         return out, st.as_dict()
+
+    def plan(self) -> dict:
+        p = Plan()
+        _check(lib().ngia_ctx_get_plan(self._h, C.byref(p)), "ngia_ctx_get_plan")
+        return p.as_dict()
+
+    def set_plan(self, plan: dict) -> None:
+        p = Plan.from_dict(plan)
+        _check(lib().ngia_ctx_set_plan(self._h, C.byref(p)), "ngia_ctx_set_plan")
+
+    def autotune(self, d_pairs: int, count: int, identity: int, reps: int = 2) -> tuple[dict, float]:
+        """Picks the binning plan on `count` device pairs; returns it and its time (ms)."""
+        p, ms = Plan(), C.c_double()
+        _check(lib().ngia_ctx_autotune(self._h, d_pairs, count, identity, reps, C.byref(p),
+                                       C.byref(ms)), "ngia_ctx_autotune")
+        return p.as_dict(), float(ms.value)
 
     def use_graphs(self, on: bool) -> bool:
         """Capture/replay the batched round as a CUDA graph; returns the old setting."""

@@ -255,7 +255,7 @@ __device__ inline uint32_t lcs_general(const uint32_t *__restrict__ rep,
 //   0..6   streaming shared-memory table kernel (align_stream.cuh), one pair
 //          per lane, W = 4, 6, ..., 16 words by stream_width
 //   7..12  group kernel (align_group.cuh), one pair per group of G lanes with
-//          K words per lane: (16,1) (32,1) (32,2) (32,4) (32,8) (32,16)
+//          K words per lane: (16,1) (16,2) (16,4) (32,4) (32,8) (32,16)
 //   13     general kernel, one pair per thread (any width)
 //   14     pairs failing the length filter (score 0, not launched)
 constexpr int kNumLdsClasses = 7;
@@ -270,8 +270,8 @@ struct GroupShape {
 };
 __host__ __device__ constexpr GroupShape group_shape(int c) {
   return c == 7 ? GroupShape{16, 1}
-       : c == 8 ? GroupShape{32, 1}
-       : c == 9 ? GroupShape{32, 2}
+       : c == 8 ? GroupShape{16, 2}
+       : c == 9 ? GroupShape{16, 4}
        : c == 10 ? GroupShape{32, 4}
        : c == 11 ? GroupShape{32, 8}
                  : GroupShape{32, 16};
@@ -294,13 +294,43 @@ __host__ __device__ inline bool group_fits(const Band &b, int G, int K) {
   return ns <= (uint32_t)G || b.ls + b.rs <= (uint32_t)((G - 1) * K + G);
 }
 
-__host__ __device__ inline int width_class(const Band &b) {
+// Largest ls + rs a group class can hold with one live slice per lane.
+__host__ __device__ constexpr uint32_t group_span_limit(int c) {
+  return (uint32_t)((group_shape(c).G - 1) * group_shape(c).K + group_shape(c).G);
+}
+
+// The binning plan (what an autotuner picks): the widest window sent to the
+// one-pair-per-lane kernels, and per group class the widest band (ls + rs) it
+// takes (0: class unused; never above group_span_limit).  A pair goes to the
+// first class that takes it; reps of at most G slices fit a group class of G
+// lanes whatever the band (each slice has its own lane).
+struct ClassPlan {
+  uint32_t stream_max;
+  uint32_t group_limit[kNumGroupClasses];
+};
+
+__host__ __device__ inline ClassPlan default_plan() {
+  ClassPlan p{16, {}};
+  for (int g = 0; g < kNumGroupClasses; ++g) p.group_limit[g] = group_span_limit(kFirstGroupClass + g);
+  return p;
+}
+
+__host__ __device__ inline int width_class(const Band &b, const ClassPlan &plan) {
   if (!b.pass) return kSkipClass;
   const uint32_t ws = stream_width(b);
-  if (ws <= 16) return ws <= 4 ? 0 : (int)((ws - 3) / 2);  // 5,6 -> 1; 7,8 -> 2; ...
-  for (int c = kFirstGroupClass; c < kFirstGroupClass + kNumGroupClasses; ++c)
-    if (group_fits(b, group_shape(c).G, group_shape(c).K)) return c;
+  if (ws <= plan.stream_max) return ws <= 4 ? 0 : (int)((ws - 3) / 2);  // 5,6 -> 1; 7,8 -> 2
+  for (int g = 0; g < kNumGroupClasses; ++g) {
+    const uint32_t lim = plan.group_limit[g];
+    if (lim == 0) continue;
+    const GroupShape sh = group_shape(kFirstGroupClass + g);
+    const uint32_t ns = (b.nr + sh.K - 1) / sh.K;
+    if (ns <= (uint32_t)sh.G || b.ls + b.rs <= lim) return kFirstGroupClass + g;
+  }
   return kGeneralClass;
+}
+
+__host__ __device__ inline int width_class(const Band &b) {
+  return width_class(b, default_plan());
 }
 
 // Queue order inside a class: longest targets first.  The sort key of a pair

@@ -134,7 +134,11 @@ __device__ inline uint32_t align_group(const uint32_t *__restrict__ packed,
   // this lane's slice
   uint32_t q = 0, e = 0, r = 0, zret = 0, pub_q = kNoSlice, pub_c = 0;
   uint4 codes = make_uint4(0u, 0u, 0u, 0u);
-  uint32_t done = 0;
+  // loads issued one step ahead: the slice's next code block, the planes of
+  // its next entering word
+  uint4 nxt = codes, pf = codes;
+  uint32_t nxt_q = kNoSlice, nxt_i = 0, pf_row = kFull;
+  uint32_t done = 0, wstep = 0;
 
   for (;;) {
     // groups without a pair take the next ones (one atomic per warp)
@@ -172,6 +176,8 @@ __device__ inline uint32_t align_group(const uint32_t *__restrict__ packed,
             e = r = zret = 0;
             pub_q = kNoSlice;
             pub_c = 0;
+            nxt_q = kNoSlice;
+            pf_row = kFull;
           }
         } else {
           drained = true;
@@ -223,33 +229,54 @@ __device__ inline uint32_t align_group(const uint32_t *__restrict__ packed,
             r = rr;
           }
           const uint32_t ee = j1 - lo < (uint32_t)K ? j1 - lo : (uint32_t)K;
-          for (; e < ee; ++e) tab.fill(e, load4(rep + 1 + 4 * (lo + e)));
+          for (; e < ee; ++e)
+            tab.fill(e, lo + e == pf_row ? pf : load4(rep + 1 + 4 * (lo + e)));
+          // next step's loads: this slice's next code block and the word
+          // that enters then (J1 moves up at most one word per block)
+          if (I + 1 < nc) {
+            const uint32_t j1n = I + 1 + rs < nr ? I + 1 + rs : nr;
+            if (e < (uint32_t)K && lo + e < j1n && pf_row != lo + e) {
+              pf_row = lo + e;
+              pf = load4(rep + 1 + 4 * pf_row);
+            }
+          }
         }
       }
     }
     cin = (live && q > 0 && qin == q - 1) ? cin : 0u;
     uint32_t cout = 0;
     if (live) {
-      codes = load4(tar + 4 * I);
+      codes = (nxt_q == q && nxt_i == I) ? nxt : load4(tar + 4 * I);
+      if (I + 1 < nc) {
+        nxt = load4(tar + 4 * (I + 1));
+        nxt_q = q;
+        nxt_i = I + 1;
+      }
       group_columns<K>(V, tab.base, codes, cin, cout);
       done += K;
     }
     pub_c = cout;
     pub_q = live ? q : kNoSlice;
 
-    // bound of the final LCS, and the end of the pair
-    uint32_t zl = zret;
+    // bound of the final LCS every fourth step, and the end of the pair
+    ++wstep;
+    const bool last = active && tau + 1 >= tau_end;
+    const bool check = (wstep & 3u) == 0 || __any_sync(kFull, last);
+    uint32_t S = 0, qhi1 = 0;
+    if (check) {
+      uint32_t zl = zret;
 #pragma unroll
-    for (int m = 0; m < K; ++m) zl += __popc(~V[m]);
-    const uint32_t S = group_sum<G>(zl);
-    const uint32_t qhi1 = group_max<G>((active && q < ns && e > 0) ? q + 1 : 0u);
+      for (int m = 0; m < K; ++m) zl += __popc(~V[m]);
+      S = group_sum<G>(zl);
+      qhi1 = group_max<G>((active && q < ns && e > 0) ? q + 1 : 0u);
+    }
     if (active) {
       ++tau;
       bool fin = tau >= tau_end;
       uint32_t score = 0;
       if (fin) {
         score = identity_score(S, lr, lt, t);
-      } else if (qhi1) {
+      } else if (check && qhi1) {
         const uint32_t blocks = tau - (qhi1 - 1);  // column blocks done by the top slice
         const uint32_t cols = 32 * blocks < lt ? 32 * blocks : lt;
         fin = !stream_may_reach(S, cols, lr, lt, t);

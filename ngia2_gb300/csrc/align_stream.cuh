@@ -49,6 +49,8 @@ struct StreamPair {
   uint32_t lcs;         // zeros of the retired rows
   uint32_t lr, lt;
   uint4 cur;            // code words of block i
+  uint4 pf;             // planes of row pf_row, loaded one block ahead
+  uint32_t pf_row;
   bool active;
 };
 
@@ -58,15 +60,29 @@ template <int W, int R, typename Tab>
 __device__ __forceinline__ void stream_block(uint32_t (&V)[W], const Tab &tab,
                                              StreamPair &sp) {
   constexpr int out = (R + W - 1) % W;
+  // the next block's code words and entering row (J1 moves up at most one row
+  // per block), loaded now so that their latency hides behind this block
+  const bool more = sp.i + 1 < sp.nc;
+  const uint4 nxt = more ? load4(sp.tar + 4 * (sp.i + 1)) : sp.cur;
+  const uint32_t j1 = sp.i + sp.rs < sp.nr ? sp.i + sp.rs : sp.nr;
+  const uint32_t j1n = sp.i + 1 + sp.rs < sp.nr ? sp.i + 1 + sp.rs : sp.nr;
+  uint4 pfn = sp.pf;
+  uint32_t pfn_row = sp.pf_row;
+  if (more && j1n > j1) {
+    pfn_row = j1n - 1;
+    pfn = load4(sp.rep + 1 + 4 * pfn_row);
+  }
   sp.lcs += __popc(~V[out]);
   V[out] = kFull;
   tab.clear(out);
-  const uint32_t j1 = sp.i + sp.rs < sp.nr ? sp.i + sp.rs : sp.nr;
   for (; sp.act < j1; ++sp.act) {
-    tab.fill(sp.in_slot, load4(sp.rep + 1 + 4 * sp.act));
+    tab.fill(sp.in_slot, sp.act == sp.pf_row ? sp.pf : load4(sp.rep + 1 + 4 * sp.act));
     sp.in_slot = sp.in_slot + 1 == (uint32_t)W ? 0u : sp.in_slot + 1;
   }
   lds_columns<W, R>(V, tab.base, sp.cur);
+  sp.cur = nxt;
+  sp.pf = pfn;
+  sp.pf_row = pfn_row;
 }
 
 template <int W, typename Tab, int R = 0>
@@ -138,6 +154,7 @@ __device__ inline uint32_t align_stream(const uint32_t *__restrict__ packed,
             sp.in_slot = (g + b.ls) % (uint32_t)W;
             sp.lcs = 0;
             sp.cur = load4(sp.tar);
+            sp.pf_row = kFull;
             sp.active = true;
           }
         } else {
@@ -165,8 +182,6 @@ __device__ inline uint32_t align_stream(const uint32_t *__restrict__ packed,
         for (int m = 0; m < W; ++m) V[m] = kFull;
 #pragma unroll 1
         for (uint32_t s = 0; s < (uint32_t)W; ++s) tab.clear(s);
-      } else {
-        sp.cur = load4(sp.tar + 4 * sp.i);
       }
     }
   }

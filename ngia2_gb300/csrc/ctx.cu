@@ -63,6 +63,11 @@ struct ngia_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaEvent_t ev[8] = {};
+  // the width classes of a batched round run as concurrent branches: forked
+  // from `stream` onto these streams and joined back
+  static constexpr int kSide = 4;
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t join[kSide] = {}, fork = nullptr;
   // resident database
   uint32_t n = 0;
   uint64_t packed_words = 0;
@@ -80,15 +85,18 @@ struct ngia_ctx {
   // the batched round of ngia_ctx_align_pairs as a CUDA graph, replayed while
   // its inputs (addresses, count, identity, rounding, allocations) match
   bool use_graphs = true;
+  ngia::ClassPlan plan = ngia::default_plan();
+  uint64_t plan_gen = 0;  // bumped by every plan change
   cudaGraphExec_t round_exec = nullptr;
   struct RoundKey {
     const void *pairs, *scores, *nib;
     uint32_t m, identity;
     int round_mode;
-    uint64_t alloc_gen;
+    uint64_t alloc_gen, plan_gen;
     bool operator==(const RoundKey &o) const {
       return pairs == o.pairs && scores == o.scores && nib == o.nib && m == o.m &&
-             identity == o.identity && round_mode == o.round_mode && alloc_gen == o.alloc_gen;
+             identity == o.identity && round_mode == o.round_mode &&
+             alloc_gen == o.alloc_gen && plan_gen == o.plan_gen;
     }
   } round_key{};
 };
@@ -154,20 +162,33 @@ static int align_reserve(ngia_ctx *c, uint32_t m) {
 static int align_batched(ngia_ctx *c, const uint2 *pairs, uint32_t m, uint32_t identity,
                          uint32_t *scores, Counters *dc, int ev_first) {
   cudaStream_t s = c->stream;
-  NGIA_TRY(classify(c->lens.as<uint32_t>(), pairs, m, identity, c->cls.as<uint32_t>(),
-                    dc->class_count, &dc->cells, dc->bounds, s));
+  NGIA_TRY(classify(c->lens.as<uint32_t>(), pairs, m, identity, c->plan,
+                    c->cls.as<uint32_t>(), dc->class_count, &dc->cells, dc->bounds, s));
   NGIA_TRY(radix_sort_pairs(c->cls.as<uint32_t>(), nullptr, c->cls_sorted.as<uint32_t>(),
                             c->order.as<uint32_t>(), m, 1, 0, kClassKeyBits, c->sort_tmp.p,
                             s));
   NGIA_CUDA(cudaMemsetAsync(scores, 0, (size_t)(m ? m : 1) * 4, s));
   if (ev_first >= 0) NGIA_CUDA(cudaEventRecord(c->ev[ev_first], s));
+  // classes as concurrent branches, widest first (dealt round-robin over the
+  // side streams): the few long pairs' warps leave most of the device to the
+  // other classes instead of running alone at the end
   const int launch_order[] = {kGeneralClass, 12, 11, 10, 9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
-  if (m > 0)
-    for (int cl : launch_order)
+  if (m > 0) {
+    NGIA_CUDA(cudaEventRecord(c->fork, s));
+    for (int k = 0; k < ngia_ctx::kSide; ++k) NGIA_CUDA(cudaStreamWaitEvent(c->side[k], c->fork, 0));
+    int k = 0;
+    for (int cl : launch_order) {
       NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->align_nib, c->ab,
                                   c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
                                   dc->bounds, scores, identity, &dc->work, &dc->cursor[cl],
-                                  s));
+                                  c->side[k]));
+      k = (k + 1) % ngia_ctx::kSide;
+    }
+    for (int j = 0; j < ngia_ctx::kSide; ++j) {
+      NGIA_CUDA(cudaEventRecord(c->join[j], c->side[j]));
+      NGIA_CUDA(cudaStreamWaitEvent(s, c->join[j], 0));
+    }
+  }
   if (ev_first >= 0) NGIA_CUDA(cudaEventRecord(c->ev[ev_first + 1], s));
   return NGIA_OK;
 }
@@ -244,8 +265,9 @@ int ctx_align_pairs(ngia_ctx *c, const uint2 *d_pairs, uint32_t m, uint32_t iden
   NGIA_TRY(align_reserve(c, m));
   Counters *dc = c->counters.as<Counters>();
   if (c->use_graphs) {
-    const ngia_ctx::RoundKey key{d_pairs, d_scores, c->align_nib, m, identity, round_mode(),
-                                 g_alloc_gen.load()};
+    const ngia_ctx::RoundKey key{d_pairs, d_scores, c->align_nib,  m,
+                                 identity, round_mode(),        g_alloc_gen.load(),
+                                 c->plan_gen};
     if (!c->round_exec || !(key == c->round_key)) {
       if (c->round_exec) cudaGraphExecDestroy(c->round_exec);
       c->round_exec = nullptr;
@@ -421,6 +443,11 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
     c->own_stream = (e == cudaSuccess);
   }
   for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+  for (int k = 0; k < ngia_ctx::kSide && e == cudaSuccess; ++k) {
+    e = cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join[k], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     ngia_ctx_destroy(c);
     return ngia::cuda_fail(e);
@@ -438,6 +465,12 @@ void ngia_ctx_destroy(ngia_ctx *c) {
                           &c->emit_tmp, &c->edges, &c->scan_tmp, &c->jobs};
   for (ngia::DevBuf *b : bufs) b->release();
   if (c->round_exec) cudaGraphExecDestroy(c->round_exec);
+  for (int k = 0; k < ngia_ctx::kSide; ++k) {
+    if (c->side[k]) cudaStreamSynchronize(c->side[k]);
+    if (c->side[k]) cudaStreamDestroy(c->side[k]);
+    if (c->join[k]) cudaEventDestroy(c->join[k]);
+  }
+  if (c->fork) cudaEventDestroy(c->fork);
   for (int k = 0; k < 8; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -504,6 +537,90 @@ int ngia_ctx_align_pairs(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count,
   if (!c || (count && (!d_pairs || !d_scores))) return NGIA_ERR_ARG;
   return ngia::ctx_align_pairs(c, reinterpret_cast<const uint2 *>(d_pairs), count, identity,
                                d_scores, stats);
+}
+
+static_assert(NGIA_GROUP_CLASSES == ngia::kNumGroupClasses, "plan layout");
+
+static bool plan_valid(const ngia_plan &p) {
+  if (p.stream_max < 4 || p.stream_max > 16) return false;
+  for (int g = 0; g < NGIA_GROUP_CLASSES; ++g)
+    if (p.group_limit[g] > ngia::group_span_limit(ngia::kFirstGroupClass + g)) return false;
+  return true;
+}
+
+int ngia_ctx_get_plan(ngia_ctx *c, ngia_plan *p) {
+  if (!c || !p) return NGIA_ERR_ARG;
+  p->stream_max = c->plan.stream_max;
+  for (int g = 0; g < NGIA_GROUP_CLASSES; ++g) p->group_limit[g] = c->plan.group_limit[g];
+  return NGIA_OK;
+}
+
+int ngia_ctx_set_plan(ngia_ctx *c, const ngia_plan *p) {
+  if (!c || !p || !plan_valid(*p)) return NGIA_ERR_ARG;
+  c->plan.stream_max = p->stream_max;
+  for (int g = 0; g < NGIA_GROUP_CLASSES; ++g) c->plan.group_limit[g] = p->group_limit[g];
+  ++c->plan_gen;
+  return NGIA_OK;
+}
+
+int ngia_ctx_autotune(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count, uint32_t identity,
+                      int reps, ngia_plan *best, double *best_ms) {
+  if (!c || (count && !d_pairs)) return NGIA_ERR_ARG;
+  if (c->n == 0) return NGIA_ERR_STATE;
+  if (identity < 1 || identity > 99 || count == 0) return NGIA_ERR_ARG;
+  if (reps < 1) reps = 1;
+  NGIA_TRY(c->scores.reserve((size_t)count * 4));
+  const bool graphs = c->use_graphs;
+  c->use_graphs = false;
+  const uint2 *pairs = reinterpret_cast<const uint2 *>(d_pairs);
+  auto time_plan = [&](const ngia_plan &p, double *ms) -> int {
+    NGIA_TRY(ngia_ctx_set_plan(c, &p));
+    double t_min = 1e30;
+    for (int r = 0; r < reps; ++r) {
+      ngia_stats st;
+      NGIA_TRY(ngia::ctx_align_pairs(c, pairs, count, identity, c->scores.as<uint32_t>(), &st));
+      const double t = st.ms_pairs + st.ms_align;
+      if (t < t_min) t_min = t;
+    }
+    *ms = t_min;
+    return NGIA_OK;
+  };
+  ngia_plan cur;
+  ngia_ctx_get_plan(c, &cur);
+  double t_cur = 0;
+  int rc = time_plan(cur, &t_cur);
+  // coordinate descent: the widest per-lane window, then each group class
+  // on (at its largest band) or off; a move must win by 2 %
+  for (int pass = 0; pass < 2 && rc == NGIA_OK; ++pass) {
+    for (uint32_t sm = 8; sm <= 16 && rc == NGIA_OK; sm += 2) {
+      if (sm == cur.stream_max) continue;
+      ngia_plan p = cur;
+      p.stream_max = sm;
+      double t = 0;
+      rc = time_plan(p, &t);
+      if (rc == NGIA_OK && t < 0.98 * t_cur) {
+        cur = p;
+        t_cur = t;
+      }
+    }
+    for (int g = 0; g < NGIA_GROUP_CLASSES && rc == NGIA_OK; ++g) {
+      ngia_plan p = cur;
+      const uint32_t lim = ngia::group_span_limit(ngia::kFirstGroupClass + g);
+      p.group_limit[g] = cur.group_limit[g] ? 0u : lim;
+      double t = 0;
+      rc = time_plan(p, &t);
+      if (rc == NGIA_OK && t < 0.98 * t_cur) {
+        cur = p;
+        t_cur = t;
+      }
+    }
+  }
+  c->use_graphs = graphs;
+  if (rc != NGIA_OK) return rc;
+  NGIA_TRY(ngia_ctx_set_plan(c, &cur));
+  if (best) *best = cur;
+  if (best_ms) *best_ms = t_cur;
+  return NGIA_OK;
 }
 
 int ngia_ctx_use_graphs(ngia_ctx *c, int on) {

@@ -2,7 +2,7 @@
 // (internal header).
 #pragma once
 
-#include "common.cuh"
+#include "align.cuh"
 
 namespace ngia {
 
@@ -66,8 +66,8 @@ int collect_write(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_
 // class-major order (bounds[c] = pairs in classes below c; kNumClasses + 1
 // entries, written after the counts are complete).
 int classify(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t identity,
-             uint32_t *cls, unsigned int *class_count, unsigned long long *cells,
-             uint32_t *bounds, cudaStream_t s);
+             const ClassPlan &plan, uint32_t *cls, unsigned int *class_count,
+             unsigned long long *cells, uint32_t *bounds, cudaStream_t s);
 int bits_for(uint32_t max_value);
 size_t emit_scratch_bytes(uint32_t count, uint32_t n_nodes);
 int emit_sorted(const uint2 *pairs, const uint32_t *scores, uint32_t count,

@@ -124,7 +124,8 @@ int collect_write(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_
 // ---- width classes ------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pairs,
-                uint64_t count, float t, int fma_mode, uint32_t *__restrict__ cls,
+                uint64_t count, float t, int fma_mode, ClassPlan plan,
+                uint32_t *__restrict__ cls,
                 unsigned int *__restrict__ class_count,
                 unsigned long long *__restrict__ cells) {
   __shared__ unsigned int sc[kNumClasses];
@@ -137,7 +138,7 @@ classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pai
        p += (uint64_t)gridDim.x * blockDim.x) {
     const uint2 pr = pairs[p];
     const Band b = make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode);
-    const int c = width_class(b);
+    const int c = width_class(b, plan);
     cls[p] = class_sort_key(c, b);
     atomicAdd(&sc[c], 1u);
     my_cells += band_blocks(b);
@@ -161,16 +162,16 @@ __global__ void class_bounds_kernel(const unsigned int *__restrict__ class_count
 }
 
 int classify(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t identity,
-             uint32_t *cls, unsigned int *class_count, unsigned long long *cells,
-             uint32_t *bounds, cudaStream_t s) {
+             const ClassPlan &plan, uint32_t *cls, unsigned int *class_count,
+             unsigned long long *cells, uint32_t *bounds, cudaStream_t s) {
   if (count > 0) {
     int dev = 0, sms = 0;
     NGIA_CUDA(cudaGetDevice(&dev));
     NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const uint32_t want = ceil_div(count, 256u), cap = (uint32_t)sms * 8;
     classify_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
-        lens, pairs, count, identity_threshold(identity), round_mode(), cls, class_count,
-        cells);
+        lens, pairs, count, identity_threshold(identity), round_mode(), plan, cls,
+        class_count, cells);
     NGIA_LAUNCHED();
   }
   class_bounds_kernel<<<1, 32, 0, s>>>(class_count, bounds);

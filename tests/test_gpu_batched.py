@@ -11,7 +11,7 @@ import ngia2_gb300 as ng
 import oracle
 from ngia2_gb300 import synth
 
-GROUP_SHAPES = [(16, 1), (32, 1), (32, 2), (32, 4), (32, 8), (32, 16)]
+GROUP_SHAPES = ng.GROUP_SHAPES
 
 
 def width_class(lr: int, lt: int, identity: int) -> int:
@@ -108,6 +108,39 @@ def test_every_group_class_is_covered(built):
         seen |= {width_class(lens[r], lens[t], identity) for r, t in pairs}
     assert set(range(7, 13)) <= seen, sorted(seen)
     assert {0, 13} <= seen, sorted(seen)
+
+
+@pytest.mark.gpu
+def test_plans_change_binning_not_scores(cuda, built):
+    """Every plan -- narrow per-lane windows, group classes switched off, the
+    autotuner's pick -- gives the same scores; plans beyond a class's band
+    limit are refused."""
+    from gpu_util import build_db, to_dev
+    seqs, pairs = pair_set(70, 977)
+    packed, offs, lens = build_db(seqs)
+    want = oracle.align_pairs(packed, offs, pairs, 70, oracle.ROUND_FMA)
+    with ng.Context() as ctx:
+        ctx.load(packed, offs, lens)
+        default = ctx.plan()
+        assert default["stream_max"] == 16
+        limits = default["group_limit"]
+        assert limits == [(g - 1) * k + g for g, k in ng.GROUP_SHAPES]
+        for plan in ({"stream_max": 8, "group_limit": limits},
+                     {"stream_max": 4, "group_limit": [0, limits[1], 0, limits[3], 0, 0]},
+                     {"stream_max": 12, "group_limit": [0] * 6}):
+            ctx.set_plan(plan)
+            assert ctx.plan() == plan
+            got, _ = ctx.align_pairs(pairs, 70)
+            assert np.array_equal(got, want), plan
+        with pytest.raises(ng.NgiaError):
+            ctx.set_plan({"stream_max": 18, "group_limit": limits})
+        with pytest.raises(ng.NgiaError):
+            ctx.set_plan({"stream_max": 16, "group_limit": [limits[0] + 1] + limits[1:]})
+        d_pairs = to_dev(pairs)
+        plan, ms = ctx.autotune(d_pairs.data_ptr(), len(pairs), 70, 1)
+        assert ctx.plan() == plan and ms > 0
+        got, _ = ctx.align_pairs(pairs, 70)
+        assert np.array_equal(got, want)
 
 
 @pytest.mark.gpu
