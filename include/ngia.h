@@ -230,6 +230,57 @@ int ngia_ctx_use_graphs(ngia_ctx *ctx, int on);
 int ngia_ctx_align_pairs_host(ngia_ctx *ctx, const uint32_t *h_pairs, uint32_t count,
                               uint32_t identity, uint32_t *h_scores, ngia_stats *stats);
 
+/* ---- serving: query batches against a resident database ------------------------
+ * A server holds a database (a loaded context's records, copied, with their
+ * 64-band signatures sorted per band and the database's cluster ids) and
+ * assigns query sequences to its clusters at one identity, by fast mode's
+ * rule (src/fastClustering.hpp:249-352) against the database snapshot: in
+ * band order 0..63, a query's candidate in a band is the latest database
+ * record (in index order) with the same band signature; the pair is aligned
+ * with the longer record as rep (the database record on a tie), and the first
+ * band whose candidate scores > 0 gives the query that record's cluster id; a
+ * query with no hit opens a new cluster (NGIA_NEW_CLUSTER).  Queries never
+ * see each other, so a result does not depend on what else is in flight.
+ *
+ * Requests (batches of queries as packed records) are admitted in arrival
+ * order while a slot is free and the working bytes of the requests in flight
+ * stay within the HBM budget (a request larger than the budget runs alone).
+ * Each slot runs its request -- copy in, sketch, signature lookup, batched
+ * alignment, selection, copy out -- on its own stream, so requests overlap on
+ * the device.  plain = 1 gives the per-request plain form to compare with: one
+ * slot, and the one-thread-per-pair drop-in kernel over the request's pairs. */
+#define NGIA_NEW_CLUSTER 0xFFFFFFFFu
+typedef struct ngia_server ngia_server;
+typedef struct ngia_server_config {
+  uint32_t identity;    /* 1..99 */
+  uint32_t slots;       /* requests in flight at once, 1..16 */
+  uint32_t max_queries; /* per request */
+  uint64_t max_words;   /* packed-record words per request */
+  uint64_t hbm_budget;  /* bytes of request working memory in flight */
+  int plain;
+} ngia_server_config;
+typedef struct ngia_request_stats {
+  double queue_ms, run_ms, total_ms; /* submit->admit, admit->done, submit->done */
+  uint32_t queries, assigned;        /* assigned: queries given an existing cluster */
+} ngia_request_stats;
+
+/* db: a loaded context (its records are copied; it may be destroyed after).
+ * h_cluster: the database's cluster id per record (e.g. from
+ * ngia_ctx_fast_cluster).  Computes the context's signatures if needed. */
+int ngia_server_create(ngia_server **srv, ngia_ctx *db, const uint32_t *h_cluster,
+                       const ngia_server_config *cfg);
+/* Queues a request (the arrays are copied before return): count packed
+ * records (h_offs: word offset of each in h_packed, h_lens: lengths). */
+int ngia_server_submit(ngia_server *srv, const uint32_t *h_packed, uint64_t words,
+                       const uint64_t *h_offs, const uint32_t *h_lens, uint32_t count,
+                       uint64_t *ticket);
+/* Waits for a request; h_cluster receives a cluster id (or NGIA_NEW_CLUSTER)
+ * per query.  The ticket is spent. */
+int ngia_server_wait(ngia_server *srv, uint64_t ticket, uint32_t *h_cluster,
+                     ngia_request_stats *stats);
+/* Finishes the requests in flight and queued, then frees everything. */
+void ngia_server_destroy(ngia_server *srv);
+
 /* Fast greedy clustering (src/fastClustering.hpp:249-352): per band, targets
  * not yet assigned are aligned against their rep and assigned on a hit;
  * h_cluster[i] = root index.  Synchronises. */

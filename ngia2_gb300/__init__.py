@@ -76,6 +76,22 @@ class Plan(C.Structure):
         return p
 
 
+NEW_CLUSTER = 0xFFFFFFFF
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("identity", C.c_uint32), ("slots", C.c_uint32), ("max_queries", C.c_uint32),
+                ("max_words", C.c_uint64), ("hbm_budget", C.c_uint64), ("plain", C.c_int)]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double),
+                ("queries", C.c_uint32), ("assigned", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
@@ -117,6 +133,13 @@ _SIGNATURES = {
     "ngia_ctx_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,
                                     C.POINTER(Plan), C.POINTER(C.c_double)]),
     "ngia_int32_peak": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "ngia_server_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_void_p,
+                                     C.POINTER(ServerConfig)]),
+    "ngia_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                     C.c_uint32, C.POINTER(C.c_uint64)]),
+    "ngia_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p,
+                                   C.POINTER(RequestStats)]),
+    "ngia_server_destroy": (None, [C.c_void_p]),
     "ngia_ctx_fast_cluster": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.POINTER(Stats)]),
     "ngia_ctx_rep_rows": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
@@ -351,6 +374,56 @@ class Context:
                "ngia_ctx_run_host")
         self.n = int(lens.size)
         return int(m.value), st.as_dict()
+
+
+# ---- serving --------------------------------------------------------------------------
+class Server:
+    """Query batches assigned to a resident database's clusters
+    (ngia_server_*): submit() queues a request, wait() returns its cluster ids
+    (NEW_CLUSTER for a query that opens a new cluster) and timings."""
+
+    def __init__(self, ctx: "Context", cluster: np.ndarray, identity: int = 90, slots: int = 4,
+                 max_queries: int = 50_000, max_words: int = 16 << 20,
+                 hbm_budget: int = 8 << 30, plain: bool = False):
+        cluster = np.ascontiguousarray(cluster, dtype=np.uint32)
+        cfg = ServerConfig(identity, slots, max_queries, max_words, hbm_budget, 1 if plain else 0)
+        h = C.c_void_p()
+        _check(lib().ngia_server_create(C.byref(h), ctx._h, _ptr(cluster), C.byref(cfg)),
+               "ngia_server_create")
+        self._h = h
+
+    def submit(self, packed: np.ndarray, offsets: np.ndarray, lens: np.ndarray) -> int:
+        packed = np.ascontiguousarray(packed, dtype=np.uint32)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        lens = np.ascontiguousarray(lens, dtype=np.uint32)
+        t = C.c_uint64()
+        _check(lib().ngia_server_submit(self._h, _ptr(packed), packed.size, _ptr(offsets),
+                                        _ptr(lens), lens.size, C.byref(t)), "ngia_server_submit")
+        return int(t.value)
+
+    def wait(self, ticket: int, count: int) -> tuple[np.ndarray, dict]:
+        out = np.empty(count, np.uint32)
+        st = RequestStats()
+        _check(lib().ngia_server_wait(self._h, ticket, _ptr(out), C.byref(st)),
+               "ngia_server_wait")
+        return out, st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().ngia_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 # ---- host-side drop-in pieces ---------------------------------------------------------

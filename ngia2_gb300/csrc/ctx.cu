@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "align.cuh"
+#include "ctx.cuh"
 #include "host.hpp"
 #include "kernels.cuh"
 
@@ -25,99 +26,13 @@ int round_mode() { return g_round_mode; }
 static std::atomic<unsigned long long> g_launches(0);
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
-// Every device (re)allocation of the contexts bumps this, so that a captured
-// graph, whose nodes hold buffer addresses, is known to be stale.
-static std::atomic<uint64_t> g_alloc_gen{0};
-
-// Grow-only device buffer.
-struct DevBuf {
-  void *p = nullptr;
-  size_t bytes = 0;
-  int reserve(size_t want) {
-    if (want <= bytes) return NGIA_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    ++g_alloc_gen;
-    if (want == 0) return NGIA_OK;
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e != cudaSuccess) {
-      cuda_fail(e);
-      return NGIA_ERR_NOMEM;
-    }
-    bytes = want;
-    return NGIA_OK;
-  }
-  template <typename T>
-  T *as() const { return static_cast<T *>(p); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-};
-
 }  // namespace ngia
-
-struct ngia_ctx {
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  cudaEvent_t ev[8] = {};
-  // the width classes of a batched round run as concurrent branches: forked
-  // from `stream` onto these streams and joined back
-  static constexpr int kSide = 4;
-  cudaStream_t side[kSide] = {};
-  cudaEvent_t join[kSide] = {}, fork = nullptr;
-  // resident database
-  uint32_t n = 0;
-  uint64_t packed_words = 0;
-  uint32_t rep_bands = 0;
-  ngia::DevBuf packed, nib, offs, lens, rep, sigs;
-  // targets as the aligner reads them: densely recoded when the database uses
-  // at most 7 nonzero residue codes (aligner tables of 8 entries), else `nib`
-  ngia::DevBuf nib_dense, presence;
-  const uint32_t *align_nib = nullptr;
-  ngia::Alphabet ab{16, 0xFEDCBA9876543210ull};
-  // graph build work
-  ngia::DevBuf ucount, uoff, counters, pairs, scores, cls, cls_sorted, order, sort_tmp,
-      emit_tmp, edges, scan_tmp, jobs;
-  uint64_t n_edges = 0;
-  // the batched round of ngia_ctx_align_pairs as a CUDA graph, replayed while
-  // its inputs (addresses, count, identity, rounding, allocations) match
-  bool use_graphs = true;
-  ngia::ClassPlan plan = ngia::default_plan();
-  uint64_t plan_gen = 0;  // bumped by every plan change
-  cudaGraphExec_t round_exec = nullptr;
-  struct RoundKey {
-    const void *pairs, *scores, *nib;
-    uint32_t m, identity;
-    int round_mode;
-    uint64_t alloc_gen, plan_gen;
-    bool operator==(const RoundKey &o) const {
-      return pairs == o.pairs && scores == o.scores && nib == o.nib && m == o.m &&
-             identity == o.identity && round_mode == o.round_mode &&
-             alloc_gen == o.alloc_gen && plan_gen == o.plan_gen;
-    }
-  } round_key{};
-};
 
 namespace ngia {
 
-struct Counters {  // device-side counters of one graph build
-  unsigned long long cand_total;
-  unsigned long long cells;
-  uint64_t unique_total;
-  unsigned int class_count[kNumClasses];
-  uint32_t fast_count;
-  unsigned long long work;  // 32x32 blocks the aligners computed
-  unsigned int cursor[kNumClasses];  // pairs taken from each class's queue
-  uint32_t bounds[kNumClasses + 1];  // class ranges of the queue order
-};
-
-static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
-  float ms = 0.f;
-  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.0;
-  return ms;
+DbView db_view(const ngia_ctx *c) {
+  return DbView{c->packed.as<uint32_t>(), c->align_nib, c->ab, c->offs.as<uint64_t>(),
+                c->lens.as<uint32_t>()};
 }
 
 int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
@@ -135,61 +50,12 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
                   c->sort_tmp.p, s));
   NGIA_CUDA(cudaEventRecord(c->ev[2], s));
   c->rep_bands = bands;
+  c->sigs_valid = true;
   if (st) {
     NGIA_CUDA(cudaEventSynchronize(c->ev[2]));
     st->ms_sketch = ev_ms(c->ev[0], c->ev[1]);
     st->ms_bucket = ev_ms(c->ev[1], c->ev[2]);
   }
-  return NGIA_OK;
-}
-
-// Scratch of a batched round over m pairs (reserved before any capture).
-static int align_reserve(ngia_ctx *c, uint32_t m) {
-  NGIA_TRY(c->counters.reserve(sizeof(Counters)));
-  NGIA_TRY(c->cls.reserve((size_t)(m ? m : 1) * 4));
-  NGIA_TRY(c->cls_sorted.reserve((size_t)(m ? m : 1) * 4));
-  NGIA_TRY(c->order.reserve((size_t)(m ? m : 1) * 4));
-  NGIA_TRY(c->sort_tmp.reserve(radix_sort_scratch_bytes(m ? m : 1, 1)));
-  return NGIA_OK;
-}
-
-// The batched aligner over m pairs on the device, all stream-ordered with no
-// host round trip (capturable): width classes and their bounds (classify),
-// class-major queue order with the longest targets first (one radix pass),
-// scores zeroed, then one persistent launch per class, widest first; empty
-// classes' grids find their queue empty and return.  ev_first >= 0 records
-// events ev_first (classified) and ev_first + 1 (aligned).  *dc must be zero.
-static int align_batched(ngia_ctx *c, const uint2 *pairs, uint32_t m, uint32_t identity,
-                         uint32_t *scores, Counters *dc, int ev_first) {
-  cudaStream_t s = c->stream;
-  NGIA_TRY(classify(c->lens.as<uint32_t>(), pairs, m, identity, c->plan,
-                    c->cls.as<uint32_t>(), dc->class_count, &dc->cells, dc->bounds, s));
-  NGIA_TRY(radix_sort_pairs(c->cls.as<uint32_t>(), nullptr, c->cls_sorted.as<uint32_t>(),
-                            c->order.as<uint32_t>(), m, 1, 0, kClassKeyBits, c->sort_tmp.p,
-                            s));
-  NGIA_CUDA(cudaMemsetAsync(scores, 0, (size_t)(m ? m : 1) * 4, s));
-  if (ev_first >= 0) NGIA_CUDA(cudaEventRecord(c->ev[ev_first], s));
-  // classes as concurrent branches, widest first (dealt round-robin over the
-  // side streams): the few long pairs' warps leave most of the device to the
-  // other classes instead of running alone at the end
-  const int launch_order[] = {kGeneralClass, 12, 11, 10, 9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
-  if (m > 0) {
-    NGIA_CUDA(cudaEventRecord(c->fork, s));
-    for (int k = 0; k < ngia_ctx::kSide; ++k) NGIA_CUDA(cudaStreamWaitEvent(c->side[k], c->fork, 0));
-    int k = 0;
-    for (int cl : launch_order) {
-      NGIA_TRY(launch_align_class(cl, c->packed.as<uint32_t>(), c->align_nib, c->ab,
-                                  c->offs.as<uint64_t>(), pairs, c->order.as<uint32_t>(),
-                                  dc->bounds, scores, identity, &dc->work, &dc->cursor[cl],
-                                  c->side[k]));
-      k = (k + 1) % ngia_ctx::kSide;
-    }
-    for (int j = 0; j < ngia_ctx::kSide; ++j) {
-      NGIA_CUDA(cudaEventRecord(c->join[j], c->side[j]));
-      NGIA_CUDA(cudaStreamWaitEvent(s, c->join[j], 0));
-    }
-  }
-  if (ev_first >= 0) NGIA_CUDA(cudaEventRecord(c->ev[ev_first + 1], s));
   return NGIA_OK;
 }
 
@@ -225,9 +91,11 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   uint2 *pairs = c->pairs.as<uint2>();
   uint32_t *scores = c->scores.as<uint32_t>();
   NGIA_TRY(collect_write(rep, lens, n, bands, identity, c->uoff.as<uint64_t>(), pairs, s));
-  // 2-3. width classes, then one persistent launch per class
-  NGIA_TRY(align_reserve(c, m));
-  NGIA_TRY(align_batched(c, pairs, m, identity, scores, dc, 1));
+  // 2-3. width classes, then one persistent launch per class (the round is
+  // on the context's stream)
+  NGIA_TRY(c->round.reserve(m));
+  NGIA_TRY(c->round.enqueue(db_view(c), pairs, m, identity, scores, c->ev[1]));
+  NGIA_CUDA(cudaEventRecord(c->ev[2], s));
   // 4. emit: compact hits, sort by (rep, tar)
   NGIA_TRY(c->emit_tmp.reserve(emit_scratch_bytes(m, n)));
   NGIA_TRY(c->edges.reserve((size_t)(m ? m : 1) * sizeof(ngia_edge)));
@@ -238,11 +106,12 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   c->n_edges = ne;
   if (h_n_edges) *h_n_edges = ne;
   if (st) {
-    NGIA_CUDA(cudaMemcpy(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost));
+    Counters rc;
+    NGIA_CUDA(cudaMemcpy(&rc, c->round.counters(), sizeof(Counters), cudaMemcpyDeviceToHost));
     st->candidate_pairs = hc.cand_total;
     st->unique_pairs = total;
-    st->aligned_cells = hc.cells;
-    st->computed_cells = hc.work * 1024ull;
+    st->aligned_cells = rc.cells;
+    st->computed_cells = rc.work * 1024ull;
     st->edges = ne;
     st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
     st->ms_align = ev_ms(c->ev[1], c->ev[2]);
@@ -254,65 +123,21 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
 // The batched aligner on caller-given pairs (device arrays) of the resident
 // database.  Every index must be below the record count.  With graphs on, the
 // round is captured once per (pairs, scores, count, identity, rounding,
-// allocations) and replayed.
+// allocations, plan) and replayed.
 int ctx_align_pairs(ngia_ctx *c, const uint2 *d_pairs, uint32_t m, uint32_t identity,
                     uint32_t *d_scores, ngia_stats *st) {
   if (c->n == 0) return NGIA_ERR_STATE;
   if (identity < 1 || identity > 99) return NGIA_ERR_ARG;
   if (st) std::memset(st, 0, sizeof(*st));
-  if (m == 0) return NGIA_OK;
-  cudaStream_t s = c->stream;
-  NGIA_TRY(align_reserve(c, m));
-  Counters *dc = c->counters.as<Counters>();
-  if (c->use_graphs) {
-    const ngia_ctx::RoundKey key{d_pairs, d_scores, c->align_nib,  m,
-                                 identity, round_mode(),        g_alloc_gen.load(),
-                                 c->plan_gen};
-    if (!c->round_exec || !(key == c->round_key)) {
-      if (c->round_exec) cudaGraphExecDestroy(c->round_exec);
-      c->round_exec = nullptr;
-      NGIA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-      int rc = NGIA_OK;
-      const cudaError_t e0 = cudaMemsetAsync(dc, 0, sizeof(Counters), s);
-      if (e0 != cudaSuccess) rc = cuda_fail(e0);
-      if (rc == NGIA_OK) rc = align_batched(c, d_pairs, m, identity, d_scores, dc, -1);
-      cudaGraph_t graph = nullptr;
-      const cudaError_t e1 = cudaStreamEndCapture(s, &graph);
-      if (rc == NGIA_OK && e1 != cudaSuccess) rc = cuda_fail(e1);
-      if (rc == NGIA_OK) {
-        const cudaError_t e2 = cudaGraphInstantiate(&c->round_exec, graph, 0);
-        if (e2 != cudaSuccess) rc = cuda_fail(e2);
-      }
-      if (graph) cudaGraphDestroy(graph);
-      if (rc != NGIA_OK) {
-        c->round_exec = nullptr;
-        return rc;
-      }
-      c->round_key = key;
-    }
-    NGIA_CUDA(cudaEventRecord(c->ev[0], s));
-    NGIA_CUDA(cudaGraphLaunch(c->round_exec, s));
-    NGIA_CUDA(cudaEventRecord(c->ev[2], s));
-    NGIA_CUDA(cudaEventRecord(c->ev[1], s));  // no split inside a graph
-  } else {
-    NGIA_CUDA(cudaMemsetAsync(dc, 0, sizeof(Counters), s));
-    NGIA_CUDA(cudaEventRecord(c->ev[0], s));
-    NGIA_TRY(align_batched(c, d_pairs, m, identity, d_scores, dc, 1));
-  }
-  NGIA_CUDA(cudaEventSynchronize(c->ev[2]));
+  RoundStats rs;
+  NGIA_TRY(c->round.run(db_view(c), d_pairs, m, identity, d_scores, &rs));
   if (st) {
-    Counters hc;
-    NGIA_CUDA(cudaMemcpy(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost));
     st->candidate_pairs = m;
     st->unique_pairs = m;
-    st->aligned_cells = hc.cells;
-    st->computed_cells = hc.work * 1024ull;
-    if (c->use_graphs) {
-      st->ms_align = ev_ms(c->ev[0], c->ev[2]);
-    } else {
-      st->ms_pairs = ev_ms(c->ev[0], c->ev[1]);
-      st->ms_align = ev_ms(c->ev[1], c->ev[2]);
-    }
+    st->aligned_cells = rs.cells;
+    st->computed_cells = rs.work * 1024ull;
+    st->ms_pairs = rs.ms_classify;
+    st->ms_align = rs.ms_align;
   }
   return NGIA_OK;
 }
@@ -372,6 +197,7 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
   // codes, all the aligner looks at, is unchanged by a bijection.
   c->align_nib = c->nib.as<uint32_t>();
   c->ab = Alphabet{16, 0xFEDCBA9876543210ull};
+  c->recode_map = 0;
   if (__builtin_popcount(present & ~1u) <= 7) {
     uint64_t map = 0, inv = 0;
     int next = 1;
@@ -386,8 +212,10 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
                            c->nib_dense.as<uint32_t>(), s));
     c->align_nib = c->nib_dense.as<uint32_t>();
     c->ab = Alphabet{8, inv};
+    c->recode_map = map;
   }
   c->n = n;
+  c->sigs_valid = false;
   c->packed_words = words;
   c->rep_bands = 0;
   c->n_edges = 0;
@@ -443,14 +271,14 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
     c->own_stream = (e == cudaSuccess);
   }
   for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
-  for (int k = 0; k < ngia_ctx::kSide && e == cudaSuccess; ++k) {
-    e = cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join[k], cudaEventDisableTiming);
-  }
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     ngia_ctx_destroy(c);
     return ngia::cuda_fail(e);
+  }
+  const int rc = c->round.init(c->stream);
+  if (rc != NGIA_OK) {
+    ngia_ctx_destroy(c);
+    return rc;
   }
   *out = c;
   return NGIA_OK;
@@ -459,18 +287,12 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
 void ngia_ctx_destroy(ngia_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  ngia::DevBuf *bufs[] = {&c->packed, &c->nib, &c->nib_dense, &c->presence, &c->offs,  &c->lens,       &c->rep,    &c->sigs,
-                          &c->ucount, &c->uoff,  &c->counters,   &c->pairs,  &c->scores,
-                          &c->cls,    &c->cls_sorted, &c->order, &c->sort_tmp,
-                          &c->emit_tmp, &c->edges, &c->scan_tmp, &c->jobs};
+  ngia::DevBuf *bufs[] = {&c->packed,   &c->nib,   &c->nib_dense, &c->presence, &c->offs,
+                          &c->lens,     &c->rep,   &c->sigs,      &c->ucount,   &c->uoff,
+                          &c->counters, &c->pairs, &c->scores,    &c->sort_tmp, &c->emit_tmp,
+                          &c->edges,    &c->scan_tmp, &c->jobs};
   for (ngia::DevBuf *b : bufs) b->release();
-  if (c->round_exec) cudaGraphExecDestroy(c->round_exec);
-  for (int k = 0; k < ngia_ctx::kSide; ++k) {
-    if (c->side[k]) cudaStreamSynchronize(c->side[k]);
-    if (c->side[k]) cudaStreamDestroy(c->side[k]);
-    if (c->join[k]) cudaEventDestroy(c->join[k]);
-  }
-  if (c->fork) cudaEventDestroy(c->fork);
+  c->round.destroy();  // shares c->stream, which it leaves alone
   for (int k = 0; k < 8; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -550,16 +372,16 @@ static bool plan_valid(const ngia_plan &p) {
 
 int ngia_ctx_get_plan(ngia_ctx *c, ngia_plan *p) {
   if (!c || !p) return NGIA_ERR_ARG;
-  p->stream_max = c->plan.stream_max;
-  for (int g = 0; g < NGIA_GROUP_CLASSES; ++g) p->group_limit[g] = c->plan.group_limit[g];
+  p->stream_max = c->round.plan.stream_max;
+  for (int g = 0; g < NGIA_GROUP_CLASSES; ++g) p->group_limit[g] = c->round.plan.group_limit[g];
   return NGIA_OK;
 }
 
 int ngia_ctx_set_plan(ngia_ctx *c, const ngia_plan *p) {
   if (!c || !p || !plan_valid(*p)) return NGIA_ERR_ARG;
-  c->plan.stream_max = p->stream_max;
-  for (int g = 0; g < NGIA_GROUP_CLASSES; ++g) c->plan.group_limit[g] = p->group_limit[g];
-  ++c->plan_gen;
+  c->round.plan.stream_max = p->stream_max;
+  for (int g = 0; g < NGIA_GROUP_CLASSES; ++g) c->round.plan.group_limit[g] = p->group_limit[g];
+  ++c->round.plan_gen;
   return NGIA_OK;
 }
 
@@ -570,8 +392,8 @@ int ngia_ctx_autotune(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count, uint
   if (identity < 1 || identity > 99 || count == 0) return NGIA_ERR_ARG;
   if (reps < 1) reps = 1;
   NGIA_TRY(c->scores.reserve((size_t)count * 4));
-  const bool graphs = c->use_graphs;
-  c->use_graphs = false;
+  const bool graphs = c->round.use_graphs;
+  c->round.use_graphs = false;
   const uint2 *pairs = reinterpret_cast<const uint2 *>(d_pairs);
   auto time_plan = [&](const ngia_plan &p, double *ms) -> int {
     NGIA_TRY(ngia_ctx_set_plan(c, &p));
@@ -615,7 +437,7 @@ int ngia_ctx_autotune(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count, uint
       }
     }
   }
-  c->use_graphs = graphs;
+  c->round.use_graphs = graphs;
   if (rc != NGIA_OK) return rc;
   NGIA_TRY(ngia_ctx_set_plan(c, &cur));
   if (best) *best = cur;
@@ -625,8 +447,8 @@ int ngia_ctx_autotune(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count, uint
 
 int ngia_ctx_use_graphs(ngia_ctx *c, int on) {
   if (!c) return NGIA_ERR_ARG;
-  const int old = c->use_graphs ? 1 : 0;
-  c->use_graphs = on != 0;
+  const int old = c->round.use_graphs ? 1 : 0;
+  c->round.use_graphs = on != 0;
   return old;
 }
 

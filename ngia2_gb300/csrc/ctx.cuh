@@ -1,0 +1,36 @@
+// ctx.cuh -- the resident-database context behind the opaque ngia_ctx of the
+// C ABI (internal header; ctx.cu and serve.cu).
+#pragma once
+
+#include "round.cuh"
+
+struct ngia_ctx {
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaEvent_t ev[8] = {};
+  // resident database
+  uint32_t n = 0;
+  uint64_t packed_words = 0;
+  uint32_t rep_bands = 0;
+  ngia::DevBuf packed, nib, offs, lens, rep, sigs;
+  bool sigs_valid = false;  // sigs hold all 64 bands of the loaded records
+  // targets as the aligner reads them: densely recoded when the database uses
+  // at most 7 nonzero residue codes (aligner tables of 8 entries), else `nib`
+  ngia::DevBuf nib_dense, presence;
+  const uint32_t *align_nib = nullptr;
+  ngia::Alphabet ab{16, 0xFEDCBA9876543210ull};
+  uint64_t recode_map = 0;  // nibble c = aligner code of residue code c (when dense)
+  // graph build work
+  ngia::DevBuf ucount, uoff, counters, pairs, scores, emit_tmp, edges, scan_tmp, jobs,
+      sort_tmp;
+  uint64_t n_edges = 0;
+  // the batched aligner (scratch, side streams, plan, cached graph) on `stream`
+  ngia::Round round;
+};
+
+namespace ngia {
+DbView db_view(const ngia_ctx *c);
+int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st);
+int ctx_fast_cluster(ngia_ctx *c, uint32_t identity, uint32_t bands, uint32_t *h_cluster,
+                     ngia_stats *st);
+}  // namespace ngia

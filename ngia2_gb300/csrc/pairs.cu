@@ -137,6 +137,11 @@ classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pai
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
        p += (uint64_t)gridDim.x * blockDim.x) {
     const uint2 pr = pairs[p];
+    if (pr.x == kFull) {  // an empty pair slot (serving): never aligned
+      cls[p] = ((uint32_t)kSkipClass << 4) | 15u;
+      atomicAdd(&sc[kSkipClass], 1u);
+      continue;
+    }
     const Band b = make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode);
     const int c = width_class(b, plan);
     cls[p] = class_sort_key(c, b);
