@@ -23,6 +23,11 @@ pairs   (one GPU) aligned cells/s of the batched aligner against the plain
         one-thread-per-pair form launched once per group, on 2,000,000
         heavy-tailed protein candidate pairs at identity 90, scores compared
         bit for bit (--pairs N to resize, 0 to skip; --pairs-only).
+serving (one GPU) queries/s and p50/p99 request latency of the serving engine
+        (a resident 2,000,000-protein database, Poisson-arriving requests of
+        1-50,000 queries at identity 90, 8 slots) against the same requests
+        run one at a time in the plain form, results compared per request
+        (--serve-db N to resize, 0 to skip; --serve-only).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -67,6 +72,13 @@ CPU_SAMPLE_FAMILIES = 6500
 # the plain form launched once per group (the reference launches once per band).
 PAIRS_N, PAIRS_SEED, PAIRS_IDENTITY, PAIRS_GROUPS = 2_000_000, 3, 90, 64
 PAIRS_MAX_STEPS = 5
+# Serving leg: a resident database of 2,000,000 proteins (the small-protein
+# generator scaled to 100,000 families), 300,000 held-out queries (10 %
+# unrelated) in Poisson-arriving requests of log-uniform 1..50,000 queries,
+# identity 90; against the same requests run one at a time in the plain form.
+SERVE_DB, SERVE_QUERIES, SERVE_FAMILIES, SERVE_SEED, SERVE_IDENTITY = (
+    2_000_000, 300_000, 100_000, 4, 90)
+SERVE_MAX_BATCH, SERVE_SLOTS, SERVE_LOAD, SERVE_REPLAY = 50_000, 8, 3.0, 10
 
 
 def log(*a):
@@ -91,6 +103,10 @@ def parse():
                    help="batched leg with the default binning plan")
     p.add_argument("--no-plain", action="store_true",
                    help="skip the plain arm of the batched leg (profiling)")
+    p.add_argument("--serve-db", type=int, default=SERVE_DB,
+                   help="database sequences of the serving leg (0 = skip it)")
+    p.add_argument("--serve-only", action="store_true",
+                   help="run only the serving leg and print its object")
     return p.parse_args()
 
 
@@ -440,6 +456,9 @@ def run_ours(args, world, rank, local, pg):
     if world == 1 and args.pairs > 0:
         # the batched-vs-plain leg on heavy-tailed protein pairs (one GPU)
         line["pairs"] = run_pairs(args)
+    if world == 1 and args.serve_db > 0:
+        # the serving leg: continuous batching vs per-request plain runs
+        line["serving"] = run_serving(args)
     if world == 1 and not args.no_cpu_baseline:
         try:
             # about 10 s of the reference's host code on all cores
@@ -612,9 +631,161 @@ def run_pairs(args) -> dict:
     }
 
 
+# ---- serving: continuous batching vs per-request plain runs ---------------------------
+def make_serving(n_db: int, workdir: Path):
+    """Database (packed through makedb) and query records of the serving leg."""
+    import ngia2_gb300 as ng
+    from ngia2_gb300 import synth
+    t0 = time.time()
+    scale = n_db / SERVE_DB
+    n_q = max(1000, int(SERVE_QUERIES * scale))
+    n_fam = max(100, int(SERVE_FAMILIES * scale))
+    cache = os.environ.get("NGIA_BENCH_CACHE")
+    if cache:
+        workdir = Path(cache) / f"serve_{n_db}_{SERVE_SEED}"
+        workdir.mkdir(parents=True, exist_ok=True)
+    dbp, qp = workdir / "db.packed", workdir / "queries.packed"
+    if not (cache and dbp.exists() and qp.exists()):
+        db, q = synth.serving_set(n_db, n_q, n_fam, seed=SERVE_SEED)
+        db.write_fasta(workdir / "db.fa")
+        q.write_fasta(workdir / "queries.fa")
+        ng.makedb(workdir / "db.fa", dbp)
+        ng.makedb(workdir / "queries.fa", qp)
+    db, q = ng.read_packed(dbp), ng.read_packed(qp)
+    log(f"serving workload: {db['n']} database sequences, {q['n']} queries "
+        f"({time.time() - t0:.1f} s)")
+    return db, q
+
+
+def serving_requests(q, seed: int = SERVE_SEED):
+    """Requests of log-uniform 1..SERVE_MAX_BATCH queries, in a random order
+    of the queries: (packed words, local offsets, lengths) each."""
+    import numpy as np
+    rng = np.random.default_rng(seed + 7)
+    n = q["n"]
+    order = rng.permutation(n)
+    words = 1 + 4 * ((q["lens"].astype(np.int64) + 31) // 32)
+    reqs, k = [], 0
+    while k < n:
+        s = int(min(n - k, max(1, np.floor(np.exp(rng.uniform(0, np.log(SERVE_MAX_BATCH)))))))
+        idx = order[k:k + s]
+        w = words[idx]
+        run = np.concatenate([[0], np.cumsum(w)[:-1]])
+        owner = np.repeat(np.arange(s), w)
+        gather = q["offsets"][idx].astype(np.int64)[owner] + (np.arange(int(w.sum())) - run[owner])
+        reqs.append((np.ascontiguousarray(q["packed"][gather], np.uint32),
+                     run.astype(np.uint64), np.ascontiguousarray(q["lens"][idx], np.uint32)))
+        k += s
+    return reqs
+
+
+def run_serving(args) -> dict:
+    """p50/p99 latency and queries/s of the serving engine (continuous batching
+    over SERVE_SLOTS slots, Poisson arrivals at SERVE_LOAD x the plain form's
+    request rate) against the same requests run one at a time in the plain form;
+    per-request results compared."""
+    import threading
+
+    import numpy as np
+    import torch
+
+    import ngia2_gb300 as ng
+    workdir = Path(tempfile.mkdtemp(prefix="ngia_serve_"))
+    db, q = make_serving(args.serve_db, workdir)
+    reqs = serving_requests(q) * SERVE_REPLAY  # the stream, replayed
+    stream = torch.cuda.Stream()
+    ctx = ng.Context(stream.cuda_stream)
+    ctx.load(db["packed"], db["offsets"], db["lens"])
+    t0 = time.time()
+    ctx.sketch_bucket(BANDS)
+    cluster = ctx.fast_cluster(SERVE_IDENTITY)  # the database's clusters (fast mode)
+    t_setup = time.time() - t0
+    nq = sum(len(r[2]) for r in reqs)
+
+    # plain: one request at a time, plain kernel, no overlap
+    plain_out, plain_ms = [], []
+    with ng.Server(ctx, cluster, SERVE_IDENTITY, plain=True, max_queries=SERVE_MAX_BATCH) as srv:
+        srv.wait(srv.submit(*reqs[0]), len(reqs[0][2]))  # warm-up
+        t_begin = time.perf_counter()
+        for r in reqs:
+            out, st = srv.wait(srv.submit(*r), len(r[2]))
+            plain_out.append(out)
+            plain_ms.append(st["total_ms"])
+        plain_s = time.perf_counter() - t_begin
+    plain_rate = len(reqs) / plain_s
+
+    # serving: Poisson arrivals at SERVE_LOAD x the plain request rate
+    rng = np.random.default_rng(SERVE_SEED + 11)
+    gaps = rng.exponential(1.0 / (SERVE_LOAD * plain_rate), size=len(reqs))
+    with ng.Server(ctx, cluster, SERVE_IDENTITY, slots=SERVE_SLOTS,
+                   max_queries=SERVE_MAX_BATCH) as srv:
+        srv.wait(srv.submit(*reqs[0]), len(reqs[0][2]))  # warm-up
+        tickets: list = [None] * len(reqs)
+        ready = [threading.Event() for _ in reqs]
+        results: list = [None] * len(reqs)
+        done_at = [0.0] * len(reqs)
+
+        def waiter():
+            for k in range(len(reqs)):
+                ready[k].wait()
+                results[k] = srv.wait(tickets[k], len(reqs[k][2]))
+                done_at[k] = time.perf_counter()
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t_begin = time.perf_counter()
+        t_next = t_begin
+        for k, r in enumerate(reqs):
+            t_next += gaps[k]
+            delay = t_next - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            tickets[k] = srv.submit(*r)
+            ready[k].set()
+        th.join()
+        serve_s = max(done_at) - t_begin
+        # capacity: every request submitted at once
+        t_begin = time.perf_counter()
+        ts = [srv.submit(*r) for r in reqs]
+        for t, r in zip(ts, reqs):
+            srv.wait(t, len(r[2]))
+        burst_s = time.perf_counter() - t_begin
+    lat = np.array([res[1]["total_ms"] for res in results])
+    pl = np.array(plain_ms)
+    identical = all(np.array_equal(a, b[0]) for a, b in zip(plain_out, results))
+    assigned = int(sum(int((o != ng.NEW_CLUSTER).sum()) for o in plain_out))
+    ctx.close()
+    return {
+        "workload": f"serving_db{db['n']}_queries{nq}_id{SERVE_IDENTITY}",
+        "data": "synthetic: small-protein generator (log-normal roots median 300 sigma 0.5, "
+                "5-35% subs, 2% indels) scaled to "
+                f"{int(SERVE_FAMILIES * args.serve_db / SERVE_DB)} families; queries held out "
+                "of the same families plus 10% unrelated; requests log-uniform 1-50,000 queries",
+        "metric": "queries/s (and request latency)", "unit": "queries/s",
+        "requests": len(reqs), "queries": nq, "assigned": assigned,
+        "replayed": SERVE_REPLAY,
+        "setup_s": t_setup,
+        "serving": {"value": nq / serve_s, "slots": SERVE_SLOTS,
+                    "arrivals": f"Poisson, {SERVE_LOAD} x the plain request rate",
+                    "p50_ms": float(np.percentile(lat, 50)),
+                    "p99_ms": float(np.percentile(lat, 99)), "makespan_s": serve_s,
+                    "capacity": nq / burst_s},
+        "plain": {"value": nq / plain_s, "p50_ms": float(np.percentile(pl, 50)),
+                  "p99_ms": float(np.percentile(pl, 99)), "total_s": plain_s,
+                  "form": "one request at a time, one-thread-per-pair kernel"},
+        "serving_over_plain": plain_s / serve_s,
+        "results_identical": identical,
+    }
+
+
 def main():
     args = parse()
     world, rank, local, pg = dist_setup(args)
+    if args.serve_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps(run_serving(args)), flush=True)
+        return
     if args.pairs_only:
         import torch
         torch.cuda.set_device(local)

@@ -156,16 +156,29 @@ def _gather_runs(starts, lens):
     return starts[owner] + (np.arange(total) - run_start[owner])
 
 
+class _LogNormalRoots:  # classes rather than closures: they pickle into workers
+    def __init__(self, median, sigma, lo, hi):
+        self.median, self.sigma, self.lo, self.hi = median, sigma, lo, hi
+
+    def __call__(self, rng, k):
+        return np.clip(np.round(rng.lognormal(np.log(self.median), self.sigma, size=k)),
+                       self.lo, self.hi)
+
+
+class _UniformRoots:
+    def __init__(self, lo, hi):
+        self.lo, self.hi = lo, hi
+
+    def __call__(self, rng, k):
+        return rng.integers(self.lo, self.hi + 1, size=k)
+
+
 def _lognormal_roots(median, sigma, lo, hi):
-    def fn(rng, k):
-        return np.clip(np.round(rng.lognormal(np.log(median), sigma, size=k)), lo, hi)
-    return fn
+    return _LogNormalRoots(median, sigma, lo, hi)
 
 
 def _uniform_roots(lo, hi):
-    def fn(rng, k):
-        return rng.integers(lo, hi + 1, size=k)
-    return fn
+    return _UniformRoots(lo, hi)
 
 
 def protein_families(n_seqs=20_000, n_families=2_000, seed=1) -> SeqSet:
@@ -176,6 +189,84 @@ def protein_families(n_seqs=20_000, n_families=2_000, seed=1) -> SeqSet:
 def dna_families(n_seqs=200_000, n_families=20_000, seed=2) -> SeqSet:
     return families(n_seqs, n_families, NUCLEO, NUCLEO_FREQ, _uniform_roots(200, 3000),
                     0.01, 0.10, 0.01, 2.0, seed, prefix=b"dna")
+
+
+def _family_chunk(args):
+    """Worker of families_parallel: one chunk of families from its own seed."""
+    (seed, f0, f1, per, alphabet, freqs, root_len_fn, sub_lo, sub_hi, indel_rate, indel_mean,
+     prefix) = args
+    rng = np.random.default_rng(seed)
+    rl = root_len_fn(rng, f1 - f0).astype(np.int64)
+    roots = _draw(rng, alphabet, freqs, int(rl.sum()))
+    out, lens, fam = _mutate_chunk(rng, roots, rl, per, alphabet, freqs, sub_lo, sub_hi,
+                                   indel_rate, indel_mean)
+    mem = np.concatenate([np.arange(k) for k in per])
+    names = [b">%s%07d_%02d" % (prefix, f0 + fam[i], mem[i]) for i in range(len(fam))]
+    return out, lens, names
+
+
+def families_parallel(n_seqs, n_families, alphabet, freqs, root_len_fn, sub_lo, sub_hi,
+                      indel_rate, indel_mean, seed, chunk_families=5000, prefix=b"fam",
+                      workers=0) -> SeqSet:
+    """families() for large sets: every chunk of families draws from its own
+    child seed (numpy SeedSequence), so chunks are generated in parallel
+    processes (spawned) and the result does not depend on the worker count.
+    Sequences are in generation order (family-major)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import os
+    per = np.full(n_families, n_seqs // n_families, dtype=np.int64)
+    per[: n_seqs - int(per.sum())] += 1
+    starts = list(range(0, n_families, chunk_families))
+    seeds = np.random.SeedSequence(seed).spawn(len(starts))
+    jobs = [(seeds[k], f0, min(n_families, f0 + chunk_families),
+             per[f0:min(n_families, f0 + chunk_families)], alphabet, freqs, root_len_fn,
+             sub_lo, sub_hi, indel_rate, indel_mean, prefix) for k, f0 in enumerate(starts)]
+    workers = workers or min(len(jobs), os.cpu_count() or 1)
+    if workers > 1:
+        with cf.ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+            parts = list(ex.map(_family_chunk, jobs))
+    else:
+        parts = [_family_chunk(j) for j in jobs]
+    residues = np.concatenate([p[0] for p in parts])
+    lens = np.concatenate([p[1] for p in parts])
+    names = [nm for p in parts for nm in p[2]]
+    return SeqSet(residues, lens, names)
+
+
+def serving_set(n_db=2_000_000, n_queries=300_000, n_families=100_000, novel=0.1, seed=4):
+    """The serving workload: sequences of the small-protein generator (log-normal
+    roots, median 300, sigma 0.5, 50-1500; 5-35 % substitutions, 2 % indels of
+    mean 3) from n_families families, split at random into a database of n_db
+    (index order: length descending) and held-out queries; a share `novel`
+    of the queries are unrelated sequences (new clusters).  Returns
+    (database SeqSet, queries SeqSet in random order)."""
+    n_rel = int(round(n_queries * (1 - novel)))
+    fam = families_parallel(n_db + n_rel, n_families, AMINO, AMINO_FREQ,
+                            _lognormal_roots(300, 0.5, 50, 1500), 0.05, 0.35, 0.02, 3.0, seed,
+                            prefix=b"srv")
+    rng = np.random.default_rng(seed + 1)
+    perm = rng.permutation(len(fam))
+    db_ids, q_ids = perm[:n_db], perm[n_db:]
+    db_ids = db_ids[np.argsort(-fam.lens[db_ids], kind="stable")]
+
+    def subset(ids):
+        idx = _gather_runs(fam.starts[ids], fam.lens[ids])
+        return fam.residues[idx], fam.lens[ids], [fam.names[i] for i in ids]
+
+    db = SeqSet(*subset(db_ids))
+    qr, ql, qn = subset(q_ids)
+    n_nov = n_queries - n_rel
+    nl = _lognormal_roots(300, 0.5, 50, 1500)(rng, n_nov).astype(np.int64)
+    nov = _draw(rng, AMINO, AMINO_FREQ, int(nl.sum()))
+    res = np.concatenate([qr, nov])
+    lens = np.concatenate([ql, nl])
+    names = qn + [b">novel%07d" % k for k in range(n_nov)]
+    order = rng.permutation(len(lens))
+    starts = np.concatenate([[0], np.cumsum(lens)[:-1]])
+    q = SeqSet(res[_gather_runs(starts[order], lens[order])], lens[order],
+               [names[i] for i in order])
+    return db, q
 
 
 def _heavy_tailed_roots(rng, k):
