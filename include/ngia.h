@@ -230,6 +230,30 @@ int ngia_ctx_use_graphs(ngia_ctx *ctx, int on);
 int ngia_ctx_align_pairs_host(ngia_ctx *ctx, const uint32_t *h_pairs, uint32_t count,
                               uint32_t identity, uint32_t *h_scores, ngia_stats *stats);
 
+/* ---- a database larger than device memory ----------------------------------------
+ * The graph build of ngia_ctx_group_align (sketch + bucket of `bands` rows,
+ * candidates, batched alignment, sorted unique edges) for records held in
+ * host memory, streamed through at most `chunk_bytes` of device memory for
+ * records (three chunk slots of planes, nibble codes and recoded codes; the
+ * rest -- signatures, rep rows, lengths, offsets, pairs, scores -- grows with
+ * the record count only and stays on the device).  The records pass through
+ * pinned double-buffered copies twice: once to sketch them, once per block
+ * of pairs (rep chunk, target chunk) to align them.  The edges equal the
+ * resident path's.  Records must be in index order (increasing offsets, not
+ * overlapping); h_edges needs room for the edges (NGIA_ERR_NOMEM if cap is
+ * too small).  Replaces the reference's managed-memory oversubscription
+ * (src/buildGraph.hpp:58-65,143-171). */
+typedef struct ngia_stream_stats {
+  uint64_t chunks, chunk_loads, bytes_h2d_sketch, bytes_h2d_align;
+  uint64_t candidate_pairs, unique_pairs, aligned_cells, computed_cells, edges;
+  double ms_sketch, ms_bucket, ms_pairs, ms_align, ms_emit, ms_total;
+} ngia_stream_stats;
+
+int ngia_stream_graph(const uint32_t *h_packed, uint64_t words, const uint64_t *h_offs,
+                      const uint32_t *h_lens, uint32_t n, uint32_t identity, uint32_t bands,
+                      uint64_t chunk_bytes, ngia_edge *h_edges, uint64_t cap,
+                      uint64_t *n_edges, ngia_stream_stats *stats);
+
 /* ---- serving: query batches against a resident database ------------------------
  * A server holds a database (a loaded context's records, copied, with their
  * 64-band signatures sorted per band and the database's cluster ids) and

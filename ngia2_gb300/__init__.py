@@ -79,6 +79,17 @@ class Plan(C.Structure):
 NEW_CLUSTER = 0xFFFFFFFF
 
 
+class StreamStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("chunks", "chunk_loads", "bytes_h2d_sketch",
+                                          "bytes_h2d_align", "candidate_pairs", "unique_pairs",
+                                          "aligned_cells", "computed_cells", "edges")] + \
+               [(k, C.c_double) for k in ("ms_sketch", "ms_bucket", "ms_pairs", "ms_align",
+                                          "ms_emit", "ms_total")]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("identity", C.c_uint32), ("slots", C.c_uint32), ("max_queries", C.c_uint32),
                 ("max_words", C.c_uint64), ("hbm_budget", C.c_uint64), ("plain", C.c_int)]
@@ -140,6 +151,9 @@ _SIGNATURES = {
     "ngia_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p,
                                    C.POINTER(RequestStats)]),
     "ngia_server_destroy": (None, [C.c_void_p]),
+    "ngia_stream_graph": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint32,
+                                    C.c_uint32, C.c_uint32, C.c_uint64, C.c_void_p, C.c_uint64,
+                                    C.POINTER(C.c_uint64), C.POINTER(StreamStats)]),
     "ngia_ctx_fast_cluster": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.POINTER(Stats)]),
     "ngia_ctx_rep_rows": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
@@ -424,6 +438,23 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def stream_graph(packed: np.ndarray, offsets: np.ndarray, lens: np.ndarray, identity: int,
+                 bands: int, chunk_bytes: int, cap: int | None = None) -> tuple[np.ndarray, dict]:
+    """The graph build of a database held in host memory, with at most
+    chunk_bytes of device memory for its records (ngia_stream_graph): the
+    sorted unique edges and per-stage stats."""
+    packed = np.ascontiguousarray(packed, dtype=np.uint32)
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    lens = np.ascontiguousarray(lens, dtype=np.uint32)
+    cap = int(cap if cap is not None else max(1, lens.size * bands))
+    edges = np.empty(cap, EDGE_DTYPE)
+    m, st = C.c_uint64(), StreamStats()
+    _check(lib().ngia_stream_graph(_ptr(packed), packed.size, _ptr(offsets), _ptr(lens),
+                                   lens.size, identity, bands, chunk_bytes, _ptr(edges), cap,
+                                   C.byref(m), C.byref(st)), "ngia_stream_graph")
+    return edges[: m.value].copy(), st.as_dict()
 
 
 # ---- host-side drop-in pieces ---------------------------------------------------------
