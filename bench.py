@@ -79,6 +79,12 @@ PAIRS_MAX_STEPS = 5
 SERVE_DB, SERVE_QUERIES, SERVE_FAMILIES, SERVE_SEED, SERVE_IDENTITY = (
     2_000_000, 300_000, 100_000, 4, 90)
 SERVE_MAX_BATCH, SERVE_SLOTS, SERVE_LOAD, SERVE_REPLAY = 50_000, 8, 3.0, 10
+# Streaming leg: a protein database held in host memory (the small-protein
+# generator, 12 sequences per family) clustered through 1 GiB of device memory
+# for records, 3 rehash rounds at identities 50 and 90; the out-of-HBM
+# configuration names 60,000,000 sequences (--stream-seqs 60000000).
+STREAM_SEQS, STREAM_PER_FAMILY, STREAM_SEED, STREAM_BANDS = 6_000_000, 12, 5, 3
+STREAM_IDENTITIES, STREAM_CHUNK_BYTES = (50, 90), 1 << 30
 
 
 def log(*a):
@@ -107,6 +113,14 @@ def parse():
                    help="database sequences of the serving leg (0 = skip it)")
     p.add_argument("--serve-only", action="store_true",
                    help="run only the serving leg and print its object")
+    p.add_argument("--stream-seqs", type=int, default=STREAM_SEQS,
+                   help="sequences of the streaming leg (0 = skip it)")
+    p.add_argument("--stream-only", action="store_true",
+                   help="run only the streaming leg and print its object")
+    p.add_argument("--stream-check", type=int, default=1,
+                   help="1: compare the streamed edges with the resident path's")
+    p.add_argument("--stream-chunk-bytes", type=int, default=STREAM_CHUNK_BYTES,
+                   help="device bytes for record chunks in the streaming leg")
     return p.parse_args()
 
 
@@ -459,6 +473,9 @@ def run_ours(args, world, rank, local, pg):
     if world == 1 and args.serve_db > 0:
         # the serving leg: continuous batching vs per-request plain runs
         line["serving"] = run_serving(args)
+    if world == 1 and args.stream_seqs > 0:
+        # the streaming leg: records in host memory, a bounded device budget
+        line["stream"] = run_stream(args)
     if world == 1 and not args.no_cpu_baseline:
         try:
             # about 10 s of the reference's host code on all cores
@@ -631,6 +648,78 @@ def run_pairs(args) -> dict:
     }
 
 
+# ---- streaming: a database in host memory through a bounded device budget ------------
+def make_stream(n: int, workdir: Path):
+    import numpy as np
+
+    from ngia2_gb300 import synth
+    t0 = time.time()
+    cache = os.environ.get("NGIA_BENCH_CACHE")
+    d = Path(cache) / f"stream_{n}_{STREAM_SEED}" if cache else workdir
+    d.mkdir(parents=True, exist_ok=True)
+    files = [d / f"{k}.npy" for k in ("packed", "offs", "lens")]
+    if cache and all(f.exists() for f in files):
+        packed, offs, lens = (np.load(f) for f in files)
+    else:
+        packed, offs, lens = synth.packed_proteins(n, max(1, n // STREAM_PER_FAMILY),
+                                                   seed=STREAM_SEED)
+        if cache:
+            for f, a in zip(files, (packed, offs, lens)):
+                np.save(f, a)
+    log(f"streaming workload: {len(lens)} sequences, {int(lens.sum())} residues, "
+        f"{packed.nbytes / 1e9:.2f} GB packed ({time.time() - t0:.1f} s)")
+    return packed, offs, lens
+
+
+def run_stream(args) -> dict:
+    """End-to-end seqs/s of the streamed graph build (sketch, bucket, candidates,
+    align, emit) with the records in host memory and STREAM_CHUNK_BYTES of device
+    memory for them; per stage the host-to-device GB/s; the edges compared with
+    the resident path's when --stream-check (and the records fit)."""
+    import numpy as np
+
+    import ngia2_gb300 as ng
+    workdir = Path(tempfile.mkdtemp(prefix="ngia_stream_"))
+    packed, offs, lens = make_stream(args.stream_seqs, workdir)
+    n = len(lens)
+    runs = {}
+    k = min(n, 1000)  # warm-up on the first records
+    k_words = int(offs[k - 1]) + 1 + 4 * ((int(lens[k - 1]) + 31) // 32)
+    budget = args.stream_chunk_bytes
+    for identity in STREAM_IDENTITIES:
+        ng.stream_graph(packed[:k_words], offs[:k], lens[:k], identity, STREAM_BANDS, budget)
+        edges, st = ng.stream_graph(packed, offs, lens, identity, STREAM_BANDS, budget,
+                                    cap=n * STREAM_BANDS)
+        gbs = lambda b, ms: b / (ms * 1e-3) / 1e9 if ms > 0 else None  # noqa: E731
+        run = {"value": n / (st["ms_total"] * 1e-3), "unit": "seqs/s", "edges": int(len(edges)),
+               "chunks": st["chunks"], "chunk_loads": st["chunk_loads"],
+               "stages_ms": {k: st[k] for k in ("ms_sketch", "ms_bucket", "ms_pairs",
+                                                "ms_align", "ms_emit", "ms_total")},
+               "h2d_gbs": {"sketch": gbs(st["bytes_h2d_sketch"], st["ms_sketch"]),
+                           "align": gbs(st["bytes_h2d_align"], st["ms_align"])},
+               "h2d_bytes": {"sketch": st["bytes_h2d_sketch"], "align": st["bytes_h2d_align"]},
+               "unique_pairs": st["unique_pairs"], "computed_cells": st["computed_cells"]}
+        if args.stream_check:
+            with ng.Context() as ctx:
+                ctx.load(packed, offs, lens)
+                m, _ = ctx.group_align(identity, STREAM_BANDS)
+                res = ctx.edges(m)
+            run["edges_identical_to_resident"] = bool(
+                len(res) == len(edges) and np.array_equal(res["rep"], edges["rep"])
+                and np.array_equal(res["tar"], edges["tar"])
+                and np.array_equal(res["weight"], edges["weight"]))
+        runs[f"id{identity}"] = run
+    return {
+        "workload": f"stream_{n}_proteins_{STREAM_BANDS}bands",
+        "data": "synthetic: small-protein generator (log-normal roots median 300 sigma 0.5, "
+                f"5-35% subs, 2% indels), {STREAM_PER_FAMILY} sequences per family, "
+                "packed on the device",
+        "metric": "seqs/s end to end", "unit": "seqs/s", "sequences": n,
+        "packed_bytes": int(packed.nbytes), "device_bytes_for_records": budget,
+        "runs": runs,
+    }
+
+
 # ---- serving: continuous batching vs per-request plain runs ---------------------------
 def make_serving(n_db: int, workdir: Path):
     """Database (packed through makedb) and query records of the serving leg."""
@@ -785,6 +874,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         print(json.dumps(run_serving(args)), flush=True)
+        return
+    if args.stream_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps(run_stream(args)), flush=True)
         return
     if args.pairs_only:
         import torch

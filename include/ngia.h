@@ -230,6 +230,22 @@ int ngia_ctx_use_graphs(ngia_ctx *ctx, int on);
 int ngia_ctx_align_pairs_host(ngia_ctx *ctx, const uint32_t *h_pairs, uint32_t count,
                               uint32_t identity, uint32_t *h_scores, ngia_stats *stats);
 
+/* ---- packing on the device ----------------------------------------------------------
+ * Residues (ASCII, one byte each, record i at d_starts[i], d_lens[i] bytes)
+ * into packed records at word offsets d_rec_offsets[i]: [u32 L][4*ceil(L/32)
+ * plane words], codes from the reduced 15-letter table -- the packing half of
+ * MakeDB::packData (src/makedb.hpp:162-171,223-231).  One warp per record,
+ * plane words from ballots.  The records must not overlap. */
+int ngia_pack(const uint8_t *d_residues, const uint64_t *d_starts, const uint32_t *d_lens,
+              uint32_t n, const uint64_t *d_rec_offsets, uint32_t *d_packed, void *stream);
+
+/* Same from host arrays, records placed back to back: h_rec_offsets receives
+ * each record's word offset; h_packed needs room for sum(1 + 4*ceil(L/32))
+ * words (`words`).  Allocates its device buffers; synchronous. */
+int ngia_pack_records(const uint8_t *h_residues, uint64_t residue_bytes,
+                      const uint64_t *h_starts, const uint32_t *h_lens, uint32_t n,
+                      uint32_t *h_packed, uint64_t words, uint64_t *h_rec_offsets);
+
 /* ---- a database larger than device memory ----------------------------------------
  * The graph build of ngia_ctx_group_align (sketch + bucket of `bands` rows,
  * candidates, batched alignment, sorted unique edges) for records held in

@@ -151,6 +151,10 @@ _SIGNATURES = {
     "ngia_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p,
                                    C.POINTER(RequestStats)]),
     "ngia_server_destroy": (None, [C.c_void_p]),
+    "ngia_pack": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                            C.c_void_p, C.c_void_p]),
+    "ngia_pack_records": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint32,
+                                    C.c_void_p, C.c_uint64, C.c_void_p]),
     "ngia_stream_graph": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint32,
                                     C.c_uint32, C.c_uint32, C.c_uint64, C.c_void_p, C.c_uint64,
                                     C.POINTER(C.c_uint64), C.POINTER(StreamStats)]),
@@ -438,6 +442,21 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def pack_records(residues: np.ndarray, starts: np.ndarray, lens: np.ndarray):
+    """Pack residues (uint8 ASCII; record i at starts[i], lens[i] bytes) on the
+    device into back-to-back packed records: (packed words, word offsets)."""
+    residues = np.ascontiguousarray(residues, dtype=np.uint8)
+    starts = np.ascontiguousarray(starts, dtype=np.uint64)
+    lens = np.ascontiguousarray(lens, dtype=np.uint32)
+    words = int((1 + 4 * ((lens.astype(np.int64) + 31) // 32)).sum())
+    packed = np.empty(max(words, 1), np.uint32)
+    offs = np.empty(max(lens.size, 1), np.uint64)
+    _check(lib().ngia_pack_records(_ptr(residues), residues.size, _ptr(starts), _ptr(lens),
+                                   lens.size, _ptr(packed), words, _ptr(offs)),
+           "ngia_pack_records")
+    return packed[:words], offs[: lens.size]
 
 
 def stream_graph(packed: np.ndarray, offsets: np.ndarray, lens: np.ndarray, identity: int,

@@ -200,6 +200,8 @@ def _family_chunk(args):
     roots = _draw(rng, alphabet, freqs, int(rl.sum()))
     out, lens, fam = _mutate_chunk(rng, roots, rl, per, alphabet, freqs, sub_lo, sub_hi,
                                    indel_rate, indel_mean)
+    if prefix is None:  # no names (large sets that never become FASTA)
+        return out, lens, None
     mem = np.concatenate([np.arange(k) for k in per])
     names = [b">%s%07d_%02d" % (prefix, f0 + fam[i], mem[i]) for i in range(len(fam))]
     return out, lens, names
@@ -230,8 +232,24 @@ def families_parallel(n_seqs, n_families, alphabet, freqs, root_len_fn, sub_lo, 
         parts = [_family_chunk(j) for j in jobs]
     residues = np.concatenate([p[0] for p in parts])
     lens = np.concatenate([p[1] for p in parts])
-    names = [nm for p in parts for nm in p[2]]
+    names = [nm for p in parts for nm in p[2]] if prefix is not None else []
     return SeqSet(residues, lens, names)
+
+
+def packed_proteins(n_seqs, n_families, seed=5):
+    """A large protein database as packed records, without FASTA: the
+    small-protein generator (log-normal roots median 300, sigma 0.5, 50-1500;
+    5-35 % substitutions, 2 % indels of mean 3), index order = length
+    descending (stable), packed on the device.  Returns (packed words, word
+    offsets, lengths)."""
+    from . import pack_records
+    fam = families_parallel(n_seqs, n_families, AMINO, AMINO_FREQ,
+                            _lognormal_roots(300, 0.5, 50, 1500), 0.05, 0.35, 0.02, 3.0, seed,
+                            prefix=None)
+    order = np.argsort(-fam.lens, kind="stable")
+    lens = fam.lens[order].astype(np.uint32)
+    packed, offs = pack_records(fam.residues, fam.starts[order].astype(np.uint64), lens)
+    return packed, offs, lens
 
 
 def serving_set(n_db=2_000_000, n_queries=300_000, n_families=100_000, novel=0.1, seed=4):
