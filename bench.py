@@ -63,6 +63,7 @@ SKETCH_ALU_OPS_PER_HASH = 10
 # 100,000-sequence case of the same generator (profiles/*_dna100k.txt); scaled
 # to a full launch by the units it processes (both grow in proportion).
 SKETCH_DRAM_BYTES_PER_POSITION = 0.553
+SKETCH_TABLE_DRAM_BYTES_PER_POSITION = None
 ALIGN_DRAM_BYTES_PER_CELL = 5.9e-4
 # The reference's host code clusters about 650 families (6,500 sequences) of
 # this generator per second on 16 Grace cores; samples are sized from that.
@@ -416,6 +417,7 @@ def run_ours(args, world, rank, local, pg):
     sketch_ms = statistics.mean(s["ms_sketch"] for s in stats)
     positions = signed_positions(db["lens"])
     hbm = peaks().get("hbm_gbs")
+    table_active = ctx.sketch_table_active()
 
     def roof(kernel, ops, ms, units, unit_name, bytes_per_unit, algo_bytes, launches_):
         achieved = ops / (ms * 1e-3)
@@ -428,18 +430,27 @@ def run_ours(args, world, rank, local, pg):
                 "algorithmic_bytes": algo_bytes / launches_,
                 "hbm_frac_of_measured": (algo_bytes / (ms * 1e-3) / (hbm * 1e9)) if hbm else None}
 
+    # the sketch: 64 hashed bands per position, or on a four-letter database
+    # table_bands bands gathered from the 8-mer table (a min each) + the rest hashed
+    tb = ng.lib().ngia_sketch_table_bands() if table_active else 0
+    sketch_ops = positions * ((BANDS - tb) * SKETCH_ALU_OPS_PER_HASH + tb)
     rs = {
-        "sketch": roof("sketch_kernel<NibbleKmers>", positions * BANDS * SKETCH_ALU_OPS_PER_HASH,
-                       sketch_ms, positions, "signed_positions", SKETCH_DRAM_BYTES_PER_POSITION,
+        "sketch": roof("sketch_table_kernel" if tb else "sketch_kernel<NibbleKmers>", sketch_ops,
+                       sketch_ms, positions, "signed_positions",
+                       SKETCH_TABLE_DRAM_BYTES_PER_POSITION if tb
+                       else SKETCH_DRAM_BYTES_PER_POSITION,
                        # nibble codes read (half a byte per residue) + 64 signatures written
                        int(db["lens"].sum()) / 2 + 4 * BANDS * n, 1),
         # the align phase: one launch per populated width class, timed as a whole
-        "align": roof("align phase (align_lds_kernel / align_class_kernel per width class)",
+        "align": roof("align phase (align_stream_kernel / align_group_kernel / align_general_kernel per width class)",
                       cells / 32 * ALIGN_OPS_PER_WORD_STEP, align_ms, cells, "computed_cells",
                       ALIGN_DRAM_BYTES_PER_CELL,
                       # the pair list and scores once + every record's codes once
                       st["unique_pairs"] * 12 + int(db["lens"].sum()) / 2, 1),
     }
+    if tb:
+        # table entries are gathered from L2 (the 65,536 x table_bands words stay resident)
+        rs["sketch"].update(table_bands=tb, l2_table_bytes=positions * tb * 4)
     dominant = max(rs, key=lambda k: rs[k]["ms"])
     line = {
         "metric": "seqs clustered/s", "value": world * n / (mean_ms_max * 1e-3),

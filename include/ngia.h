@@ -327,6 +327,22 @@ void ngia_server_destroy(ngia_server *srv);
 int ngia_ctx_fast_cluster(ngia_ctx *ctx, uint32_t identity, uint32_t bands,
                           uint32_t *h_cluster, ngia_stats *stats);
 
+/* The loaded records' 64 signatures, band-major [64][n], after
+ * ngia_ctx_sketch_bucket (NGIA_ERR_STATE before). */
+int ngia_ctx_sigs(ngia_ctx *ctx, uint32_t *h_sigs);
+
+/* For a database of at most four residue codes (nucleotides), the sketch reads
+ * part of the band hashes of each 8-mer from a table of all 4^8 8-mers (the
+ * same signatures; a table row gather for those bands instead of hashing).
+ * On by default; returns the previous setting (0/1). */
+int ngia_ctx_use_sketch_table(ngia_ctx *ctx, int on);
+/* 1 when the context's sketch goes through that table (on, and the loaded
+ * database qualifies), else 0. */
+int ngia_ctx_sketch_table_active(ngia_ctx *ctx);
+/* How many of the 64 bands that table holds (the rest are hashed meanwhile:
+ * the table's row gathers load L2 while the hashes load the logic pipe). */
+int ngia_sketch_table_bands(void);
+
 /* Copy the device rep rows (bands x n) to the host. */
 int ngia_ctx_rep_rows(ngia_ctx *ctx, uint32_t *h_rep, uint32_t bands);
 

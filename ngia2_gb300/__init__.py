@@ -161,6 +161,10 @@ _SIGNATURES = {
     "ngia_ctx_fast_cluster": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.POINTER(Stats)]),
     "ngia_ctx_rep_rows": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "ngia_ctx_sigs": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ngia_ctx_use_sketch_table": (C.c_int, [C.c_void_p, C.c_int]),
+    "ngia_ctx_sketch_table_active": (C.c_int, [C.c_void_p]),
+    "ngia_sketch_table_bands": (C.c_int, []),
     "ngia_ctx_run_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
                                     C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                     C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64),
@@ -302,6 +306,22 @@ class Context:
 
     def sketch_bucket(self, bands: int = BANDS) -> None:
         _check(lib().ngia_ctx_sketch_bucket(self._h, bands), "ngia_ctx_sketch_bucket")
+
+    def sigs(self) -> np.ndarray:
+        """The 64 signatures of every record, band-major [64][n]."""
+        out = np.empty((BANDS, self.n), np.uint32)
+        _check(lib().ngia_ctx_sigs(self._h, _ptr(out)), "ngia_ctx_sigs")
+        return out
+
+    def sketch_table_active(self) -> bool:
+        return lib().ngia_ctx_sketch_table_active(self._h) == 1
+
+    def use_sketch_table(self, on: bool) -> bool:
+        """Sketch 4-letter databases through the 8-mer hash table; returns the old setting."""
+        r = lib().ngia_ctx_use_sketch_table(self._h, 1 if on else 0)
+        if r < 0:
+            _check(r, "ngia_ctx_use_sketch_table")
+        return bool(r)
 
     def rep_rows(self, bands: int = BANDS) -> np.ndarray:
         out = np.empty((bands, self.n), np.uint32)

@@ -159,7 +159,8 @@ nibble_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ 
         for (int j = 0; j < 8; ++j) out |= ((byte >> j) & 1u) << (28 - 4 * j + e);
       }
       nib[o + 1 + w] = out;
-      const uint32_t valid = len - 8 * w < 8 ? len - 8 * w : 8;  // codes of real residues
+      // codes of real residues (none in the padding words past the record's end)
+      const uint32_t valid = 8 * w >= len ? 0u : (len - 8 * w < 8 ? len - 8 * w : 8u);
 #pragma unroll
       for (uint32_t j = 0; j < 8; ++j)
         if (j < valid) mine |= 1u << ((out >> (28 - 4 * j)) & 15u);

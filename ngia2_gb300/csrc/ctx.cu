@@ -42,9 +42,19 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
   NGIA_TRY(c->sigs.reserve((size_t)kBands * c->n * 4));
   NGIA_TRY(c->rep.reserve((size_t)kBands * c->n * 4));
   NGIA_TRY(c->sort_tmp.reserve(bucket_scratch_bytes(c->n, bands)));
+  if (c->use_table && c->table_ok && !c->table_built) {
+    NGIA_TRY(c->sketch_table.reserve((size_t)kSketchTableEntries * kBands * 4));
+    NGIA_TRY(build_sketch_table(c->ab.inv, c->sketch_table.as<uint32_t>(), s));
+    c->table_built = true;
+  }
   NGIA_CUDA(cudaEventRecord(c->ev[0], s));
-  NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
+  if (c->use_table && c->table_ok)
+    NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
+                                 c->offs.as<uint64_t>(), c->n, c->sketch_table.as<uint32_t>(),
                                  c->sigs.as<uint32_t>(), s));
+  else
+    NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
+                                   c->sigs.as<uint32_t>(), s));
   NGIA_CUDA(cudaEventRecord(c->ev[1], s));
   NGIA_TRY(bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(),
                   c->sort_tmp.p, s));
@@ -198,6 +208,8 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
   c->align_nib = c->nib.as<uint32_t>();
   c->ab = Alphabet{16, 0xFEDCBA9876543210ull};
   c->recode_map = 0;
+  c->table_ok = (present & 1u) == 0 && present != 0 && __builtin_popcount(present) <= 4;
+  c->table_built = false;
   if (__builtin_popcount(present & ~1u) <= 7) {
     uint64_t map = 0, inv = 0;
     int next = 1;
@@ -290,7 +302,7 @@ void ngia_ctx_destroy(ngia_ctx *c) {
   ngia::DevBuf *bufs[] = {&c->packed,   &c->nib,   &c->nib_dense, &c->presence, &c->offs,
                           &c->lens,     &c->rep,   &c->sigs,      &c->ucount,   &c->uoff,
                           &c->counters, &c->pairs, &c->scores,    &c->sort_tmp, &c->emit_tmp,
-                          &c->edges,    &c->scan_tmp, &c->jobs};
+                          &c->edges,    &c->scan_tmp, &c->jobs, &c->sketch_table};
   for (ngia::DevBuf *b : bufs) b->release();
   c->round.destroy();  // shares c->stream, which it leaves alone
   for (int k = 0; k < 8; ++k)
@@ -442,6 +454,27 @@ int ngia_ctx_autotune(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count, uint
   NGIA_TRY(ngia_ctx_set_plan(c, &cur));
   if (best) *best = cur;
   if (best_ms) *best_ms = t_cur;
+  return NGIA_OK;
+}
+
+int ngia_ctx_use_sketch_table(ngia_ctx *c, int on) {
+  if (!c) return NGIA_ERR_ARG;
+  const int old = c->use_table ? 1 : 0;
+  c->use_table = on != 0;
+  return old;
+}
+
+int ngia_ctx_sketch_table_active(ngia_ctx *c) {
+  if (!c) return NGIA_ERR_ARG;
+  return c->use_table && c->table_ok ? 1 : 0;
+}
+
+int ngia_ctx_sigs(ngia_ctx *c, uint32_t *h_sigs) {
+  if (!c || !h_sigs) return NGIA_ERR_ARG;
+  if (!c->sigs_valid) return NGIA_ERR_STATE;
+  NGIA_CUDA(cudaMemcpyAsync(h_sigs, c->sigs.p, (size_t)ngia::kBands * c->n * 4,
+                            cudaMemcpyDeviceToHost, c->stream));
+  NGIA_CUDA(cudaStreamSynchronize(c->stream));
   return NGIA_OK;
 }
 

@@ -20,6 +20,10 @@ struct ngia_ctx {
   const uint32_t *align_nib = nullptr;
   ngia::Alphabet ab{16, 0xFEDCBA9876543210ull};
   uint64_t recode_map = 0;  // nibble c = aligner code of residue code c (when dense)
+  // at most four residue codes, none of them 0: the sketch reads the 64 band
+  // hashes of every 8-mer from a table (built on first use after a load)
+  bool table_ok = false, table_built = false, use_table = true;
+  ngia::DevBuf sketch_table;
   // graph build work
   ngia::DevBuf ucount, uoff, counters, pairs, scores, emit_tmp, edges, scan_tmp, jobs,
       sort_tmp;

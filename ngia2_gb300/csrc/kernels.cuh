@@ -11,6 +11,13 @@ int launch_sketch(const uint32_t *packed, const uint64_t *offs, uint32_t n,
                   uint32_t *sigs, cudaStream_t s);
 int launch_sketch_nibbles(const uint32_t *nib, const uint64_t *offs, uint32_t n,
                           uint32_t *sigs, cudaStream_t s);
+// Databases of at most four residue codes (none of them 0): the 64 band hashes
+// of every 8-mer in a table of kSketchTableEntries x 64 words, built from the
+// aligner codes' inverse map; the sketch then reads the aligner codes (dense).
+constexpr uint32_t kSketchTableEntries = 1u << 16;
+int build_sketch_table(uint64_t inv, uint32_t *table, cudaStream_t s);
+int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
+                        uint32_t n, const uint32_t *table, uint32_t *sigs, cudaStream_t s);
 
 // sort.cu
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs);

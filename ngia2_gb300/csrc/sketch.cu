@@ -158,7 +158,129 @@ int launch_sketch_nibbles(const uint32_t *nib, const uint64_t *offs, uint32_t n,
   return launch<NibbleKmers>(nib, offs, n, sigs, s);
 }
 
+// ---- databases of at most four residue codes: part of the hashes by table -------
+// With at most four codes (nucleotides) an 8-mer is one of 4^8 = 65,536
+// values, so the band hashes of all of them can be tabulated.  Gathering a
+// whole 64-band row per position is bound by L2 bandwidth (slower than
+// hashing), while hashing is bound by the logic/shift pipe; the kernel splits
+// the bands between the two: bands [0, kTableBands) come from the table
+// (16-byte loads + a min each), the others are hashed as in sketch_kernel.
+// Entry idx (2 bits per position, the newest in the low bits; digit d is
+// aligner code d + 1, i.e. the residue code in nibble d + 1 of `inv`) holds
+// that 8-mer's hashes exactly as sketch_kernel computes them, so the
+// signatures are the same.
+#ifndef NGIA_SKETCH_TABLE_BANDS
+#define NGIA_SKETCH_TABLE_BANDS 24  // multiple of 4
+#endif
+constexpr int kTableBands = NGIA_SKETCH_TABLE_BANDS;
+static_assert(kTableBands % 4 == 0 && kTableBands <= kBands, "table bands");
+
+__global__ void __launch_bounds__(256)
+sketch_table_build_kernel(uint64_t inv, uint32_t *__restrict__ table) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= kSketchTableEntries * (uint32_t)kTableBands) return;
+  const uint32_t idx = t / kTableBands, band = t % kTableBands;
+  uint32_t kmer = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const uint32_t d = (idx >> (2 * j)) & 3u;
+    kmer |= ((uint32_t)(inv >> (4 * (d + 1))) & 15u) << (4 * j);
+  }
+  const uint32_t y = kmer ^ (kmer >> 16);
+  table[t] = band_hash_tail(y ^ band_seed_fold(band));
+}
+
+// nib: the records' residue codes (records shorter than 8 are hashed
+// directly); dense: the same records in aligner codes 1..4.
+__global__ void __launch_bounds__(256)
+sketch_table_kernel(const uint32_t *__restrict__ nib, const uint32_t *__restrict__ dense,
+                    const uint64_t *__restrict__ offs, uint32_t n,
+                    const uint4 *__restrict__ table, uint32_t *__restrict__ sigs) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const uint64_t o = offs[i];
+    const uint32_t len = __ldg(nib + o);
+    uint32_t mn[kBands];
+#pragma unroll
+    for (int k = 0; k < kBands; ++k) mn[k] = kFull;
+    if (len >= 8) {
+      const uint32_t span = len - 7;  // signed positions 7 .. len-1
+      const uint32_t per = (span + 31u) >> 5;
+      const uint32_t pb = 7 + lane * per;
+      const uint32_t pe = min(pb + per, len);
+      if (pb < pe) {
+        const uint32_t *w = dense + o + 1;
+        const NibbleKmers src = NibbleKmers::make(nib + o);
+        uint32_t idx = 0;
+        for (uint32_t q = pb - 7; q < pb; ++q)
+          idx = (idx << 2) | (((__ldg(w + (q >> 3)) >> (28 - 4 * (q & 7u))) & 15u) - 1u);
+        uint32_t word = __ldg(w + (pb >> 3));
+        for (uint32_t p = pb; p < pe; ++p) {
+          if ((p & 7u) == 0) word = __ldg(w + (p >> 3));
+          idx = ((idx << 2) | (((word >> (28 - 4 * (p & 7u))) & 15u) - 1u)) & 0xFFFFu;
+          const uint4 *row = table + (size_t)idx * (kTableBands / 4);
+          uint4 v[kTableBands / 4];
+#pragma unroll
+          for (int k = 0; k < kTableBands / 4; ++k) v[k] = __ldg(row + k);
+          // the other bands are hashed while the row is on its way
+          const uint32_t kmer = NibbleKmers(src).at(p);
+          const uint32_t y = kmer ^ (kmer >> 16);
+#pragma unroll
+          for (int k = kTableBands; k < kBands; ++k)
+            mn[k] = min(mn[k], band_hash_tail(y ^ band_seed_fold((uint32_t)k)));
+#pragma unroll
+          for (int k = 0; k < kTableBands / 4; ++k) {
+            mn[4 * k] = min(mn[4 * k], v[k].x);
+            mn[4 * k + 1] = min(mn[4 * k + 1], v[k].y);
+            mn[4 * k + 2] = min(mn[4 * k + 2], v[k].z);
+            mn[4 * k + 3] = min(mn[4 * k + 3], v[k].w);
+          }
+        }
+      }
+    } else if (len > 0 && lane == 0) {  // the one signed position: the whole record
+      const uint32_t kmer = NibbleKmers::make(nib + o).at(len - 1);
+      const uint32_t y = kmer ^ (kmer >> 16);
+#pragma unroll
+      for (int k = 0; k < kBands; ++k) mn[k] = band_hash_tail(y ^ band_seed_fold((uint32_t)k));
+    }
+    uint32_t lo = kFull, hi = kFull;
+#pragma unroll
+    for (int k = 0; k < kBands; ++k) {
+      const uint32_t r = __reduce_min_sync(kFull, mn[k]);
+      if ((uint32_t)(k & 31) == lane) {
+        if (k < 32) lo = r;
+        else hi = r;
+      }
+    }
+    sigs[(size_t)lane * n + i] = lo;
+    sigs[(size_t)(lane + 32) * n + i] = hi;
+  }
+}
+
+int build_sketch_table(uint64_t inv, uint32_t *table, cudaStream_t s) {
+  const uint32_t total = kSketchTableEntries * (uint32_t)kTableBands;
+  sketch_table_build_kernel<<<ceil_div(total, 256u), 256, 0, s>>>(inv, table);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
+                        uint32_t n, const uint32_t *table, uint32_t *sigs, cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
+  sketch_table_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
+      nib, dense, offs, n, reinterpret_cast<const uint4 *>(table), sigs);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
 }  // namespace ngia
+
+extern "C" int ngia_sketch_table_bands(void) { return ngia::kTableBands; }
 
 extern "C" int ngia_sketch(const uint32_t *d_packed, const uint64_t *d_rec_offsets,
                            uint32_t n, uint32_t *d_sigs, void *stream) {
