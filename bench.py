@@ -63,7 +63,7 @@ SKETCH_ALU_OPS_PER_HASH = 10
 # 100,000-sequence case of the same generator (profiles/*_dna100k.txt); scaled
 # to a full launch by the units it processes (both grow in proportion).
 SKETCH_DRAM_BYTES_PER_POSITION = 0.553
-SKETCH_TABLE_DRAM_BYTES_PER_POSITION = None
+SKETCH_TABLE_DRAM_BYTES_PER_POSITION = 0.537  # sketch_rank_kernel, per signed position
 ALIGN_DRAM_BYTES_PER_CELL = 5.9e-4
 # The reference's host code clusters about 650 families (6,500 sequences) of
 # this generator per second on 16 Grace cores; samples are sized from that.
@@ -430,17 +430,31 @@ def run_ours(args, world, rank, local, pg):
                 "algorithmic_bytes": algo_bytes / launches_,
                 "hbm_frac_of_measured": (algo_bytes / (ms * 1e-3) / (hbm * 1e9)) if hbm else None}
 
-    # the sketch: 64 hashed bands per position, or on a four-letter database
-    # table_bands bands gathered from the 8-mer table (a min each) + the rest hashed
-    tb = ng.lib().ngia_sketch_table_bands() if table_active else 0
-    sketch_ops = positions * ((BANDS - tb) * SKETCH_ALU_OPS_PER_HASH + tb)
+    # the sketch: 64 hashed bands per position (logic-pipe bound), or on a
+    # four-letter database the rank walk over the 8-mer orders
+    sketch_bytes = int(db["lens"].sum()) / 2 + 4 * BANDS * n  # codes read + signatures
+    if table_active:
+        achieved = sketch_bytes / (sketch_ms * 1e-3)
+        sketch_roof = {
+            "bound": "hbm", "kernel": "sketch_rank_kernel (+ sketch_table_kernel for records "
+            "under the rank walk's minimum span)",
+            "achieved": achieved / 1e9, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / (hbm * 1e9) if hbm else None,
+            "peak_source": "measured: MEASURED_PEAKS hbm_gbs",
+            "units": {"signed_positions": positions}, "launches": 2, "ms": sketch_ms,
+            "traffic": SKETCH_TABLE_DRAM_BYTES_PER_POSITION * positions,
+            "algorithmic_bytes": sketch_bytes,
+            "note": "input read once; the walk is bound by shared-memory bit tests and "
+                    "issue, not by HBM",
+            "hash_equivalent_tops": positions * BANDS * SKETCH_ALU_OPS_PER_HASH
+            / (sketch_ms * 1e-3) / 1e12,
+            "table_bands": ng.lib().ngia_sketch_table_bands()}
+    else:
+        sketch_roof = roof("sketch_kernel<NibbleKmers>",
+                           positions * BANDS * SKETCH_ALU_OPS_PER_HASH, sketch_ms, positions,
+                           "signed_positions", SKETCH_DRAM_BYTES_PER_POSITION, sketch_bytes, 1)
     rs = {
-        "sketch": roof("sketch_table_kernel" if tb else "sketch_kernel<NibbleKmers>", sketch_ops,
-                       sketch_ms, positions, "signed_positions",
-                       SKETCH_TABLE_DRAM_BYTES_PER_POSITION if tb
-                       else SKETCH_DRAM_BYTES_PER_POSITION,
-                       # nibble codes read (half a byte per residue) + 64 signatures written
-                       int(db["lens"].sum()) / 2 + 4 * BANDS * n, 1),
+        "sketch": sketch_roof,
         # the align phase: one launch per populated width class, timed as a whole
         "align": roof("align phase (align_stream_kernel / align_group_kernel / align_general_kernel per width class)",
                       cells / 32 * ALIGN_OPS_PER_WORD_STEP, align_ms, cells, "computed_cells",
@@ -448,9 +462,6 @@ def run_ours(args, world, rank, local, pg):
                       # the pair list and scores once + every record's codes once
                       st["unique_pairs"] * 12 + int(db["lens"].sum()) / 2, 1),
     }
-    if tb:
-        # table entries are gathered from L2 (the 65,536 x table_bands words stay resident)
-        rs["sketch"].update(table_bands=tb, l2_table_bytes=positions * tb * 4)
     dominant = max(rs, key=lambda k: rs[k]["ms"])
     line = {
         "metric": "seqs clustered/s", "value": world * n / (mean_ms_max * 1e-3),

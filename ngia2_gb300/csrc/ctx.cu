@@ -43,14 +43,14 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
   NGIA_TRY(c->rep.reserve((size_t)kBands * c->n * 4));
   NGIA_TRY(c->sort_tmp.reserve(bucket_scratch_bytes(c->n, bands)));
   if (c->use_table && c->table_ok && !c->table_built) {
-    NGIA_TRY(c->sketch_table.reserve((size_t)kSketchTableEntries * kBands * 4));
-    NGIA_TRY(build_sketch_table(c->ab.inv, c->sketch_table.as<uint32_t>(), s));
+    NGIA_TRY(c->sketch_table.reserve(sketch_table_bytes()));
+    NGIA_TRY(build_sketch_table(c->ab.inv, c->sketch_table.p, s));
     c->table_built = true;
   }
   NGIA_CUDA(cudaEventRecord(c->ev[0], s));
   if (c->use_table && c->table_ok)
     NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
-                                 c->offs.as<uint64_t>(), c->n, c->sketch_table.as<uint32_t>(),
+                                 c->offs.as<uint64_t>(), c->n, c->ab.inv, c->sketch_table.p,
                                  c->sigs.as<uint32_t>(), s));
   else
     NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,

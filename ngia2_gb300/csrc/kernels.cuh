@@ -11,13 +11,17 @@ int launch_sketch(const uint32_t *packed, const uint64_t *offs, uint32_t n,
                   uint32_t *sigs, cudaStream_t s);
 int launch_sketch_nibbles(const uint32_t *nib, const uint64_t *offs, uint32_t n,
                           uint32_t *sigs, cudaStream_t s);
-// Databases of at most four residue codes (none of them 0): the 64 band hashes
-// of every 8-mer in a table of kSketchTableEntries x 64 words, built from the
-// aligner codes' inverse map; the sketch then reads the aligner codes (dense).
+// Databases of at most four residue codes (none of them 0): an 8-mer is one of
+// kSketchTableEntries values.  build_sketch_table fills sketch_table_bytes()
+// of device memory from the aligner codes' inverse map (part of the band
+// hashes of every 8-mer, and per band the 8-mers in increasing hash order);
+// the sketch then reads the aligner codes (dense).
 constexpr uint32_t kSketchTableEntries = 1u << 16;
-int build_sketch_table(uint64_t inv, uint32_t *table, cudaStream_t s);
+size_t sketch_table_bytes();
+int build_sketch_table(uint64_t inv, void *table, cudaStream_t s);
 int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
-                        uint32_t n, const uint32_t *table, uint32_t *sigs, cudaStream_t s);
+                        uint32_t n, uint64_t inv, const void *table, uint32_t *sigs,
+                        cudaStream_t s);
 
 // sort.cu
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs);

@@ -20,8 +20,16 @@ def dna_db(extra: list[bytes]):
     return build_db(seqs)
 
 
+def random_dna(lengths, seed):
+    rng = np.random.default_rng(seed)
+    return [bytes(rng.choice(np.frombuffer(b"ACGT", np.uint8), size=n)) for n in lengths]
+
+
 @pytest.mark.parametrize("extra", [
     [b"ACGT"[: k % 4 + 1] * (k % 9) for k in range(1, 40)],   # lengths 0..8 included
+    # both sides of the rank walk's minimum span (256 signed positions = length 263),
+    # a record of one repeated 8-mer, and a long one
+    random_dna(list(range(255, 272)) + [20_000], 5) + [b"ACGTACGT" * 400],
     [b"ACGTNACGTACGT" * 5],                                    # an N: five codes, no table
 ])
 def test_table_sketch_equals_hashing(cuda, built, extra):
