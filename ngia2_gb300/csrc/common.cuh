@@ -116,16 +116,19 @@ __host__ __device__ inline Band make_band(uint32_t lr, uint32_t lt, float t,
   return b;
 }
 
-// 32x32 blocks the reference loop visits for this pair.
+// 32x32 blocks the reference loop visits for this pair:
+//   sum over column blocks i < nc of max(0, min(i + rs, nr) - max(i - ls, 0)).
+// Terms vanish from i = nr + ls on; below that both ends are arithmetic runs,
+// so the sum has a closed form (checked against the loop on all small shapes).
 __host__ __device__ inline uint64_t band_blocks(const Band &b) {
   if (!b.pass) return 0;
-  uint64_t blocks = 0;
-  for (uint32_t i = 0; i < b.nc; ++i) {
-    const uint32_t j0 = i > b.ls ? i - b.ls : 0;
-    const uint32_t j1 = (i + b.rs < b.nr) ? i + b.rs : b.nr;
-    if (j1 > j0) blocks += j1 - j0;
-  }
-  return blocks;
+  const uint64_t ls = b.ls, rs = b.rs, nr = b.nr;
+  const uint64_t nc = b.nc < nr + ls ? b.nc : nr + ls;  // columns with live rows
+  const uint64_t up = nr > rs ? nr - rs : 0;            // columns with i + rs < nr
+  const uint64_t a = nc < up ? nc : up;
+  const uint64_t top = a * rs + a * (a - (a ? 1 : 0)) / 2 + (nc - a) * nr;
+  const uint64_t m = nc > ls + 1 ? nc - 1 - ls : 0;
+  return top - m * (m + 1) / 2;
 }
 
 // Final score from the LCS (src/buildGraph.hpp:245-252).

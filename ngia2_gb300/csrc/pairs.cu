@@ -134,19 +134,26 @@ classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pai
   if (threadIdx.x == 0) scells = 0;
   __syncthreads();
   unsigned long long my_cells = 0;
-  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
-       p += (uint64_t)gridDim.x * blockDim.x) {
-    const uint2 pr = pairs[p];
-    if (pr.x == kFull) {  // an empty pair slot (serving): never aligned
-      cls[p] = ((uint32_t)kSkipClass << 4) | 15u;
-      atomicAdd(&sc[kSkipClass], 1u);
-      continue;
+  const uint32_t lt_mask = (1u << (threadIdx.x & 31u)) - 1u;
+  // block-uniform trips, so that the class counts can be summed per warp
+  for (uint64_t p0 = (uint64_t)blockIdx.x * blockDim.x; p0 < count;
+       p0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t p = p0 + threadIdx.x;
+    uint32_t c = kFull;
+    if (p < count) {
+      const uint2 pr = pairs[p];
+      if (pr.x == kFull) {  // an empty pair slot (serving): never aligned
+        c = kSkipClass;
+        cls[p] = ((uint32_t)kSkipClass << 4) | 15u;
+      } else {
+        const Band b = make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode);
+        c = (uint32_t)width_class(b, plan);
+        cls[p] = class_sort_key((int)c, b);
+        my_cells += band_blocks(b);
+      }
     }
-    const Band b = make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode);
-    const int c = width_class(b, plan);
-    cls[p] = class_sort_key(c, b);
-    atomicAdd(&sc[c], 1u);
-    my_cells += band_blocks(b);
+    const uint32_t peers = __match_any_sync(kFull, c);
+    if (c != kFull && (peers & lt_mask) == 0) atomicAdd(&sc[c], (unsigned int)__popc(peers));
   }
   atomicAdd(&scells, my_cells);
   __syncthreads();

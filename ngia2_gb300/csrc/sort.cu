@@ -63,6 +63,96 @@ segment_scan_kernel(uint32_t *__restrict__ data, uint32_t len) {
   }
 }
 
+// Segments longer than one block's share (the digit counts of a big single
+// segment) are scanned by many blocks: chunk sums, a scan of the sums per
+// segment, then each chunk scanned from its offset.
+constexpr uint32_t kScanChunk = 8192;  // u32 per block, 8 per thread
+
+__device__ __forceinline__ uint32_t block_excl_scan_u32(uint32_t v, uint32_t *sh,
+                                                        uint32_t &total) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < blockDim.x / 32 ? sh[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, w, o);
+      if (lane >= (uint32_t)o) w += y;
+    }
+    sh[lane] = w;
+  }
+  __syncthreads();
+  total = sh[blockDim.x / 32 - 1];
+  const uint32_t before = warp ? sh[warp - 1] : 0u;
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(1024)
+chunk_sum_kernel(const uint32_t *__restrict__ data, uint32_t len, uint32_t nchunks,
+                 uint32_t *__restrict__ sums) {
+  __shared__ uint32_t sh[32];
+  const uint32_t *d = data + (size_t)blockIdx.y * len;
+  const uint32_t beg = blockIdx.x * kScanChunk + threadIdx.x * 8;
+  uint32_t v = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 8; ++k)
+    if (beg + k < len) v += d[beg + k];
+  uint32_t total;
+  block_excl_scan_u32(v, sh, total);
+  if (threadIdx.x == 0) sums[(size_t)blockIdx.y * nchunks + blockIdx.x] = total;
+}
+
+// exclusive scan of each segment's chunk sums (one block per segment)
+__global__ void __launch_bounds__(1024)
+chunk_sums_scan_kernel(uint32_t *__restrict__ sums, uint32_t nchunks) {
+  __shared__ uint32_t sh[32];
+  uint32_t *d = sums + (size_t)blockIdx.x * nchunks;
+  uint32_t run = 0;
+  for (uint32_t b = 0; b < nchunks; b += 1024) {  // block-uniform
+    const uint32_t i = b + threadIdx.x;
+    const uint32_t v = i < nchunks ? d[i] : 0u;
+    uint32_t total;
+    const uint32_t x = block_excl_scan_u32(v, sh, total);
+    if (i < nchunks) d[i] = run + x;
+    run += total;
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+chunk_apply_kernel(uint32_t *__restrict__ data, uint32_t len, uint32_t nchunks,
+                   const uint32_t *__restrict__ sums) {
+  __shared__ uint32_t sh[32];
+  uint32_t *d = data + (size_t)blockIdx.y * len;
+  const uint32_t beg = blockIdx.x * kScanChunk + threadIdx.x * 8;
+  uint32_t v[8], s = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 8; ++k) {
+    v[k] = beg + k < len ? d[beg + k] : 0u;
+    s += v[k];
+  }
+  uint32_t total;
+  uint32_t run = block_excl_scan_u32(s, sh, total) +
+                 sums[(size_t)blockIdx.y * nchunks + blockIdx.x];
+#pragma unroll
+  for (uint32_t k = 0; k < 8; ++k) {
+    if (beg + k < len) d[beg + k] = run;
+    run += v[k];
+  }
+}
+
+static uint32_t scan_chunks(uint32_t ntiles) {
+  const uint32_t len = 256 * ntiles;
+  return len > kScanChunk ? ceil_div(len, kScanChunk) : 0u;
+}
+
 __global__ void __launch_bounds__(kSortThreads)
 rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                   uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
@@ -112,7 +202,8 @@ rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs) {
   const size_t ntiles = ceil_div<size_t>(seg_len, kTile);
   const size_t n = (size_t)seg_len * segs;
-  return 2 * n * sizeof(uint32_t) + segs * 256 * ntiles * sizeof(uint32_t) + 256;
+  return 2 * n * sizeof(uint32_t) + segs * 256 * ntiles * sizeof(uint32_t) +
+         (size_t)segs * scan_chunks((uint32_t)ntiles) * sizeof(uint32_t) + 256;
 }
 
 int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
@@ -125,6 +216,8 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
   uint32_t *tk = static_cast<uint32_t *>(scratch);
   uint32_t *tv = tk + n;
   uint32_t *counts = tv + n;
+  uint32_t *sums = counts + (size_t)segs * 256 * ntiles;
+  const uint32_t nchunks = scan_chunks(ntiles);
   const int passes = (end_bit - begin_bit + 7) / 8;
   if (passes <= 0) {
     NGIA_CUDA(cudaMemcpyAsync(keys_out, keys_in, n * 4, cudaMemcpyDeviceToDevice, s));
@@ -143,8 +236,18 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
     dim3 grid(ntiles, segs);
     rs_hist_kernel<<<grid, kSortThreads, 0, s>>>(sk, seg_len, shift, ntiles, counts);
     NGIA_LAUNCHED();
-    segment_scan_kernel<<<segs, 1024, 0, s>>>(counts, 256 * ntiles);
-    NGIA_LAUNCHED();
+    if (nchunks == 0) {
+      segment_scan_kernel<<<segs, 1024, 0, s>>>(counts, 256 * ntiles);
+      NGIA_LAUNCHED();
+    } else {
+      chunk_sum_kernel<<<dim3(nchunks, segs), 1024, 0, s>>>(counts, 256 * ntiles, nchunks, sums);
+      NGIA_LAUNCHED();
+      chunk_sums_scan_kernel<<<segs, 1024, 0, s>>>(sums, nchunks);
+      NGIA_LAUNCHED();
+      chunk_apply_kernel<<<dim3(nchunks, segs), 1024, 0, s>>>(counts, 256 * ntiles, nchunks,
+                                                             sums);
+      NGIA_LAUNCHED();
+    }
     rs_scatter_kernel<<<grid, kSortThreads, 0, s>>>(sk, sv, dk, dv, seg_len, shift,
                                                     ntiles, counts);
     NGIA_LAUNCHED();

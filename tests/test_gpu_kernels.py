@@ -158,3 +158,14 @@ def test_sketch_bucket_at_scale(cuda, built):
         assert np.array_equal(sigs[:, i], oracle.sketch_record(rec)), i
     rep = gpu_bucket(sigs, 64)
     assert np.array_equal(rep, reference_rep_rows(sigs))
+
+
+@pytest.mark.parametrize("n,bands", [(400_000, 2), (140_000, 3), (1, 1)])
+def test_bucket_long_segments(cuda, built, n, bands):
+    """Segments whose digit counts outgrow one scan block (more than 32 tiles
+    of 4096) take the chunked scan; same rep rows as the numpy restatement.
+    Signatures from a small range, so buckets hold many members."""
+    rng = np.random.default_rng(n + bands)
+    sigs = rng.integers(0, 5000, size=(bands, n), dtype=np.uint32)
+    sigs[:, ::7] = rng.integers(0, 2**32, size=sigs[:, ::7].shape, dtype=np.uint64)
+    assert np.array_equal(gpu_bucket(sigs, bands), reference_rep_rows(sigs))
