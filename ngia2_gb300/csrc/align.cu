@@ -120,7 +120,7 @@ align_group_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restri
 // Batched form, streaming shared-memory table kernel (align_stream.cuh):
 // a persistent grid whose lanes take pairs of one class from its queue.
 template <int W, int K>
-__global__ void __launch_bounds__(kStreamThreads)
+__global__ void __launch_bounds__(kStreamThreads, NGIA_STREAM_MIN_BLOCKS)
 align_stream_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
                     uint64_t inv, const uint64_t *__restrict__ offs,
                     const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,

@@ -21,8 +21,8 @@
 //
 // Streams.  A lane whose pair ends (last column block, or a score of 0
 // already certain) writes the score, resets its window and takes the next
-// pair from the class's queue (one atomic per warp for all lanes that need
-// one), so the lanes stay busy until the queue drains.  Pairs are queued
+// pair of its warp's chunk (32 pairs claimed from the class's queue with one
+// atomic), so the lanes stay busy until the queue drains.  Pairs are queued
 // longest first.
 #pragma once
 
@@ -32,9 +32,25 @@ namespace ngia {
 
 // Threads per block of the streaming kernels (each warp owns its tables).
 constexpr int kStreamThreads = 64;
+// Resident blocks per SM the register allocation must allow (1: no bound).
+#ifndef NGIA_STREAM_MIN_BLOCKS
+#define NGIA_STREAM_MIN_BLOCKS 1
+#endif
 
 __host__ __device__ constexpr size_t stream_smem_bytes(int W, int K) {
   return (size_t)kStreamThreads * K * W * 4;
+}
+
+// A queued pair, as staged for a refill.
+struct PairDesc {
+  uint32_t p, lr, lt;
+  uint64_t ro, to;  // record offsets of rep and target
+};
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, uint32_t src) {
+  const uint32_t lo = __shfl_sync(kFull, (uint32_t)v, src);
+  const uint32_t hi = __shfl_sync(kFull, (uint32_t)(v >> 32), src);
+  return ((uint64_t)hi << 32) | lo;
 }
 
 // One lane's pair.
@@ -54,12 +70,33 @@ struct StreamPair {
   bool active;
 };
 
-// One column block at warp rotation R: retire the row leaving the window,
-// enter the rows reaching the band, 32 column steps.
-template <int W, int R, typename Tab>
-__device__ __forceinline__ void stream_block(uint32_t (&V)[W], const Tab &tab,
+// Retire the window word leaving at rotation R (its zeros are returned), then
+// the block's 32 column steps.
+template <int W, int R = 0>
+__device__ __forceinline__ uint32_t columns_dispatch(uint32_t rot, uint32_t (&V)[W],
+                                                     const uint32_t *tab, const uint4 &nib) {
+  if constexpr (R < W) {
+    if (rot == R) {
+      constexpr int out = (R + W - 1) % W;
+      const uint32_t z = __popc(~V[out]);
+      V[out] = kFull;
+      lds_columns<W, R>(V, tab, nib);
+      return z;
+    }
+    return columns_dispatch<W, R + 1>(rot, V, tab, nib);
+  }
+  return 0;
+}
+
+// One column block at warp rotation `rot`: retire the row leaving the window,
+// enter the rows reaching the band, 32 column steps.  Only the retire and the
+// column steps are instantiated per rotation (W copies of a short loop); the
+// table work indexes its slots at run time, so the code of a wide class stays
+// small enough for the instruction cache.
+template <int W, typename Tab>
+__device__ __forceinline__ void stream_block(uint32_t rot, uint32_t (&V)[W], const Tab &tab,
                                              StreamPair &sp) {
-  constexpr int out = (R + W - 1) % W;
+  const uint32_t out = rot == 0 ? (uint32_t)W - 1 : rot - 1;  // (rot + W - 1) % W
   // the next block's code words and entering row (J1 moves up at most one row
   // per block), loaded now so that their latency hides behind this block
   const bool more = sp.i + 1 < sp.nc;
@@ -72,29 +109,15 @@ __device__ __forceinline__ void stream_block(uint32_t (&V)[W], const Tab &tab,
     pfn_row = j1n - 1;
     pfn = load4(sp.rep + 1 + 4 * pfn_row);
   }
-  sp.lcs += __popc(~V[out]);
-  V[out] = kFull;
   tab.clear(out);
   for (; sp.act < j1; ++sp.act) {
     tab.fill(sp.in_slot, sp.act == sp.pf_row ? sp.pf : load4(sp.rep + 1 + 4 * sp.act));
     sp.in_slot = sp.in_slot + 1 == (uint32_t)W ? 0u : sp.in_slot + 1;
   }
-  lds_columns<W, R>(V, tab.base, sp.cur);
+  sp.lcs += columns_dispatch<W>(rot, V, tab.base, sp.cur);
   sp.cur = nxt;
   sp.pf = pfn;
   sp.pf_row = pfn_row;
-}
-
-template <int W, typename Tab, int R = 0>
-__device__ __forceinline__ void stream_dispatch(uint32_t rot, uint32_t (&V)[W],
-                                                const Tab &tab, StreamPair &sp) {
-  if constexpr (R < W) {
-    if (rot == R) {
-      if (sp.active) stream_block<W, R>(V, tab, sp);
-      return;
-    }
-    stream_dispatch<W, Tab, R + 1>(rot, V, tab, sp);
-  }
 }
 
 // The persistent kernel body of one width class.  `order[begin, end)` lists
@@ -121,52 +144,80 @@ __device__ inline uint32_t align_stream(const uint32_t *__restrict__ packed,
   for (int m = 0; m < W; ++m) V[m] = kFull;
   StreamPair sp;
   sp.active = false;
-  bool drained = false;
+  // Pair descriptors, staged per warp: lane l of A holds the l-th pair of the
+  // warp's current chunk of 32 (claimed with one atomic and loaded together:
+  // queue slot -> pair -> record offsets -> lengths), so a refill waits on
+  // global memory once per 32 pairs instead of once per pair.
+  PairDesc A{};
+  uint32_t a_count = 0, a_used = 0;      // warp-uniform
+  bool queue_empty = false;
   uint32_t done = 0, g = 0;
   for (;;) {
-    // lanes without a pair take the next ones from the queue
-    const uint32_t need = __ballot_sync(kFull, !sp.active && !drained);
-    if (need) {
-      const uint32_t leader = __ffs(need) - 1;
-      uint32_t first = 0;
-      if (lane == leader) first = atomicAdd(cursor, (unsigned int)__popc(need));
-      first = __shfl_sync(kFull, first, leader);
-      if (!sp.active && !drained) {
-        const uint32_t k = begin + first + __popc(need & ((1u << lane) - 1u));
-        if (k < end) {
-          const uint32_t p = order[k];
-          const uint2 pr = pairs[p];
-          const uint64_t to = offs[pr.y];
-          sp.rep = packed + offs[pr.x];
-          sp.tar = nib + to + 1;
-          sp.lr = __ldg(sp.rep);
-          sp.lt = __ldg(packed + to);
-          const Band b = make_band(sp.lr, sp.lt, t, fma_mode);
-          if (b.nc == 0) {
-            scores[p] = identity_score(0u, sp.lr, sp.lt, t);
-          } else {
-            sp.p = p;
-            sp.i = 0;
-            sp.nc = b.nc;
-            sp.nr = b.nr;
-            sp.rs = b.rs;
-            sp.act = 0;
-            sp.in_slot = (g + b.ls) % (uint32_t)W;
-            sp.lcs = 0;
-            sp.cur = load4(sp.tar);
-            sp.pf_row = kFull;
-            sp.active = true;
-          }
-        } else {
-          drained = true;
+    // lanes without a pair take the next descriptors of A, a new chunk
+    // being claimed when A runs out
+    uint32_t need = __ballot_sync(kFull, !sp.active);
+    while (need) {
+      if (a_used == a_count) {
+        if (queue_empty) break;
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(cursor, 32u);
+        first = __shfl_sync(kFull, first, 0);
+        const uint32_t size = end - begin;
+        a_count = first < size ? min(size - first, 32u) : 0u;
+        a_used = 0;
+        if (a_count == 0) {
+          queue_empty = true;
+          break;
+        }
+        if (lane < a_count) {
+          A.p = order[begin + first + lane];
+          const uint2 pr = pairs[A.p];
+          A.ro = offs[pr.x];
+          A.to = offs[pr.y];
+          A.lr = __ldg(packed + A.ro);
+          A.lt = __ldg(packed + A.to);
         }
       }
+      const uint32_t rank = __popc(need & ((1u << lane) - 1u));
+      const uint32_t take = min((uint32_t)__popc(need), a_count - a_used);
+      const uint32_t src = a_used + (rank < take ? rank : 0u);
+      const uint32_t p = __shfl_sync(kFull, A.p, src);
+      const uint32_t lr = __shfl_sync(kFull, A.lr, src);
+      const uint32_t lt = __shfl_sync(kFull, A.lt, src);
+      const uint64_t ro = shfl64(A.ro, src), to = shfl64(A.to, src);
+      const bool mine = (need >> lane & 1u) && rank < take;
+      if (mine) {
+        const Band b = make_band(lr, lt, t, fma_mode);
+        if (b.nc == 0) {
+          scores[p] = identity_score(0u, lr, lt, t);
+        } else {
+          sp.rep = packed + ro;
+          sp.tar = nib + to + 1;
+          sp.lr = lr;
+          sp.lt = lt;
+          sp.p = p;
+          sp.i = 0;
+          sp.nc = b.nc;
+          sp.nr = b.nr;
+          sp.rs = b.rs;
+          sp.act = 0;
+          sp.in_slot = (g + b.ls) % (uint32_t)W;
+          sp.lcs = 0;
+          sp.cur = load4(sp.tar);
+          sp.pf_row = kFull;
+          sp.active = true;
+        }
+      }
+      a_used += take;
+      need &= ~__ballot_sync(kFull, mine);
+      // lanes whose pair needed no alignment ask again
+      need |= __ballot_sync(kFull, mine && !sp.active);
     }
     if (!__any_sync(kFull, sp.active)) {
-      if (__all_sync(kFull, drained)) break;
+      if (queue_empty) break;
       continue;
     }
-    stream_dispatch<W>(g % (uint32_t)W, V, tab, sp);
+    if (sp.active) stream_block<W>(g % (uint32_t)W, V, tab, sp);
     ++g;
     if (sp.active) {
       ++sp.i;
