@@ -215,6 +215,41 @@ int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_
   return NGIA_OK;
 }
 
+// One warp per record: lane r takes residue r of each 32-residue block (its
+// aligner code from the nibble words, first position in the high nibble) and
+// three ballots give the block's planes.  Padding codes are 0.
+__global__ void __launch_bounds__(256)
+dense_planes_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restrict__ offs,
+                    uint32_t n, uint32_t *__restrict__ out) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const uint64_t o = offs[i];
+    const uint32_t len = dense[o];
+    if (lane == 0) out[o] = len;
+    for (uint32_t b = 0; b < (len + 31) >> 5; ++b) {
+      const uint32_t w = __ldg(dense + o + 1 + 4 * b + (lane >> 3));
+      const uint32_t code = (w >> (28 - 4 * (lane & 7u))) & 15u;
+      const uint32_t p0 = __ballot_sync(kFull, code & 1u);
+      const uint32_t p1 = __ballot_sync(kFull, code & 2u);
+      const uint32_t p2 = __ballot_sync(kFull, code & 4u);
+      if (lane < 4) out[o + 1 + 4 * b + lane] = lane == 0 ? p0 : lane == 1 ? p1 : lane == 2 ? p2 : 0u;
+    }
+  }
+}
+
+int launch_dense_planes(const uint32_t *dense, const uint64_t *offs, uint32_t n,
+                        uint32_t *out, cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
+  dense_planes_kernel<<<want < cap ? want : cap, 256, 0, s>>>(dense, offs, n, out);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
 // Blocks of a persistent launch: as many as fit on the device at once, and no
 // more than `want`.  Occupancy is looked up once per (kernel, device).
 struct OccEntry {
@@ -251,6 +286,7 @@ static int persistent_grid(F func, int threads, size_t smem, uint32_t want, uint
 struct RoundArgs {
   const uint32_t *packed, *nib;
   uint64_t inv;
+  const uint32_t *dplanes;
   const uint64_t *offs;
   const uint2 *pairs;
   const uint32_t *order, *bounds;
@@ -266,9 +302,11 @@ static int launch_stream_k(const RoundArgs &a, int cls, unsigned int *cursor,
   constexpr size_t smem = stream_smem_bytes(W, K);
   uint32_t grid = 0;
   NGIA_TRY(persistent_grid(align_stream_kernel<W, K>, kStreamThreads, smem, kFull, &grid));
+  // with dense planes (K = 8), inv = 0 tells the table to fill from them
+  const bool dense = K == 8 && a.dplanes;
   align_stream_kernel<W, K><<<grid, kStreamThreads, smem, s>>>(
-      a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls, cursor, a.scores, a.t,
-      a.fm, a.work);
+      dense ? a.dplanes : a.packed, a.nib, dense ? 0ull : a.inv, a.offs, a.pairs, a.order,
+      a.bounds, cls, cursor, a.scores, a.t, a.fm, a.work);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
@@ -325,7 +363,7 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const uint32_t *order, const uint32_t *bounds, uint32_t *scores,
                        uint32_t identity, unsigned long long *work, unsigned int *cursor,
                        cudaStream_t s) {
-  const RoundArgs a{packed, nib, ab.inv, offs, pairs, order, bounds, scores,
+  const RoundArgs a{packed, nib, ab.inv, ab.dplanes, offs, pairs, order, bounds, scores,
                     identity_threshold(identity), round_mode(), work};
   switch (cls) {
     case 0: return launch_stream<4>(a, ab.K, cls, cursor, s);

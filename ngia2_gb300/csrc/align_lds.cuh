@@ -42,7 +42,8 @@ constexpr int kLdsUnroll = NGIA_LDS_UNROLL;
 template <int W, int K = 16>
 struct LdsTable {
   uint32_t *base;  // this thread's column of the warp's table
-  uint64_t inv;    // nibble d = residue code that aligner code d stands for
+  uint64_t inv;    // nibble d = residue code that aligner code d stands for;
+                   // 0 (K = 8): the planes hold the aligner codes themselves
   __device__ __forceinline__ uint32_t *slot(uint32_t s) const { return base + s * 32; }
   static constexpr uint32_t kCodeStride = W * 32;  // words between codes
   __device__ __forceinline__ void clear(uint32_t s) const {
@@ -58,6 +59,11 @@ struct LdsTable {
       const uint32_t hi[4] = {~pl.z & ~pl.w, pl.z & ~pl.w, ~pl.z & pl.w, pl.z & pl.w};
 #pragma unroll
       for (int c = 1; c < 16; ++c) p[c * kCodeStride] = lo[c & 3] & hi[c >> 2];
+    } else if (inv == 0) {  // dense planes: aligner code bits in planes 0-2
+#pragma unroll
+      for (int d = 1; d < K; ++d)
+        p[d * kCodeStride] = ((d & 1) ? pl.x : ~pl.x) & ((d & 2) ? pl.y : ~pl.y) &
+                             ((d & 4) ? pl.z : ~pl.z);
     } else {
 #pragma unroll
       for (int d = 1; d < K; ++d) {

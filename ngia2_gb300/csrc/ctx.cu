@@ -223,7 +223,10 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
     NGIA_TRY(launch_recode(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), n, map,
                            c->nib_dense.as<uint32_t>(), s));
     c->align_nib = c->nib_dense.as<uint32_t>();
-    c->ab = Alphabet{8, inv};
+    NGIA_TRY(c->dplanes.reserve(words * 4));
+    NGIA_TRY(launch_dense_planes(c->nib_dense.as<uint32_t>(), c->offs.as<uint64_t>(), n,
+                                 c->dplanes.as<uint32_t>(), s));
+    c->ab = Alphabet{8, inv, c->dplanes.as<uint32_t>()};
     c->recode_map = map;
   }
   c->n = n;
@@ -299,8 +302,9 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
 void ngia_ctx_destroy(ngia_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  ngia::DevBuf *bufs[] = {&c->packed,   &c->nib,   &c->nib_dense, &c->presence, &c->offs,
-                          &c->lens,     &c->rep,   &c->sigs,      &c->ucount,   &c->uoff,
+  ngia::DevBuf *bufs[] = {&c->packed,   &c->nib,   &c->nib_dense, &c->dplanes,  &c->presence,
+                          &c->offs,     &c->lens,  &c->rep,       &c->sigs,     &c->ucount,
+                          &c->uoff,
                           &c->counters, &c->pairs, &c->scores,    &c->sort_tmp, &c->emit_tmp,
                           &c->edges,    &c->scan_tmp, &c->jobs, &c->sketch_table};
   for (ngia::DevBuf *b : bufs) b->release();

@@ -17,6 +17,7 @@ struct ngia_ctx {
   // targets as the aligner reads them: densely recoded when the database uses
   // at most 7 nonzero residue codes (aligner tables of 8 entries), else `nib`
   ngia::DevBuf nib_dense, presence;
+  ngia::DevBuf dplanes;  // recoded databases: planes of the aligner codes
   const uint32_t *align_nib = nullptr;
   ngia::Alphabet ab{16, 0xFEDCBA9876543210ull};
   uint64_t recode_map = 0;  // nibble c = aligner code of residue code c (when dense)

@@ -51,6 +51,10 @@ int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
 struct Alphabet {
   int K;         // 8 or 16 table entries per row block
   uint64_t inv;  // nibble d = residue code of aligner code d
+  // K = 8 only, optional: the records with their bit planes holding the
+  // aligner codes (planes 0-2; same layout and offsets as the packed records),
+  // from which a row block's eight table entries are one logic op each
+  const uint32_t *dplanes = nullptr;
 };
 // One width class of the batched aligner: a persistent launch over
 // order[bounds[cls], bounds[cls + 1]) (device bounds, from classify).  `cursor`
@@ -64,6 +68,10 @@ int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uin
                    uint32_t *presence, cudaStream_t s);
 int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
                   uint32_t *out, cudaStream_t s);
+// Aligner-code nibbles (recoded records) -> the same records as bit planes of
+// the aligner codes (Alphabet::dplanes).
+int launch_dense_planes(const uint32_t *dense, const uint64_t *offs, uint32_t n,
+                        uint32_t *out, cudaStream_t s);
 
 // pairs.cu
 int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
