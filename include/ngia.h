@@ -194,7 +194,7 @@ int ngia_ctx_align_pairs(ngia_ctx *ctx, const uint32_t *d_pairs, uint32_t count,
                          uint32_t identity, uint32_t *d_scores, ngia_stats *stats);
 
 /* How the batched aligner bins pairs (what ngia_ctx_autotune picks).  Width
- * classes: one pair per lane with a window of W = 4, 6, ..., 16 words for
+ * classes: one pair per lane with a window of W = 4, 5, ..., 12, 14, 16 words for
  * pairs whose window ls + min(rs, nr) (in 32-residue blocks) is at most
  * stream_max; otherwise the first group class -- G lanes per pair with K
  * words per lane: (16,1) (16,2) (16,4) (32,4) (32,8) (32,16) -- whose

@@ -366,21 +366,28 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
   const RoundArgs a{packed, nib, ab.inv, ab.dplanes, offs, pairs, order, bounds, scores,
                     identity_threshold(identity), round_mode(), work};
   switch (cls) {
-    case 0: return launch_stream<4>(a, ab.K, cls, cursor, s);
-    case 1: return launch_stream<6>(a, ab.K, cls, cursor, s);
-    case 2: return launch_stream<8>(a, ab.K, cls, cursor, s);
-    case 3: return launch_stream<10>(a, ab.K, cls, cursor, s);
-    case 4: return launch_stream<12>(a, ab.K, cls, cursor, s);
-    case 5: return launch_stream<14>(a, ab.K, cls, cursor, s);
-    case 6: return launch_stream<16>(a, ab.K, cls, cursor, s);
+#define NGIA_STREAM_CASE(C) \
+  case C: return launch_stream<class_width(C)>(a, ab.K, cls, cursor, s);
+    NGIA_STREAM_CASE(0)
+    NGIA_STREAM_CASE(1)
+    NGIA_STREAM_CASE(2)
+    NGIA_STREAM_CASE(3)
+    NGIA_STREAM_CASE(4)
+    NGIA_STREAM_CASE(5)
+    NGIA_STREAM_CASE(6)
+    NGIA_STREAM_CASE(7)
+    NGIA_STREAM_CASE(8)
+    NGIA_STREAM_CASE(9)
+    NGIA_STREAM_CASE(10)
+#undef NGIA_STREAM_CASE
 #define NGIA_GROUP_CASE(C) \
   case C: return launch_group<group_shape(C).G, group_shape(C).K>(a, ab.K, cls, cursor, s);
-    NGIA_GROUP_CASE(7)
-    NGIA_GROUP_CASE(8)
-    NGIA_GROUP_CASE(9)
-    NGIA_GROUP_CASE(10)
     NGIA_GROUP_CASE(11)
     NGIA_GROUP_CASE(12)
+    NGIA_GROUP_CASE(13)
+    NGIA_GROUP_CASE(14)
+    NGIA_GROUP_CASE(15)
+    NGIA_GROUP_CASE(16)
 #undef NGIA_GROUP_CASE
     case kGeneralClass: {
       uint32_t grid = 0;

@@ -54,14 +54,17 @@ __device__ __forceinline__ void add_chunk(uint32_t *s, const uint32_t *a, const 
 #undef NGIA_CHUNK
 }
 
-// s[0..W) = a + b as one W-word number (W even; carry in = cin != 0 when CIN).
+// s[0..W) = a + b as one W-word number (carry in = cin != 0 when CIN; W even
+// when CIN or W > 16).
 template <int W, bool CIN>
 __device__ __forceinline__ void add_words(uint32_t *s, const uint32_t *a,
                                           const uint32_t *b, uint32_t cin) {
-  static_assert(W > 0 && W % 2 == 0, "window width must be even");
   constexpr int C = W >= 8 ? 8 : (W >= 4 ? 4 : 2);
   uint32_t c = 0;
-  if constexpr (W == C) {
+  if constexpr (!CIN && W <= 16) {
+    add_run<W>(s, a, b);
+  } else if constexpr (W == C) {
+    static_assert(W % 2 == 0, "window width must be even");
     add_chunk<C, CIN, false>(s, a, b, cin, c);
   } else {
     add_chunk<C, CIN, true>(s, a, b, cin, c);
@@ -252,33 +255,35 @@ __device__ inline uint32_t lcs_general(const uint32_t *__restrict__ rep,
 }
 
 // Width classes of the batched aligner:
-//   0..6   streaming shared-memory table kernel (align_stream.cuh), one pair
-//          per lane, W = 4, 6, ..., 16 words by stream_width
-//   7..12  group kernel (align_group.cuh), one pair per group of G lanes with
+//   0..10  streaming shared-memory table kernel (align_stream.cuh), one pair
+//          per lane, W = 4, 5, ..., 12, 14, 16 words by stream_width (every
+//          width up to 12: a window word above the band costs as much as a
+//          live one, and bands of equal ls + rs - 1 are common)
+//   11..16 group kernel (align_group.cuh), one pair per group of G lanes with
 //          K words per lane: (16,1) (16,2) (16,4) (32,4) (32,8) (32,16)
-//   13     general kernel, one pair per thread (any width)
-//   14     pairs failing the length filter (score 0, not launched)
-constexpr int kNumLdsClasses = 7;
-constexpr int kFirstGroupClass = 7;
+//   17     general kernel, one pair per thread (any width)
+//   18     pairs failing the length filter (score 0, not launched)
+constexpr int kNumLdsClasses = 11;
+constexpr int kFirstGroupClass = 11;
 constexpr int kNumGroupClasses = 6;
-constexpr int kGeneralClass = 13;
-constexpr int kSkipClass = 14;
-constexpr int kNumClasses = 15;
+constexpr int kGeneralClass = 17;
+constexpr int kSkipClass = 18;
+constexpr int kNumClasses = 19;
 
 struct GroupShape {
   int G, K;
 };
 __host__ __device__ constexpr GroupShape group_shape(int c) {
-  return c == 7 ? GroupShape{16, 1}
-       : c == 8 ? GroupShape{16, 2}
-       : c == 9 ? GroupShape{16, 4}
-       : c == 10 ? GroupShape{32, 4}
-       : c == 11 ? GroupShape{32, 8}
-                 : GroupShape{32, 16};
+  return c == kFirstGroupClass ? GroupShape{16, 1}
+       : c == kFirstGroupClass + 1 ? GroupShape{16, 2}
+       : c == kFirstGroupClass + 2 ? GroupShape{16, 4}
+       : c == kFirstGroupClass + 3 ? GroupShape{32, 4}
+       : c == kFirstGroupClass + 4 ? GroupShape{32, 8}
+                                   : GroupShape{32, 16};
 }
 
-__host__ __device__ inline int class_width(int c) {
-  return c < kNumLdsClasses ? 4 + 2 * c : 0;
+__host__ __device__ constexpr int class_width(int c) {
+  return c < 9 ? 4 + c : c == 9 ? 14 : c == 10 ? 16 : 0;
 }
 
 // Window a streaming kernel needs for a pair: the live rows of block i,
@@ -318,7 +323,7 @@ __host__ __device__ inline ClassPlan default_plan() {
 __host__ __device__ inline int width_class(const Band &b, const ClassPlan &plan) {
   if (!b.pass) return kSkipClass;
   const uint32_t ws = stream_width(b);
-  if (ws <= plan.stream_max) return ws <= 4 ? 0 : (int)((ws - 3) / 2);  // 5,6 -> 1; 7,8 -> 2
+  if (ws <= plan.stream_max) return ws <= 4 ? 0 : ws <= 12 ? (int)ws - 4 : ws <= 14 ? 9 : 10;
   for (int g = 0; g < kNumGroupClasses; ++g) {
     const uint32_t lim = plan.group_limit[g];
     if (lim == 0) continue;
@@ -334,8 +339,8 @@ __host__ __device__ inline int width_class(const Band &b) {
 }
 
 // Queue order inside a class: longest targets first.  The sort key of a pair
-// is class-major, then 15 - floor(2 log2 nc) (column blocks in half-octaves,
-// capped at 15), one 8-bit radix pass.
+// is class-major, then 7 - floor(log2 nc) (column blocks in octaves, capped
+// at 7), one 8-bit radix pass.
 __host__ __device__ inline uint32_t class_sort_key(int cls, const Band &b) {
   uint32_t h = 0;
   if (b.nc > 1) {
@@ -346,8 +351,11 @@ __host__ __device__ inline uint32_t class_sort_key(int cls, const Band &b) {
 #endif
     h = 2 * lg + ((uint64_t)b.nc * b.nc >= (2ull << (2 * lg)) ? 1u : 0u);
   }
-  return ((uint32_t)cls << 4) | (15u - (h < 15u ? h : 15u));
+  h >>= 1;
+  return ((uint32_t)cls << 3) | (7u - (h < 7u ? h : 7u));
 }
 constexpr int kClassKeyBits = 8;
+static_assert(kNumClasses <= 32, "class sort key: 5 class bits");
+__host__ __device__ constexpr uint32_t skip_sort_key() { return ((uint32_t)kSkipClass << 3) | 7u; }
 
 }  // namespace ngia

@@ -260,4 +260,236 @@ __device__ __forceinline__ void add_words_pp(uint32_t *s, const uint32_t *a, con
   }
 }
 
+
+// ---- one chain of any length 1..16, no carry in or out -------------------------
+// add_run<N>(s, a, b): s[0..N) = a[0..N) + b[0..N) as one N-word number, the
+// carry rippling through the flag across the whole run (no carry value
+// materialised between words).  Written out for each N.
+__device__ __forceinline__ void add_run1(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.u32 %0, %1, %2;\n\t"
+      : "=r"(s[0])
+      : "r"(a[0]), "r"(b[0]));
+}
+__device__ __forceinline__ void add_run2(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %2, %4;\n\t"
+      "addc.u32 %1, %3, %5;\n\t"
+      : "=r"(s[0]), "=r"(s[1])
+      : "r"(a[0]), "r"(a[1]), "r"(b[0]), "r"(b[1]));
+}
+__device__ __forceinline__ void add_run3(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %3, %6;\n\t"
+      "addc.cc.u32 %1, %4, %7;\n\t"
+      "addc.u32 %2, %5, %8;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(b[0]), "r"(b[1]), "r"(b[2]));
+}
+__device__ __forceinline__ void add_run4(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %4, %8;\n\t"
+      "addc.cc.u32 %1, %5, %9;\n\t"
+      "addc.cc.u32 %2, %6, %10;\n\t"
+      "addc.u32 %3, %7, %11;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]));
+}
+__device__ __forceinline__ void add_run5(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %5, %10;\n\t"
+      "addc.cc.u32 %1, %6, %11;\n\t"
+      "addc.cc.u32 %2, %7, %12;\n\t"
+      "addc.cc.u32 %3, %8, %13;\n\t"
+      "addc.u32 %4, %9, %14;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]));
+}
+__device__ __forceinline__ void add_run6(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %6, %12;\n\t"
+      "addc.cc.u32 %1, %7, %13;\n\t"
+      "addc.cc.u32 %2, %8, %14;\n\t"
+      "addc.cc.u32 %3, %9, %15;\n\t"
+      "addc.cc.u32 %4, %10, %16;\n\t"
+      "addc.u32 %5, %11, %17;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]));
+}
+__device__ __forceinline__ void add_run7(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %7, %14;\n\t"
+      "addc.cc.u32 %1, %8, %15;\n\t"
+      "addc.cc.u32 %2, %9, %16;\n\t"
+      "addc.cc.u32 %3, %10, %17;\n\t"
+      "addc.cc.u32 %4, %11, %18;\n\t"
+      "addc.cc.u32 %5, %12, %19;\n\t"
+      "addc.u32 %6, %13, %20;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]));
+}
+__device__ __forceinline__ void add_run8(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %8, %16;\n\t"
+      "addc.cc.u32 %1, %9, %17;\n\t"
+      "addc.cc.u32 %2, %10, %18;\n\t"
+      "addc.cc.u32 %3, %11, %19;\n\t"
+      "addc.cc.u32 %4, %12, %20;\n\t"
+      "addc.cc.u32 %5, %13, %21;\n\t"
+      "addc.cc.u32 %6, %14, %22;\n\t"
+      "addc.u32 %7, %15, %23;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
+}
+__device__ __forceinline__ void add_run9(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %9, %18;\n\t"
+      "addc.cc.u32 %1, %10, %19;\n\t"
+      "addc.cc.u32 %2, %11, %20;\n\t"
+      "addc.cc.u32 %3, %12, %21;\n\t"
+      "addc.cc.u32 %4, %13, %22;\n\t"
+      "addc.cc.u32 %5, %14, %23;\n\t"
+      "addc.cc.u32 %6, %15, %24;\n\t"
+      "addc.cc.u32 %7, %16, %25;\n\t"
+      "addc.u32 %8, %17, %26;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]));
+}
+__device__ __forceinline__ void add_run10(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %10, %20;\n\t"
+      "addc.cc.u32 %1, %11, %21;\n\t"
+      "addc.cc.u32 %2, %12, %22;\n\t"
+      "addc.cc.u32 %3, %13, %23;\n\t"
+      "addc.cc.u32 %4, %14, %24;\n\t"
+      "addc.cc.u32 %5, %15, %25;\n\t"
+      "addc.cc.u32 %6, %16, %26;\n\t"
+      "addc.cc.u32 %7, %17, %27;\n\t"
+      "addc.cc.u32 %8, %18, %28;\n\t"
+      "addc.u32 %9, %19, %29;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]));
+}
+__device__ __forceinline__ void add_run11(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %11, %22;\n\t"
+      "addc.cc.u32 %1, %12, %23;\n\t"
+      "addc.cc.u32 %2, %13, %24;\n\t"
+      "addc.cc.u32 %3, %14, %25;\n\t"
+      "addc.cc.u32 %4, %15, %26;\n\t"
+      "addc.cc.u32 %5, %16, %27;\n\t"
+      "addc.cc.u32 %6, %17, %28;\n\t"
+      "addc.cc.u32 %7, %18, %29;\n\t"
+      "addc.cc.u32 %8, %19, %30;\n\t"
+      "addc.cc.u32 %9, %20, %31;\n\t"
+      "addc.u32 %10, %21, %32;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9]), "=r"(s[10])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]));
+}
+__device__ __forceinline__ void add_run12(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %12, %24;\n\t"
+      "addc.cc.u32 %1, %13, %25;\n\t"
+      "addc.cc.u32 %2, %14, %26;\n\t"
+      "addc.cc.u32 %3, %15, %27;\n\t"
+      "addc.cc.u32 %4, %16, %28;\n\t"
+      "addc.cc.u32 %5, %17, %29;\n\t"
+      "addc.cc.u32 %6, %18, %30;\n\t"
+      "addc.cc.u32 %7, %19, %31;\n\t"
+      "addc.cc.u32 %8, %20, %32;\n\t"
+      "addc.cc.u32 %9, %21, %33;\n\t"
+      "addc.cc.u32 %10, %22, %34;\n\t"
+      "addc.u32 %11, %23, %35;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9]), "=r"(s[10]), "=r"(s[11])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]), "r"(b[11]));
+}
+__device__ __forceinline__ void add_run13(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %13, %26;\n\t"
+      "addc.cc.u32 %1, %14, %27;\n\t"
+      "addc.cc.u32 %2, %15, %28;\n\t"
+      "addc.cc.u32 %3, %16, %29;\n\t"
+      "addc.cc.u32 %4, %17, %30;\n\t"
+      "addc.cc.u32 %5, %18, %31;\n\t"
+      "addc.cc.u32 %6, %19, %32;\n\t"
+      "addc.cc.u32 %7, %20, %33;\n\t"
+      "addc.cc.u32 %8, %21, %34;\n\t"
+      "addc.cc.u32 %9, %22, %35;\n\t"
+      "addc.cc.u32 %10, %23, %36;\n\t"
+      "addc.cc.u32 %11, %24, %37;\n\t"
+      "addc.u32 %12, %25, %38;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9]), "=r"(s[10]), "=r"(s[11]), "=r"(s[12])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(a[12]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]), "r"(b[11]), "r"(b[12]));
+}
+__device__ __forceinline__ void add_run14(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %14, %28;\n\t"
+      "addc.cc.u32 %1, %15, %29;\n\t"
+      "addc.cc.u32 %2, %16, %30;\n\t"
+      "addc.cc.u32 %3, %17, %31;\n\t"
+      "addc.cc.u32 %4, %18, %32;\n\t"
+      "addc.cc.u32 %5, %19, %33;\n\t"
+      "addc.cc.u32 %6, %20, %34;\n\t"
+      "addc.cc.u32 %7, %21, %35;\n\t"
+      "addc.cc.u32 %8, %22, %36;\n\t"
+      "addc.cc.u32 %9, %23, %37;\n\t"
+      "addc.cc.u32 %10, %24, %38;\n\t"
+      "addc.cc.u32 %11, %25, %39;\n\t"
+      "addc.cc.u32 %12, %26, %40;\n\t"
+      "addc.u32 %13, %27, %41;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9]), "=r"(s[10]), "=r"(s[11]), "=r"(s[12]), "=r"(s[13])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(a[12]), "r"(a[13]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]), "r"(b[11]), "r"(b[12]), "r"(b[13]));
+}
+__device__ __forceinline__ void add_run15(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %15, %30;\n\t"
+      "addc.cc.u32 %1, %16, %31;\n\t"
+      "addc.cc.u32 %2, %17, %32;\n\t"
+      "addc.cc.u32 %3, %18, %33;\n\t"
+      "addc.cc.u32 %4, %19, %34;\n\t"
+      "addc.cc.u32 %5, %20, %35;\n\t"
+      "addc.cc.u32 %6, %21, %36;\n\t"
+      "addc.cc.u32 %7, %22, %37;\n\t"
+      "addc.cc.u32 %8, %23, %38;\n\t"
+      "addc.cc.u32 %9, %24, %39;\n\t"
+      "addc.cc.u32 %10, %25, %40;\n\t"
+      "addc.cc.u32 %11, %26, %41;\n\t"
+      "addc.cc.u32 %12, %27, %42;\n\t"
+      "addc.cc.u32 %13, %28, %43;\n\t"
+      "addc.u32 %14, %29, %44;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9]), "=r"(s[10]), "=r"(s[11]), "=r"(s[12]), "=r"(s[13]), "=r"(s[14])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(a[12]), "r"(a[13]), "r"(a[14]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]), "r"(b[11]), "r"(b[12]), "r"(b[13]), "r"(b[14]));
+}
+__device__ __forceinline__ void add_run16(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  asm(
+      "add.cc.u32 %0, %16, %32;\n\t"
+      "addc.cc.u32 %1, %17, %33;\n\t"
+      "addc.cc.u32 %2, %18, %34;\n\t"
+      "addc.cc.u32 %3, %19, %35;\n\t"
+      "addc.cc.u32 %4, %20, %36;\n\t"
+      "addc.cc.u32 %5, %21, %37;\n\t"
+      "addc.cc.u32 %6, %22, %38;\n\t"
+      "addc.cc.u32 %7, %23, %39;\n\t"
+      "addc.cc.u32 %8, %24, %40;\n\t"
+      "addc.cc.u32 %9, %25, %41;\n\t"
+      "addc.cc.u32 %10, %26, %42;\n\t"
+      "addc.cc.u32 %11, %27, %43;\n\t"
+      "addc.cc.u32 %12, %28, %44;\n\t"
+      "addc.cc.u32 %13, %29, %45;\n\t"
+      "addc.cc.u32 %14, %30, %46;\n\t"
+      "addc.u32 %15, %31, %47;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(s[8]), "=r"(s[9]), "=r"(s[10]), "=r"(s[11]), "=r"(s[12]), "=r"(s[13]), "=r"(s[14]), "=r"(s[15])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(a[12]), "r"(a[13]), "r"(a[14]), "r"(a[15]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]), "r"(b[11]), "r"(b[12]), "r"(b[13]), "r"(b[14]), "r"(b[15]));
+}
+template <int N>
+__device__ __forceinline__ void add_run(uint32_t *s, const uint32_t *a, const uint32_t *b) {
+  static_assert(N >= 1 && N <= 16, "run length");
+#define NGIA_RUN(K) \
+  if constexpr (N == K) add_run##K(s, a, b);
+  NGIA_RUN(1) NGIA_RUN(2) NGIA_RUN(3) NGIA_RUN(4) NGIA_RUN(5) NGIA_RUN(6) NGIA_RUN(7)
+  NGIA_RUN(8) NGIA_RUN(9) NGIA_RUN(10) NGIA_RUN(11) NGIA_RUN(12) NGIA_RUN(13) NGIA_RUN(14)
+  NGIA_RUN(15) NGIA_RUN(16)
+#undef NGIA_RUN
+}
+
 }  // namespace ngia

@@ -144,7 +144,7 @@ classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pai
       const uint2 pr = pairs[p];
       if (pr.x == kFull) {  // an empty pair slot (serving): never aligned
         c = kSkipClass;
-        cls[p] = ((uint32_t)kSkipClass << 4) | 15u;
+        cls[p] = skip_sort_key();
       } else {
         const Band b = make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode);
         c = (uint32_t)width_class(b, plan);

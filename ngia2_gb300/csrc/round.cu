@@ -116,7 +116,9 @@ int Round::enqueue(const DbView &db, const uint2 *pairs, uint32_t m, uint32_t id
   // classes as concurrent branches, widest first (dealt round-robin over the
   // side streams): the few long pairs' warps leave most of the device to the
   // other classes instead of running alone at the end
-  const int launch_order[] = {kGeneralClass, 12, 11, 10, 9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
+  int launch_order[kNumClasses - 1];
+  launch_order[0] = kGeneralClass;
+  for (int c = 1; c < kNumClasses - 1; ++c) launch_order[c] = kGeneralClass - c;
   NGIA_CUDA(cudaEventRecord(fork_, s));
   for (int k = 0; k < kSide; ++k) NGIA_CUDA(cudaStreamWaitEvent(side_[k], fork_, 0));
   int k = 0;

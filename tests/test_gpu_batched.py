@@ -18,16 +18,16 @@ def width_class(lr: int, lt: int, identity: int) -> int:
     """The class the library bins a pair into (align.cuh width_class)."""
     bb = oracle.band_bounds(lr, lt, identity, oracle.ROUND_FMA)
     if bb is None:
-        return 14
+        return 18
     lsft, rsft = bb
     ls, rs, nr = lsft // 32, (rsft + 31) // 32, (lr + 31) // 32
     ws = ls + min(rs, nr)
     if ws <= 16:
-        return 0 if ws <= 4 else (ws - 3) // 2
-    for c, (g, k) in enumerate(GROUP_SHAPES, start=7):
+        return 0 if ws <= 4 else ws - 4 if ws <= 12 else 9 if ws <= 14 else 10
+    for c, (g, k) in enumerate(GROUP_SHAPES, start=11):
         if (nr + k - 1) // k <= g or ls + rs <= (g - 1) * k + g:
             return c
-    return 13
+    return 17
 
 
 def mutate(rng, s: bytes, sub: float, indel: float) -> bytes:
@@ -95,7 +95,7 @@ def test_batched_pairs_match_oracle(cuda, built, identity):
     assert st["unique_pairs"] == len(pairs)
     assert (want > 0).any() and (want == 0).any()
     # the set reaches the group kernels at every identity
-    assert classes & set(range(7, 13)), sorted(classes)
+    assert classes & set(range(11, 17)), sorted(classes)
 
 
 def test_every_group_class_is_covered(built):
@@ -106,8 +106,8 @@ def test_every_group_class_is_covered(built):
         seqs, pairs = pair_set(identity, 900 + identity)
         lens = [len(s) for s in seqs]
         seen |= {width_class(lens[r], lens[t], identity) for r, t in pairs}
-    assert set(range(7, 13)) <= seen, sorted(seen)
-    assert {0, 13} <= seen, sorted(seen)
+    assert set(range(11, 17)) <= seen, sorted(seen)
+    assert {0, 17} <= seen, sorted(seen)
 
 
 @pytest.mark.gpu
