@@ -59,7 +59,7 @@ struct StreamPair {
   const uint32_t *tar;  // target's nibble code words
   uint32_t p;           // pair index (score slot)
   uint32_t i;           // current column block
-  uint32_t nc, nr, rs;
+  uint32_t nc, nr, rs, ls;
   uint32_t act;         // rows entered so far
   uint32_t in_slot;     // slot of row `act`
   uint32_t lcs;         // zeros of the retired rows
@@ -70,20 +70,50 @@ struct StreamPair {
   bool active;
 };
 
+// What the early exit needs to know about a pair after a block.
+struct BlockEnd {
+  int32_t left;  // target columns after this block
+  int32_t lr;    // rep length
+  int32_t row0;  // first row of window word 0 (32 (i - ls); negative: virtual)
+};
+
 // Retire the window word leaving at rotation R (its zeros are returned), then
-// the block's 32 column steps.
+// the block's 32 column steps, then, in row order (static at rotation R):
+//   total = the LCS so far (zeros of the retired rows and of the window),
+//   ub    = an upper bound of the pair's final LCS.
+// The banded LCS is the best monotone path through the matrix counting
+// matches in band cells only (rows below the band hold their values, rows
+// above it enter all ones with empty masks).  Such a path crosses the last
+// column done at some row j, so the final LCS is at most
+//   L(j) + min(columns left, Lr - j)
+// with L(j) the zeros of rows 0..j now.  Taken at word granularity (the
+// zeros through the end of a word, the rows above its start) and over the
+// retired rows (at most all retired zeros + columns left), the maximum is an
+// upper bound no larger than total + columns left.
 template <int W, int R = 0>
 __device__ __forceinline__ uint32_t columns_dispatch(uint32_t rot, uint32_t (&V)[W],
-                                                     const uint32_t *tab, const uint4 &nib) {
+                                                     const uint32_t *tab, const uint4 &nib,
+                                                     uint32_t retired, const BlockEnd &be,
+                                                     uint32_t &total, uint32_t &ub) {
   if constexpr (R < W) {
     if (rot == R) {
       constexpr int out = (R + W - 1) % W;
       const uint32_t z = __popc(~V[out]);
       V[out] = kFull;
       lds_columns<W, R>(V, tab, nib);
+      int32_t p = (int32_t)(retired + z);
+      int32_t best = p + min(be.left, be.lr);
+#pragma unroll
+      for (int m = 0; m < W; ++m) {
+        p += __popc(~V[(R + m) % W]);
+        const int32_t above = max(be.lr - (be.row0 + 32 * m), 0);
+        best = max(best, p + min(be.left, above));
+      }
+      total = (uint32_t)p;
+      ub = (uint32_t)best;
       return z;
     }
-    return columns_dispatch<W, R + 1>(rot, V, tab, nib);
+    return columns_dispatch<W, R + 1>(rot, V, tab, nib, retired, be, total, ub);
   }
   return 0;
 }
@@ -95,7 +125,7 @@ __device__ __forceinline__ uint32_t columns_dispatch(uint32_t rot, uint32_t (&V)
 // small enough for the instruction cache.
 template <int W, typename Tab>
 __device__ __forceinline__ void stream_block(uint32_t rot, uint32_t (&V)[W], const Tab &tab,
-                                             StreamPair &sp) {
+                                             StreamPair &sp, uint32_t &total, uint32_t &ub) {
   const uint32_t out = rot == 0 ? (uint32_t)W - 1 : rot - 1;  // (rot + W - 1) % W
   // the next block's code words and entering row (J1 moves up at most one row
   // per block), loaded now so that their latency hides behind this block
@@ -114,7 +144,10 @@ __device__ __forceinline__ void stream_block(uint32_t rot, uint32_t (&V)[W], con
     tab.fill(sp.in_slot, sp.act == sp.pf_row ? sp.pf : load4(sp.rep + 1 + 4 * sp.act));
     sp.in_slot = sp.in_slot + 1 == (uint32_t)W ? 0u : sp.in_slot + 1;
   }
-  sp.lcs += columns_dispatch<W>(rot, V, tab.base, sp.cur);
+  const int32_t cols = 32 * (int32_t)(sp.i + 1);
+  const BlockEnd be{(int32_t)sp.lt > cols ? (int32_t)sp.lt - cols : 0, (int32_t)sp.lr,
+                    32 * ((int32_t)sp.i - (int32_t)sp.ls)};
+  sp.lcs += columns_dispatch<W>(rot, V, tab.base, sp.cur, sp.lcs, be, total, ub);
   sp.cur = nxt;
   sp.pf = pfn;
   sp.pf_row = pfn_row;
@@ -200,6 +233,7 @@ __device__ inline uint32_t align_stream(const uint32_t *__restrict__ packed,
           sp.nc = b.nc;
           sp.nr = b.nr;
           sp.rs = b.rs;
+          sp.ls = b.ls;
           sp.act = 0;
           sp.in_slot = (g + b.ls) % (uint32_t)W;
           sp.lcs = 0;
@@ -217,17 +251,15 @@ __device__ inline uint32_t align_stream(const uint32_t *__restrict__ packed,
       if (queue_empty) break;
       continue;
     }
-    if (sp.active) stream_block<W>(g % (uint32_t)W, V, tab, sp);
+    uint32_t total = 0, ub = 0;
+    if (sp.active) stream_block<W>(g % (uint32_t)W, V, tab, sp, total, ub);
     ++g;
     if (sp.active) {
       ++sp.i;
       done += W;
-      uint32_t z = sp.lcs;
-#pragma unroll
-      for (int m = 0; m < W; ++m) z += __popc(~V[m]);
       const bool last = sp.i >= sp.nc;
-      if (last || !stream_may_reach(z, 32 * sp.i, sp.lr, sp.lt, t)) {
-        scores[sp.p] = last ? identity_score(z, sp.lr, sp.lt, t) : 0u;
+      if (last || !lcs_may_reach(ub, sp.lr, sp.lt, t)) {
+        scores[sp.p] = last ? identity_score(total, sp.lr, sp.lt, t) : 0u;
         sp.active = false;
 #pragma unroll
         for (int m = 0; m < W; ++m) V[m] = kFull;

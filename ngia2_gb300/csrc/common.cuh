@@ -158,6 +158,12 @@ __host__ __device__ inline bool stream_may_reach(uint32_t lcs_so_far, uint32_t c
   return identity_score(ub, lr, lt, t) > 0;
 }
 
+// The same test for an upper bound of the final LCS itself.
+__host__ __device__ inline bool lcs_may_reach(uint32_t ub, uint32_t lr, uint32_t lt, float t) {
+  const uint32_t cap = lr < lt ? lr : lt;
+  return identity_score(ub < cap ? ub : cap, lr, lt, t) > 0;
+}
+
 __host__ __device__ inline bool may_reach_threshold(uint32_t lcs_so_far, uint32_t cols_done,
                                                     const Band &b) {
   return stream_may_reach(lcs_so_far, cols_done, b.lr, b.lt, b.t);
