@@ -133,59 +133,133 @@ align_stream_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restr
   count_work(done, work);
 }
 
+// Load-time layout kernels: one warp per record, lane k taking the record's
+// 32-residue blocks k, k + 32, ... (four words each, coalesced across the
+// warp); bit work by shifts and masks, no per-residue loops.
+
+// bits 0..7 of b to bits 0, 4, ..., 28
+__device__ __forceinline__ uint32_t spread8(uint32_t b) {
+  b = (b | (b << 12)) & 0x000F000Fu;
+  b = (b | (b << 6)) & 0x03030303u;
+  return (b | (b << 3)) & 0x11111111u;
+}
+
+// Four plane words of a block (bit r of plane e = bit e of the code of
+// residue r) -> its four nibble words (word q: residues 8q..8q+7, the first in
+// the high nibble).
+__device__ __forceinline__ void planes_to_nibbles(const uint32_t (&pl)[4], int np,
+                                                  uint32_t (&out)[4]) {
+  uint32_t rv[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) rv[e] = e < np ? __brev(pl[e]) : 0u;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t w = 0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (e < np) w |= spread8((rv[e] >> (24 - 8 * q)) & 0xFFu) << e;
+    out[q] = w;
+  }
+}
+
+// mask of the residues of a block whose code is c, from its four planes
+__device__ __forceinline__ uint32_t code_mask(const uint32_t (&pl)[4], uint32_t c) {
+  return ((c & 1u) ? pl[0] : ~pl[0]) & ((c & 2u) ? pl[1] : ~pl[1]) &
+         ((c & 4u) ? pl[2] : ~pl[2]) & ((c & 8u) ? pl[3] : ~pl[3]);
+}
+
 // Planes -> nibbles: the same record layout, with each block's four plane
-// words replaced by four words of eight 4-bit codes (position 8k + j of the
-// record in nibble 7 - j of word k).  The length word is copied.
+// words replaced by four words of eight 4-bit codes.  The length word is
+// copied.  presence |= bit c for every code c of a real residue.
 __global__ void __launch_bounds__(256)
 nibble_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
               uint32_t n, uint32_t *__restrict__ nib, uint32_t *__restrict__ presence) {
-  __shared__ uint32_t seen;
-  if (threadIdx.x == 0) seen = 0;
-  __syncthreads();
-  uint32_t mine = 0;  // bit c set when code c occurs
-  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  uint32_t mine = 0;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
-    const uint32_t len = packed[o];
-    if (threadIdx.x == 0) nib[o] = len;
+    const uint32_t len = __ldg(packed + o);
+    if (lane == 0) nib[o] = len;
     const uint32_t blocks = (len + 31) >> 5;
-    for (uint32_t w = threadIdx.x; w < 4 * blocks; w += blockDim.x) {
-      const uint32_t blk = w >> 2, q = w & 3u;
-      const uint32_t *pl = packed + o + 1 + 4 * blk;
-      uint32_t out = 0;
+    for (uint32_t k = lane; k < blocks; k += 32) {
+      const uint32_t *src = packed + o + 1 + 4 * k;
+      const uint32_t pl[4] = {__ldg(src), __ldg(src + 1), __ldg(src + 2), __ldg(src + 3)};
+      uint32_t w[4];
+      planes_to_nibbles(pl, 4, w);
+      uint32_t *dst = nib + o + 1 + 4 * k;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const uint32_t byte = (pl[e] >> (8 * q)) & 0xFFu;
+      for (int q = 0; q < 4; ++q) dst[q] = w[q];
+      const uint32_t left = len - 32 * k;
+      const uint32_t real = left >= 32 ? kFull : (1u << left) - 1u;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) out |= ((byte >> j) & 1u) << (28 - 4 * j + e);
-      }
-      nib[o + 1 + w] = out;
-      // codes of real residues (none in the padding words past the record's end)
-      const uint32_t valid = 8 * w >= len ? 0u : (len - 8 * w < 8 ? len - 8 * w : 8u);
-#pragma unroll
-      for (uint32_t j = 0; j < 8; ++j)
-        if (j < valid) mine |= 1u << ((out >> (28 - 4 * j)) & 15u);
+      for (uint32_t c = 0; c < 16; ++c)
+        if (code_mask(pl, c) & real) mine |= 1u << c;
     }
   }
-  if (mine) atomicOr(&seen, mine);
-  __syncthreads();
-  if (threadIdx.x == 0 && seen) atomicOr(presence, seen);
+  mine = __reduce_or_sync(kFull, mine);
+  if (lane == 0 && mine) atomicOr(presence, mine);
 }
 
 // Rewrites nibble codes through a 16-entry map (map nibble c = new code of c).
 __global__ void __launch_bounds__(256)
 recode_kernel(const uint32_t *__restrict__ nib, const uint64_t *__restrict__ offs, uint32_t n,
               uint64_t map, uint32_t *__restrict__ out) {
-  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
-    const uint32_t len = nib[o];
-    if (threadIdx.x == 0) out[o] = len;
+    const uint32_t len = __ldg(nib + o);
+    if (lane == 0) out[o] = len;
     const uint32_t words = ((len + 31) >> 5) * 4;
-    for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) {
-      const uint32_t x = nib[o + 1 + w];
+    for (uint32_t w = lane; w < words; w += 32) {
+      const uint32_t x = __ldg(nib + o + 1 + w);
       uint32_t y = 0;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) y |= (uint32_t)((map >> (4 * ((x >> (4 * j)) & 15u))) & 15u) << (4 * j);
+      for (int j = 0; j < 8; ++j)
+        y |= (uint32_t)((map >> (4 * ((x >> (4 * j)) & 15u))) & 15u) << (4 * j);
       out[o + 1 + w] = y;
+    }
+  }
+}
+
+// Recoded databases from their packed planes, in one pass: the aligner-code
+// nibbles (as recode_kernel writes them) and the planes of the aligner codes
+// (planes 0-2, plane 3 zero).  bits[b] = the residue codes whose aligner code
+// has bit b set.
+__global__ void __launch_bounds__(256)
+dense_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
+                     uint32_t n, uint32_t bit0, uint32_t bit1, uint32_t bit2,
+                     uint32_t *__restrict__ dense_nib, uint32_t *__restrict__ dplanes) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const uint64_t o = offs[i];
+    const uint32_t len = __ldg(packed + o);
+    if (lane == 0) {
+      dense_nib[o] = len;
+      dplanes[o] = len;
+    }
+    const uint32_t blocks = (len + 31) >> 5;
+    for (uint32_t k = lane; k < blocks; k += 32) {
+      const uint32_t *src = packed + o + 1 + 4 * k;
+      const uint32_t pl[4] = {__ldg(src), __ldg(src + 1), __ldg(src + 2), __ldg(src + 3)};
+      uint32_t d[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (uint32_t c = 1; c < 16; ++c) {
+        const uint32_t m = code_mask(pl, c);
+        d[0] |= (bit0 >> c) & 1u ? m : 0u;
+        d[1] |= (bit1 >> c) & 1u ? m : 0u;
+        d[2] |= (bit2 >> c) & 1u ? m : 0u;
+      }
+      uint32_t w[4];
+      planes_to_nibbles(d, 3, w);
+      uint32_t *dn = dense_nib + o + 1 + 4 * k, *dp = dplanes + o + 1 + 4 * k;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        dn[q] = w[q];
+        dp[q] = d[q];
+      }
     }
   }
 }
@@ -196,9 +270,9 @@ int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uin
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const uint32_t cap = (uint32_t)sms * 16;
+  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
   NGIA_CUDA(cudaMemsetAsync(presence, 0, sizeof(uint32_t), s));
-  nibble_kernel<<<n < cap ? n : cap, 256, 0, s>>>(packed, offs, n, nib, presence);
+  nibble_kernel<<<want < cap ? want : cap, 256, 0, s>>>(packed, offs, n, nib, presence);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
@@ -209,43 +283,29 @@ int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const uint32_t cap = (uint32_t)sms * 16;
-  recode_kernel<<<n < cap ? n : cap, 256, 0, s>>>(nib, offs, n, map, out);
+  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
+  recode_kernel<<<want < cap ? want : cap, 256, 0, s>>>(nib, offs, n, map, out);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
 
-// One warp per record: lane r takes residue r of each 32-residue block (its
-// aligner code from the nibble words, first position in the high nibble) and
-// three ballots give the block's planes.  Padding codes are 0.
-__global__ void __launch_bounds__(256)
-dense_planes_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restrict__ offs,
-                    uint32_t n, uint32_t *__restrict__ out) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-    const uint64_t o = offs[i];
-    const uint32_t len = dense[o];
-    if (lane == 0) out[o] = len;
-    for (uint32_t b = 0; b < (len + 31) >> 5; ++b) {
-      const uint32_t w = __ldg(dense + o + 1 + 4 * b + (lane >> 3));
-      const uint32_t code = (w >> (28 - 4 * (lane & 7u))) & 15u;
-      const uint32_t p0 = __ballot_sync(kFull, code & 1u);
-      const uint32_t p1 = __ballot_sync(kFull, code & 2u);
-      const uint32_t p2 = __ballot_sync(kFull, code & 4u);
-      if (lane < 4) out[o + 1 + 4 * b + lane] = lane == 0 ? p0 : lane == 1 ? p1 : lane == 2 ? p2 : 0u;
-    }
-  }
-}
-
-int launch_dense_planes(const uint32_t *dense, const uint64_t *offs, uint32_t n,
-                        uint32_t *out, cudaStream_t s) {
+int launch_dense_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n,
+                         uint64_t map, uint32_t *dense_nib, uint32_t *dplanes,
+                         cudaStream_t s) {
   if (n == 0) return NGIA_OK;
+  uint32_t bits[3] = {0u, 0u, 0u};
+  for (uint32_t c = 1; c < 16; ++c) {
+    const uint32_t d = (uint32_t)(map >> (4 * c)) & 15u;
+    if (d > 7) return NGIA_ERR_ARG;  // three planes hold aligner codes 0..7
+    for (int b = 0; b < 3; ++b)
+      if ((d >> b) & 1u) bits[b] |= 1u << c;
+  }
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
-  dense_planes_kernel<<<want < cap ? want : cap, 256, 0, s>>>(dense, offs, n, out);
+  dense_layouts_kernel<<<want < cap ? want : cap, 256, 0, s>>>(packed, offs, n, bits[0], bits[1],
+                                                               bits[2], dense_nib, dplanes);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

@@ -42,10 +42,12 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
   NGIA_TRY(c->sigs.reserve((size_t)kBands * c->n * 4));
   NGIA_TRY(c->rep.reserve((size_t)kBands * c->n * 4));
   NGIA_TRY(c->sort_tmp.reserve(bucket_scratch_bytes(c->n, bands)));
-  if (c->use_table && c->table_ok && !c->table_built) {
+  // the tables depend only on the aligner-code map: built once per map
+  if (c->use_table && c->table_ok && !(c->table_built && c->table_inv == c->ab.inv)) {
     NGIA_TRY(c->sketch_table.reserve(sketch_table_bytes()));
     NGIA_TRY(build_sketch_table(c->ab.inv, c->sketch_table.p, s));
     c->table_built = true;
+    c->table_inv = c->ab.inv;
   }
   NGIA_CUDA(cudaEventRecord(c->ev[0], s));
   if (c->use_table && c->table_ok)
@@ -209,7 +211,6 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
   c->ab = Alphabet{16, 0xFEDCBA9876543210ull};
   c->recode_map = 0;
   c->table_ok = (present & 1u) == 0 && present != 0 && __builtin_popcount(present) <= 4;
-  c->table_built = false;
   if (__builtin_popcount(present & ~1u) <= 7) {
     uint64_t map = 0, inv = 0;
     int next = 1;
@@ -220,12 +221,10 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
       ++next;
     }
     NGIA_TRY(c->nib_dense.reserve(words * 4));
-    NGIA_TRY(launch_recode(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), n, map,
-                           c->nib_dense.as<uint32_t>(), s));
-    c->align_nib = c->nib_dense.as<uint32_t>();
     NGIA_TRY(c->dplanes.reserve(words * 4));
-    NGIA_TRY(launch_dense_planes(c->nib_dense.as<uint32_t>(), c->offs.as<uint64_t>(), n,
-                                 c->dplanes.as<uint32_t>(), s));
+    NGIA_TRY(launch_dense_layouts(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), n, map,
+                                  c->nib_dense.as<uint32_t>(), c->dplanes.as<uint32_t>(), s));
+    c->align_nib = c->nib_dense.as<uint32_t>();
     c->ab = Alphabet{8, inv, c->dplanes.as<uint32_t>()};
     c->recode_map = map;
   }

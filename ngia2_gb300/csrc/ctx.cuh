@@ -24,6 +24,7 @@ struct ngia_ctx {
   // at most four residue codes, none of them 0: the sketch reads the 64 band
   // hashes of every 8-mer from a table (built on first use after a load)
   bool table_ok = false, table_built = false, use_table = true;
+  uint64_t table_inv = 0;  // the aligner-code map the sketch tables were built for
   ngia::DevBuf sketch_table;
   // graph build work
   ngia::DevBuf ucount, uoff, counters, pairs, scores, emit_tmp, edges, scan_tmp, jobs,

@@ -68,10 +68,12 @@ int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uin
                    uint32_t *presence, cudaStream_t s);
 int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
                   uint32_t *out, cudaStream_t s);
-// Aligner-code nibbles (recoded records) -> the same records as bit planes of
-// the aligner codes (Alphabet::dplanes).
-int launch_dense_planes(const uint32_t *dense, const uint64_t *offs, uint32_t n,
-                        uint32_t *out, cudaStream_t s);
+// Packed records and a code map with new codes 0..7 -> the recoded nibbles
+// (as launch_recode of their nibbles) and the planes of the new codes
+// (Alphabet::dplanes), in one pass.
+int launch_dense_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n,
+                         uint64_t map, uint32_t *dense_nib, uint32_t *dplanes,
+                         cudaStream_t s);
 
 // pairs.cu
 int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
