@@ -332,6 +332,9 @@ static int persistent_grid(F func, int threads, size_t smem, uint32_t want, uint
     OccEntry e{key, dev, 0, 0};
     NGIA_CUDA(cudaDeviceGetAttribute(&e.sms, cudaDevAttrMultiProcessorCount, dev));
     NGIA_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the most shared memory per SM the L1 split allows: more resident blocks
+    NGIA_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   (int)cudaSharedmemCarveoutMaxShared));
     NGIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e.per_sm, func, threads, smem));
     if (e.per_sm < 1) e.per_sm = 1;
     g_occ.push_back(e);
@@ -362,11 +365,11 @@ static int launch_stream_k(const RoundArgs &a, int cls, unsigned int *cursor,
   constexpr size_t smem = stream_smem_bytes(W, K);
   uint32_t grid = 0;
   NGIA_TRY(persistent_grid(align_stream_kernel<W, K>, kStreamThreads, smem, kFull, &grid));
-  // with dense planes (K = 8), inv = 0 tells the table to fill from them
-  const bool dense = K == 8 && a.dplanes;
+  // K = 8 tables fill from the code planes (records with the same offsets)
+  if (K == 8 && !a.dplanes) return NGIA_ERR_STATE;
   align_stream_kernel<W, K><<<grid, kStreamThreads, smem, s>>>(
-      dense ? a.dplanes : a.packed, a.nib, dense ? 0ull : a.inv, a.offs, a.pairs, a.order,
-      a.bounds, cls, cursor, a.scores, a.t, a.fm, a.work);
+      K == 8 ? a.dplanes : a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls,
+      cursor, a.scores, a.t, a.fm, a.work);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
@@ -376,9 +379,10 @@ static int launch_group_k(const RoundArgs &a, int cls, unsigned int *cursor, cud
   constexpr size_t smem = group_smem_bytes(K, KC);
   uint32_t grid = 0;
   NGIA_TRY(persistent_grid(align_group_kernel<G, K, KC>, kGroupThreads, smem, kFull, &grid));
+  if (KC == 8 && !a.dplanes) return NGIA_ERR_STATE;
   align_group_kernel<G, K, KC><<<grid, kGroupThreads, smem, s>>>(
-      a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls, cursor, a.scores, a.t,
-      a.fm, a.work);
+      KC == 8 ? a.dplanes : a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls,
+      cursor, a.scores, a.t, a.fm, a.work);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

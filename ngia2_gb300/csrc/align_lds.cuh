@@ -23,6 +23,8 @@
 // lanes of a load hit 32 different banks.
 #pragma once
 
+#include <utility>
+
 #include "align.cuh"
 
 #ifndef NGIA_LDS_UNROLL
@@ -42,8 +44,8 @@ constexpr int kLdsUnroll = NGIA_LDS_UNROLL;
 template <int W, int K = 16>
 struct LdsTable {
   uint32_t *base;  // this thread's column of the warp's table
-  uint64_t inv;    // nibble d = residue code that aligner code d stands for;
-                   // 0 (K = 8): the planes hold the aligner codes themselves
+  uint64_t inv;    // nibble d = residue code that aligner code d stands for
+                   // (K = 8: the rows come as code planes, see fill)
   __device__ __forceinline__ uint32_t *slot(uint32_t s) const { return base + s * 32; }
   static constexpr uint32_t kCodeStride = W * 32;  // words between codes
   __device__ __forceinline__ void clear(uint32_t s) const {
@@ -59,25 +61,25 @@ struct LdsTable {
       const uint32_t hi[4] = {~pl.z & ~pl.w, pl.z & ~pl.w, ~pl.z & pl.w, pl.z & pl.w};
 #pragma unroll
       for (int c = 1; c < 16; ++c) p[c * kCodeStride] = lo[c & 3] & hi[c >> 2];
-    } else if (inv == 0) {  // dense planes: aligner code bits in planes 0-2
+    } else {  // K = 8: the code planes (aligner code bits in planes 0-2)
 #pragma unroll
       for (int d = 1; d < K; ++d)
         p[d * kCodeStride] = ((d & 1) ? pl.x : ~pl.x) & ((d & 2) ? pl.y : ~pl.y) &
                              ((d & 4) ? pl.z : ~pl.z);
-    } else {
-#pragma unroll
-      for (int d = 1; d < K; ++d) {
-        const uint32_t c = (uint32_t)(inv >> (4 * d)) & 15u;
-        p[d * kCodeStride] = ((c & 1u) ? pl.x : ~pl.x) & ((c & 2u) ? pl.y : ~pl.y) &
-                             ((c & 4u) ? pl.z : ~pl.z) & ((c & 8u) ? pl.w : ~pl.w) &
-                             (c ? kFull : 0u);
-      }
     }
   }
 };
 
 __device__ __forceinline__ uint4 load4(const uint32_t *p) {
   return make_uint4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
+}
+
+// One column step over the window in row order (word m of the run = slot
+// (R + m) % W), the masks M already in row order.
+template <int W, int R, int... I>
+__device__ __forceinline__ void column_run(uint32_t (&V)[W], const uint32_t (&M)[W],
+                                           std::integer_sequence<int, I...>) {
+  lcs_run<W>(V[(R + I) % W]..., M[I]...);
 }
 
 // 32 column steps of one column block with the window rotated by R.
@@ -97,16 +99,10 @@ __device__ __forceinline__ void lds_columns(uint32_t (&V)[W], const uint32_t *ta
       asm("mul.hi.u32 %0, %1, 16;" : "=r"(code) : "r"(x));
       asm("mul.lo.u32 %0, %0, 16;" : "+r"(x));
       const uint32_t *row = tab + code * LdsTable<W>::kCodeStride;
-      uint32_t a[W], t[W], s[W];
+      uint32_t M[W];
 #pragma unroll
-      for (int m = 0; m < W; ++m) {
-        const int slot = (R + m) % W;
-        a[m] = V[slot];
-        t[m] = a[m] & row[slot * 32];
-      }
-      add_words<W, false>(s, a, t, 0);
-#pragma unroll
-      for (int m = 0; m < W; ++m) V[(R + m) % W] = s[m] | (a[m] ^ t[m]);
+      for (int m = 0; m < W; ++m) M[m] = row[((R + m) % W) * 32];
+      column_run<W, R>(V, M, std::make_integer_sequence<int, W>{});
     }
   }
 }

@@ -492,4 +492,542 @@ __device__ __forceinline__ void add_run(uint32_t *s, const uint32_t *a, const ui
 #undef NGIA_RUN
 }
 
+
+// ---- one LCS column step over a run of words ---------------------------------
+// lcs_run<N>(v..., m...): for the N words of a row vector, low word first,
+//   t = v & m;  s = v + t + carry;  v = s | (v ^ t)
+// with the carry rippling through the flag across the run (lop3 and and.b32
+// leave it alone).  Each word is read and written in place, so only the words
+// and their masks are live (no separate sum array).  Written out for each N.
+__device__ __forceinline__ void lcs_run1(uint32_t &v0, uint32_t m0) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %1;\n\t"
+      "add.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0)
+      : "r"(m0));
+}
+__device__ __forceinline__ void lcs_run2(uint32_t &v0, uint32_t &v1, uint32_t m0, uint32_t m1) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %2;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %3;\n\t"
+      "addc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1)
+      : "r"(m0), "r"(m1));
+}
+__device__ __forceinline__ void lcs_run3(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t m0, uint32_t m1, uint32_t m2) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %3;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %4;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %5;\n\t"
+      "addc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2)
+      : "r"(m0), "r"(m1), "r"(m2));
+}
+__device__ __forceinline__ void lcs_run4(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %4;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %5;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %6;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %7;\n\t"
+      "addc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3));
+}
+__device__ __forceinline__ void lcs_run5(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %5;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %6;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %7;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %8;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %9;\n\t"
+      "addc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4));
+}
+__device__ __forceinline__ void lcs_run6(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %6;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %7;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %8;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %9;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %10;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %11;\n\t"
+      "addc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5));
+}
+__device__ __forceinline__ void lcs_run7(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %7;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %8;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %9;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %10;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %11;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %12;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %13;\n\t"
+      "addc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6));
+}
+__device__ __forceinline__ void lcs_run8(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %8;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %9;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %10;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %11;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %12;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %13;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %14;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %15;\n\t"
+      "addc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7));
+}
+__device__ __forceinline__ void lcs_run9(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t &v8, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7, uint32_t m8) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %9;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %10;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %11;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %12;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %13;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %14;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %15;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %16;\n\t"
+      "addc.cc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "and.b32 t, %8, %17;\n\t"
+      "addc.u32 s, %8, t;\n\t"
+      "lop3.b32 %8, s, %8, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7), "+r"(v8)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7), "r"(m8));
+}
+__device__ __forceinline__ void lcs_run10(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t &v8, uint32_t &v9, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7, uint32_t m8, uint32_t m9) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %10;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %11;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %12;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %13;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %14;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %15;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %16;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %17;\n\t"
+      "addc.cc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "and.b32 t, %8, %18;\n\t"
+      "addc.cc.u32 s, %8, t;\n\t"
+      "lop3.b32 %8, s, %8, t, 0xF6;\n\t"
+      "and.b32 t, %9, %19;\n\t"
+      "addc.u32 s, %9, t;\n\t"
+      "lop3.b32 %9, s, %9, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7), "+r"(v8), "+r"(v9)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7), "r"(m8), "r"(m9));
+}
+__device__ __forceinline__ void lcs_run11(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t &v8, uint32_t &v9, uint32_t &v10, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7, uint32_t m8, uint32_t m9, uint32_t m10) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %11;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %12;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %13;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %14;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %15;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %16;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %17;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %18;\n\t"
+      "addc.cc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "and.b32 t, %8, %19;\n\t"
+      "addc.cc.u32 s, %8, t;\n\t"
+      "lop3.b32 %8, s, %8, t, 0xF6;\n\t"
+      "and.b32 t, %9, %20;\n\t"
+      "addc.cc.u32 s, %9, t;\n\t"
+      "lop3.b32 %9, s, %9, t, 0xF6;\n\t"
+      "and.b32 t, %10, %21;\n\t"
+      "addc.u32 s, %10, t;\n\t"
+      "lop3.b32 %10, s, %10, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7), "+r"(v8), "+r"(v9), "+r"(v10)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7), "r"(m8), "r"(m9), "r"(m10));
+}
+__device__ __forceinline__ void lcs_run12(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t &v8, uint32_t &v9, uint32_t &v10, uint32_t &v11, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7, uint32_t m8, uint32_t m9, uint32_t m10, uint32_t m11) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %12;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %13;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %14;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %15;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %16;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %17;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %18;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %19;\n\t"
+      "addc.cc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "and.b32 t, %8, %20;\n\t"
+      "addc.cc.u32 s, %8, t;\n\t"
+      "lop3.b32 %8, s, %8, t, 0xF6;\n\t"
+      "and.b32 t, %9, %21;\n\t"
+      "addc.cc.u32 s, %9, t;\n\t"
+      "lop3.b32 %9, s, %9, t, 0xF6;\n\t"
+      "and.b32 t, %10, %22;\n\t"
+      "addc.cc.u32 s, %10, t;\n\t"
+      "lop3.b32 %10, s, %10, t, 0xF6;\n\t"
+      "and.b32 t, %11, %23;\n\t"
+      "addc.u32 s, %11, t;\n\t"
+      "lop3.b32 %11, s, %11, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7), "+r"(v8), "+r"(v9), "+r"(v10), "+r"(v11)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7), "r"(m8), "r"(m9), "r"(m10), "r"(m11));
+}
+__device__ __forceinline__ void lcs_run13(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t &v8, uint32_t &v9, uint32_t &v10, uint32_t &v11, uint32_t &v12, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7, uint32_t m8, uint32_t m9, uint32_t m10, uint32_t m11, uint32_t m12) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %13;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %14;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %15;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %16;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %17;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %18;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %19;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %20;\n\t"
+      "addc.cc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "and.b32 t, %8, %21;\n\t"
+      "addc.cc.u32 s, %8, t;\n\t"
+      "lop3.b32 %8, s, %8, t, 0xF6;\n\t"
+      "and.b32 t, %9, %22;\n\t"
+      "addc.cc.u32 s, %9, t;\n\t"
+      "lop3.b32 %9, s, %9, t, 0xF6;\n\t"
+      "and.b32 t, %10, %23;\n\t"
+      "addc.cc.u32 s, %10, t;\n\t"
+      "lop3.b32 %10, s, %10, t, 0xF6;\n\t"
+      "and.b32 t, %11, %24;\n\t"
+      "addc.cc.u32 s, %11, t;\n\t"
+      "lop3.b32 %11, s, %11, t, 0xF6;\n\t"
+      "and.b32 t, %12, %25;\n\t"
+      "addc.u32 s, %12, t;\n\t"
+      "lop3.b32 %12, s, %12, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7), "+r"(v8), "+r"(v9), "+r"(v10), "+r"(v11), "+r"(v12)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7), "r"(m8), "r"(m9), "r"(m10), "r"(m11), "r"(m12));
+}
+__device__ __forceinline__ void lcs_run14(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t &v8, uint32_t &v9, uint32_t &v10, uint32_t &v11, uint32_t &v12, uint32_t &v13, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7, uint32_t m8, uint32_t m9, uint32_t m10, uint32_t m11, uint32_t m12, uint32_t m13) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %14;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %15;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %16;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %17;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %18;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %19;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %20;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %21;\n\t"
+      "addc.cc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "and.b32 t, %8, %22;\n\t"
+      "addc.cc.u32 s, %8, t;\n\t"
+      "lop3.b32 %8, s, %8, t, 0xF6;\n\t"
+      "and.b32 t, %9, %23;\n\t"
+      "addc.cc.u32 s, %9, t;\n\t"
+      "lop3.b32 %9, s, %9, t, 0xF6;\n\t"
+      "and.b32 t, %10, %24;\n\t"
+      "addc.cc.u32 s, %10, t;\n\t"
+      "lop3.b32 %10, s, %10, t, 0xF6;\n\t"
+      "and.b32 t, %11, %25;\n\t"
+      "addc.cc.u32 s, %11, t;\n\t"
+      "lop3.b32 %11, s, %11, t, 0xF6;\n\t"
+      "and.b32 t, %12, %26;\n\t"
+      "addc.cc.u32 s, %12, t;\n\t"
+      "lop3.b32 %12, s, %12, t, 0xF6;\n\t"
+      "and.b32 t, %13, %27;\n\t"
+      "addc.u32 s, %13, t;\n\t"
+      "lop3.b32 %13, s, %13, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7), "+r"(v8), "+r"(v9), "+r"(v10), "+r"(v11), "+r"(v12), "+r"(v13)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7), "r"(m8), "r"(m9), "r"(m10), "r"(m11), "r"(m12), "r"(m13));
+}
+__device__ __forceinline__ void lcs_run15(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t &v8, uint32_t &v9, uint32_t &v10, uint32_t &v11, uint32_t &v12, uint32_t &v13, uint32_t &v14, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7, uint32_t m8, uint32_t m9, uint32_t m10, uint32_t m11, uint32_t m12, uint32_t m13, uint32_t m14) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %15;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %16;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %17;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %18;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %19;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %20;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %21;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %22;\n\t"
+      "addc.cc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "and.b32 t, %8, %23;\n\t"
+      "addc.cc.u32 s, %8, t;\n\t"
+      "lop3.b32 %8, s, %8, t, 0xF6;\n\t"
+      "and.b32 t, %9, %24;\n\t"
+      "addc.cc.u32 s, %9, t;\n\t"
+      "lop3.b32 %9, s, %9, t, 0xF6;\n\t"
+      "and.b32 t, %10, %25;\n\t"
+      "addc.cc.u32 s, %10, t;\n\t"
+      "lop3.b32 %10, s, %10, t, 0xF6;\n\t"
+      "and.b32 t, %11, %26;\n\t"
+      "addc.cc.u32 s, %11, t;\n\t"
+      "lop3.b32 %11, s, %11, t, 0xF6;\n\t"
+      "and.b32 t, %12, %27;\n\t"
+      "addc.cc.u32 s, %12, t;\n\t"
+      "lop3.b32 %12, s, %12, t, 0xF6;\n\t"
+      "and.b32 t, %13, %28;\n\t"
+      "addc.cc.u32 s, %13, t;\n\t"
+      "lop3.b32 %13, s, %13, t, 0xF6;\n\t"
+      "and.b32 t, %14, %29;\n\t"
+      "addc.u32 s, %14, t;\n\t"
+      "lop3.b32 %14, s, %14, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7), "+r"(v8), "+r"(v9), "+r"(v10), "+r"(v11), "+r"(v12), "+r"(v13), "+r"(v14)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7), "r"(m8), "r"(m9), "r"(m10), "r"(m11), "r"(m12), "r"(m13), "r"(m14));
+}
+__device__ __forceinline__ void lcs_run16(uint32_t &v0, uint32_t &v1, uint32_t &v2, uint32_t &v3, uint32_t &v4, uint32_t &v5, uint32_t &v6, uint32_t &v7, uint32_t &v8, uint32_t &v9, uint32_t &v10, uint32_t &v11, uint32_t &v12, uint32_t &v13, uint32_t &v14, uint32_t &v15, uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3, uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7, uint32_t m8, uint32_t m9, uint32_t m10, uint32_t m11, uint32_t m12, uint32_t m13, uint32_t m14, uint32_t m15) {
+  asm(
+      "{\n\t.reg .u32 t, s;\n\t"
+      "and.b32 t, %0, %16;\n\t"
+      "add.cc.u32 s, %0, t;\n\t"
+      "lop3.b32 %0, s, %0, t, 0xF6;\n\t"
+      "and.b32 t, %1, %17;\n\t"
+      "addc.cc.u32 s, %1, t;\n\t"
+      "lop3.b32 %1, s, %1, t, 0xF6;\n\t"
+      "and.b32 t, %2, %18;\n\t"
+      "addc.cc.u32 s, %2, t;\n\t"
+      "lop3.b32 %2, s, %2, t, 0xF6;\n\t"
+      "and.b32 t, %3, %19;\n\t"
+      "addc.cc.u32 s, %3, t;\n\t"
+      "lop3.b32 %3, s, %3, t, 0xF6;\n\t"
+      "and.b32 t, %4, %20;\n\t"
+      "addc.cc.u32 s, %4, t;\n\t"
+      "lop3.b32 %4, s, %4, t, 0xF6;\n\t"
+      "and.b32 t, %5, %21;\n\t"
+      "addc.cc.u32 s, %5, t;\n\t"
+      "lop3.b32 %5, s, %5, t, 0xF6;\n\t"
+      "and.b32 t, %6, %22;\n\t"
+      "addc.cc.u32 s, %6, t;\n\t"
+      "lop3.b32 %6, s, %6, t, 0xF6;\n\t"
+      "and.b32 t, %7, %23;\n\t"
+      "addc.cc.u32 s, %7, t;\n\t"
+      "lop3.b32 %7, s, %7, t, 0xF6;\n\t"
+      "and.b32 t, %8, %24;\n\t"
+      "addc.cc.u32 s, %8, t;\n\t"
+      "lop3.b32 %8, s, %8, t, 0xF6;\n\t"
+      "and.b32 t, %9, %25;\n\t"
+      "addc.cc.u32 s, %9, t;\n\t"
+      "lop3.b32 %9, s, %9, t, 0xF6;\n\t"
+      "and.b32 t, %10, %26;\n\t"
+      "addc.cc.u32 s, %10, t;\n\t"
+      "lop3.b32 %10, s, %10, t, 0xF6;\n\t"
+      "and.b32 t, %11, %27;\n\t"
+      "addc.cc.u32 s, %11, t;\n\t"
+      "lop3.b32 %11, s, %11, t, 0xF6;\n\t"
+      "and.b32 t, %12, %28;\n\t"
+      "addc.cc.u32 s, %12, t;\n\t"
+      "lop3.b32 %12, s, %12, t, 0xF6;\n\t"
+      "and.b32 t, %13, %29;\n\t"
+      "addc.cc.u32 s, %13, t;\n\t"
+      "lop3.b32 %13, s, %13, t, 0xF6;\n\t"
+      "and.b32 t, %14, %30;\n\t"
+      "addc.cc.u32 s, %14, t;\n\t"
+      "lop3.b32 %14, s, %14, t, 0xF6;\n\t"
+      "and.b32 t, %15, %31;\n\t"
+      "addc.u32 s, %15, t;\n\t"
+      "lop3.b32 %15, s, %15, t, 0xF6;\n\t"
+      "}"
+      : "+r"(v0), "+r"(v1), "+r"(v2), "+r"(v3), "+r"(v4), "+r"(v5), "+r"(v6), "+r"(v7), "+r"(v8), "+r"(v9), "+r"(v10), "+r"(v11), "+r"(v12), "+r"(v13), "+r"(v14), "+r"(v15)
+      : "r"(m0), "r"(m1), "r"(m2), "r"(m3), "r"(m4), "r"(m5), "r"(m6), "r"(m7), "r"(m8), "r"(m9), "r"(m10), "r"(m11), "r"(m12), "r"(m13), "r"(m14), "r"(m15));
+}
+template <int N, typename... A>
+__device__ __forceinline__ void lcs_run(A &&...a) {
+  static_assert(N >= 1 && N <= 16 && sizeof...(A) == 2 * N, "run length");
+#define NGIA_LCS(K) \
+  if constexpr (N == K) lcs_run##K(a...);
+  NGIA_LCS(1) NGIA_LCS(2) NGIA_LCS(3) NGIA_LCS(4) NGIA_LCS(5) NGIA_LCS(6) NGIA_LCS(7)
+  NGIA_LCS(8) NGIA_LCS(9) NGIA_LCS(10) NGIA_LCS(11) NGIA_LCS(12) NGIA_LCS(13) NGIA_LCS(14)
+  NGIA_LCS(15) NGIA_LCS(16)
+#undef NGIA_LCS
+}
+
 }  // namespace ngia

@@ -154,7 +154,7 @@ struct Server {
   uint64_t db_words = 0;
   Alphabet ab{16, 0};
   uint64_t recode_map = 0;    // nonzero: aligner codes are recoded (dense)
-  DevBuf packed, nib, dense, offs, lens, keys, vals, cluster;
+  DevBuf packed, nib, dense, dplanes, offs, lens, keys, vals, cluster;
   std::vector<std::unique_ptr<Slot>> slots;
   std::mutex mu;
   std::condition_variable cv;
@@ -206,8 +206,8 @@ static int run_request(Server *s, Slot *sl, Request *r) {
   NGIA_TRY(launch_nibbles(packed, offs, q, s->nib.as<uint32_t>(), sl->presence.as<uint32_t>(),
                           st));
   if (s->recode_map)
-    NGIA_TRY(launch_recode(s->nib.as<uint32_t>(), offs, q, s->recode_map,
-                           s->dense.as<uint32_t>(), st));
+    NGIA_TRY(launch_dense_layouts(packed, offs, q, s->recode_map, s->dense.as<uint32_t>(),
+                                  s->dplanes.as<uint32_t>(), st));
   NGIA_TRY(launch_sketch_nibbles(s->nib.as<uint32_t>(), offs, q, sl->sigs.as<uint32_t>(), st));
   const uint32_t slots = q * (uint32_t)kBands;
   lookup_kernel<<<ceil_div(slots, 256u), 256, 0, st>>>(s->keys.as<uint32_t>(),
@@ -288,7 +288,7 @@ static void dispatch_loop(Server *s) {
 }
 
 static size_t request_bytes(uint64_t words, uint32_t q, bool dense) {
-  return (size_t)words * 4 * (dense ? 3 : 2) + (size_t)q * (12 + 4 * kBands + 4) +
+  return (size_t)words * 4 * (dense ? 4 : 2) + (size_t)q * (12 + 4 * kBands + 4) +
          (size_t)q * kBands * (4 + 8 + 4 + 12);
 }
 
@@ -339,16 +339,23 @@ static int server_init(ngia_server *s, ngia_ctx *db, const uint32_t *h_cluster,
   cudaStream_t st = db->stream;
   NGIA_TRY(s->packed.reserve(total_words * 4));
   NGIA_TRY(s->nib.reserve(total_words * 4));
-  if (s->recode_map) NGIA_TRY(s->dense.reserve(total_words * 4));
+  if (s->recode_map) {
+    NGIA_TRY(s->dense.reserve(total_words * 4));
+    NGIA_TRY(s->dplanes.reserve(total_words * 4));
+    s->ab.dplanes = s->dplanes.as<uint32_t>();
+  }
   NGIA_TRY(s->offs.reserve(total_recs * 8));
   NGIA_TRY(s->lens.reserve(total_recs * 4));
   NGIA_CUDA(cudaMemcpyAsync(s->packed.p, db->packed.p, db->packed_words * 4,
                             cudaMemcpyDeviceToDevice, st));
   NGIA_CUDA(cudaMemcpyAsync(s->nib.p, db->nib.p, db->packed_words * 4, cudaMemcpyDeviceToDevice,
                             st));
-  if (s->recode_map)
+  if (s->recode_map) {
     NGIA_CUDA(cudaMemcpyAsync(s->dense.p, db->nib_dense.p, db->packed_words * 4,
                               cudaMemcpyDeviceToDevice, st));
+    NGIA_CUDA(cudaMemcpyAsync(s->dplanes.p, db->dplanes.p, db->packed_words * 4,
+                              cudaMemcpyDeviceToDevice, st));
+  }
   NGIA_CUDA(cudaMemcpyAsync(s->offs.p, db->offs.p, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
   NGIA_CUDA(cudaMemcpyAsync(s->lens.p, db->lens.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
   // per band, the database's (signature, index) sorted by signature then index
@@ -485,7 +492,7 @@ void ngia_server_destroy(ngia_server *s) {
                             &sl->presence, &sl->jobs,   &sl->where, &sl->count};
     for (ngia::DevBuf *b : bufs) b->release();
   }
-  ngia::DevBuf *bufs[] = {&s->packed, &s->nib, &s->dense, &s->offs, &s->lens,
+  ngia::DevBuf *bufs[] = {&s->packed, &s->nib, &s->dense, &s->dplanes, &s->offs, &s->lens,
                           &s->keys,   &s->vals, &s->cluster};
   for (ngia::DevBuf *b : bufs) b->release();
   delete s;

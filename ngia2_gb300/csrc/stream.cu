@@ -180,7 +180,7 @@ __global__ void accumulate_kernel(const Counters *__restrict__ rc,
 }
 
 struct StreamState {
-  DevBuf region_packed, region_nib, region_dense, r_offs, r_lens;
+  DevBuf region_packed, region_nib, region_dense, region_dplanes, r_offs, r_lens;
   DevBuf offs, lens, sigs, sig_tmp, rep, scratch, ucount, uoff, counters, pairs, scores,
       keys, keys_sorted, order, block_pairs, block_scores, chunk_first, presence, emit_tmp,
       edges;
@@ -188,7 +188,8 @@ struct StreamState {
   Stager stager;
   cudaStream_t s = nullptr;
   void destroy() {
-    DevBuf *bufs[] = {&region_packed, &region_nib, &region_dense, &r_offs,  &r_lens,
+    DevBuf *bufs[] = {&region_packed, &region_nib, &region_dense, &region_dplanes, &r_offs,
+                      &r_lens,
                       &offs,          &lens,       &sigs,         &sig_tmp, &rep,
                       &scratch,       &ucount,     &uoff,         &counters, &pairs,
                       &scores,        &keys,       &keys_sorted,  &order,   &block_pairs,
@@ -208,8 +209,9 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
                         ngia_stream_stats *st) {
   const auto t_all = SClock::now();
   // ---- chunks: contiguous runs of records of at most chunk_words words
-  // (three chunk slots of planes, nibble codes and recoded codes in the budget)
-  const uint64_t chunk_words = chunk_bytes / (3ull * 4 * 3);
+  // (three chunk slots of planes, nibble codes, recoded codes and code planes in
+  // the budget)
+  const uint64_t chunk_words = chunk_bytes / (3ull * 4 * 4);
   std::vector<Chunk> chunks;
   for (uint32_t i = 0; i < n; ++i) {
     const uint64_t w = 1 + 4ull * ((h_lens[i] + 31) / 32);
@@ -275,7 +277,8 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
     NGIA_LAUNCHED();
     NGIA_TRY(launch_nibbles(rp, roffs + at, c.count, rn, presence, s));
     if (dense)
-      NGIA_TRY(launch_recode(rn, roffs + at, c.count, map, S.region_dense.as<uint32_t>(), s));
+      NGIA_TRY(launch_dense_layouts(rp, roffs + at, c.count, map, S.region_dense.as<uint32_t>(),
+                                    S.region_dplanes.as<uint32_t>(), s));
     return NGIA_OK;
   };
 
@@ -368,8 +371,9 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
       ++next;
     }
     dense = true;
-    ab = Alphabet{8, inv};
     NGIA_TRY(S.region_dense.reserve(3 * chunk_words * 4));
+    NGIA_TRY(S.region_dplanes.reserve(3 * chunk_words * 4));
+    ab = Alphabet{8, inv, S.region_dplanes.as<uint32_t>()};
   }
   uint32_t max_block = 0;
   for (size_t b = 0; b < (size_t)C * C; ++b) {
