@@ -365,10 +365,10 @@ static int launch_stream_k(const RoundArgs &a, int cls, unsigned int *cursor,
   constexpr size_t smem = stream_smem_bytes(W, K);
   uint32_t grid = 0;
   NGIA_TRY(persistent_grid(align_stream_kernel<W, K>, kStreamThreads, smem, kFull, &grid));
-  // K = 8 tables fill from the code planes (records with the same offsets)
-  if (K == 8 && !a.dplanes) return NGIA_ERR_STATE;
+  // K < 16 tables fill from the code planes (records with the same offsets)
+  if (K < 16 && !a.dplanes) return NGIA_ERR_STATE;
   align_stream_kernel<W, K><<<grid, kStreamThreads, smem, s>>>(
-      K == 8 ? a.dplanes : a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls,
+      K < 16 ? a.dplanes : a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls,
       cursor, a.scores, a.t, a.fm, a.work);
   NGIA_LAUNCHED();
   return NGIA_OK;
@@ -390,14 +390,15 @@ static int launch_group_k(const RoundArgs &a, int cls, unsigned int *cursor, cud
 template <int W>
 static int launch_stream(const RoundArgs &a, int K, int cls, unsigned int *cursor,
                          cudaStream_t s) {
-  return K == 8 ? launch_stream_k<W, 8>(a, cls, cursor, s)
-                : launch_stream_k<W, 16>(a, cls, cursor, s);
+  return K == 5   ? launch_stream_k<W, 5>(a, cls, cursor, s)
+         : K == 8 ? launch_stream_k<W, 8>(a, cls, cursor, s)
+                  : launch_stream_k<W, 16>(a, cls, cursor, s);
 }
 
 template <int G, int K>
 static int launch_group(const RoundArgs &a, int KC, int cls, unsigned int *cursor,
                         cudaStream_t s) {
-  return KC == 8 ? launch_group_k<G, K, 8>(a, cls, cursor, s)
+  return KC <= 8 ? launch_group_k<G, K, 8>(a, cls, cursor, s)
                  : launch_group_k<G, K, 16>(a, cls, cursor, s);
 }
 

@@ -38,9 +38,10 @@ namespace ngia {
 
 constexpr int kLdsUnroll = NGIA_LDS_UNROLL;
 
-// K = entries per row block: 16 (all residue codes) or 8 when the database
-// uses at most 7 nonzero codes and the targets were recoded densely (the
-// table, and so the shared memory per thread, halves; nucleotides).
+// K = entries per row block: 16 (all residue codes), or 8 / 5 when the
+// database uses at most 7 / 4 nonzero codes and the records were recoded
+// densely (the table, and so the shared memory per thread, shrinks to a half /
+// under a third; nucleotides take 5).
 template <int W, int K = 16>
 struct LdsTable {
   uint32_t *base;  // this thread's column of the warp's table
@@ -61,7 +62,7 @@ struct LdsTable {
       const uint32_t hi[4] = {~pl.z & ~pl.w, pl.z & ~pl.w, ~pl.z & pl.w, pl.z & pl.w};
 #pragma unroll
       for (int c = 1; c < 16; ++c) p[c * kCodeStride] = lo[c & 3] & hi[c >> 2];
-    } else {  // K = 8: the code planes (aligner code bits in planes 0-2)
+    } else {  // K = 5 or 8: the code planes (aligner code bits in planes 0-2)
 #pragma unroll
       for (int d = 1; d < K; ++d)
         p[d * kCodeStride] = ((d & 1) ? pl.x : ~pl.x) & ((d & 2) ? pl.y : ~pl.y) &

@@ -225,7 +225,7 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
     NGIA_TRY(launch_dense_layouts(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), n, map,
                                   c->nib_dense.as<uint32_t>(), c->dplanes.as<uint32_t>(), s));
     c->align_nib = c->nib_dense.as<uint32_t>();
-    c->ab = Alphabet{8, inv, c->dplanes.as<uint32_t>()};
+    c->ab = Alphabet{next <= 5 ? 5 : 8, inv, c->dplanes.as<uint32_t>()};
     c->recode_map = map;
   }
   c->n = n;

@@ -49,11 +49,11 @@ int launch_align_jobs_dev_count(const uint32_t *packed, const uint64_t *offs,
 // inv packs, per code d < K, the residue code whose match mask d stands for
 // (identity when the codes were not recoded).
 struct Alphabet {
-  int K;         // 8 or 16 table entries per row block
+  int K;         // 5, 8 or 16 table entries per row block (aligner codes 0..K-1)
   uint64_t inv;  // nibble d = residue code of aligner code d
-  // K = 8 only, optional: the records with their bit planes holding the
-  // aligner codes (planes 0-2; same layout and offsets as the packed records),
-  // from which a row block's eight table entries are one logic op each
+  // K < 16: the records with their bit planes holding the aligner codes
+  // (planes 0-2; same layout and offsets as the packed records), from which a
+  // row block's table entries are one logic op each
   const uint32_t *dplanes = nullptr;
 };
 // One width class of the batched aligner: a persistent launch over

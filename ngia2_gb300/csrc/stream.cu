@@ -373,7 +373,7 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
     dense = true;
     NGIA_TRY(S.region_dense.reserve(3 * chunk_words * 4));
     NGIA_TRY(S.region_dplanes.reserve(3 * chunk_words * 4));
-    ab = Alphabet{8, inv, S.region_dplanes.as<uint32_t>()};
+    ab = Alphabet{next <= 5 ? 5 : 8, inv, S.region_dplanes.as<uint32_t>()};
   }
   uint32_t max_block = 0;
   for (size_t b = 0; b < (size_t)C * C; ++b) {
