@@ -53,7 +53,7 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
   if (c->use_table && c->table_ok)
     NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
                                  c->offs.as<uint64_t>(), c->n, c->ab.inv, c->sketch_table.p,
-                                 c->sigs.as<uint32_t>(), s));
+                                 c->sigs.as<uint32_t>(), s, c->side, c->ev[6], c->ev[7]));
   else
     NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
                                    c->sigs.as<uint32_t>(), s));
@@ -285,6 +285,7 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
     c->own_stream = (e == cudaSuccess);
   }
   for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     ngia_ctx_destroy(c);
     return ngia::cuda_fail(e);
@@ -310,6 +311,7 @@ void ngia_ctx_destroy(ngia_ctx *c) {
   c->round.destroy();  // shares c->stream, which it leaves alone
   for (int k = 0; k < 8; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

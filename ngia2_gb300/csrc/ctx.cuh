@@ -7,7 +7,8 @@
 struct ngia_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  cudaEvent_t ev[8] = {};
+  cudaEvent_t ev[8] = {};  // 0-3 stage timing, 6-7 fork/join of `side`
+  cudaStream_t side = nullptr;  // work that runs beside the main stream's (sketch)
   // resident database
   uint32_t n = 0;
   uint64_t packed_words = 0;

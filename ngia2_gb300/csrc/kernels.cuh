@@ -19,9 +19,12 @@ int launch_sketch_nibbles(const uint32_t *nib, const uint64_t *offs, uint32_t n,
 constexpr uint32_t kSketchTableEntries = 1u << 16;
 size_t sketch_table_bytes();
 int build_sketch_table(uint64_t inv, void *table, cudaStream_t s);
+// The short records' kernel runs on `side` (forked from and joined back into
+// s through the two events) beside the rank walk on s.
 int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
                         uint32_t n, uint64_t inv, const void *table, uint32_t *sigs,
-                        cudaStream_t s);
+                        cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
+                        cudaEvent_t join);
 
 // sort.cu
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs);

@@ -437,21 +437,29 @@ static int rank_blocks_per_sm() {
 
 int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
                         uint32_t n, uint64_t inv, const void *table, uint32_t *sigs,
-                        cudaStream_t s) {
+                        cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
+                        cudaEvent_t join) {
   if (n == 0) return NGIA_OK;
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint8_t *base = static_cast<const uint8_t *>(table);
+  // The rank walk's residency is bound by its bit sets (shared memory), which
+  // leaves each SM room in threads and registers for one block of the short
+  // records' kernel (no shared memory): one block per SM, beside it.
+  NGIA_CUDA(cudaEventRecord(fork, s));
+  NGIA_CUDA(cudaStreamWaitEvent(side, fork, 0));
+  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms;
+  sketch_table_kernel<<<want < cap ? want : cap, 256, 0, side>>>(
+      nib, dense, offs, n, reinterpret_cast<const uint4 *>(base), sigs);
+  NGIA_LAUNCHED();
   const uint32_t rank_want = ceil_div(n, kRankWarps);
   const uint32_t rank_cap = (uint32_t)(sms * rank_blocks_per_sm());
   sketch_rank_kernel<<<rank_want < rank_cap ? rank_want : rank_cap, kRankWarps * 32, 0, s>>>(
       dense, offs, n, inv, reinterpret_cast<const uint16_t *>(base + kRowTableBytes), sigs);
   NGIA_LAUNCHED();
-  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
-  sketch_table_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
-      nib, dense, offs, n, reinterpret_cast<const uint4 *>(base), sigs);
-  NGIA_LAUNCHED();
+  NGIA_CUDA(cudaEventRecord(join, side));
+  NGIA_CUDA(cudaStreamWaitEvent(s, join, 0));
   return NGIA_OK;
 }
 
