@@ -401,11 +401,12 @@ def run_ours(args, world, rank, local, pg):
     e2e_step = lambda: ctx.run_host(h_packed, h_offs, h_lens, IDENTITY, BANDS, h_edges)  # noqa
     for _ in range(max(1, args.warmup)):
         e2e_step()
-    e2e_ms = []
+    e2e_ms, e2e_st = [], []
     m_e2e = 0
     for _ in range(args.steps):
-        t, (m_e2e, _) = timed(e2e_step)
+        t, (m_e2e, st_e2e) = timed(e2e_step)
         e2e_ms.append(t)
+        e2e_st.append(st_e2e)
     e2e_mean = max_over_ranks(pg, sum(e2e_ms) / len(e2e_ms))
     h2d = h_packed.nbytes + h_offs.nbytes + h_lens.nbytes
     d2h = m_e2e * ng.EDGE_DTYPE.itemsize + 8
@@ -483,7 +484,13 @@ def run_ours(args, world, rank, local, pg):
         "roofline": dict(rs[dominant], name=dominant),
         "rooflines": rs,
         "e2e": {"value": world * n / (e2e_mean * 1e-3), "unit": "seqs/s",
-                "ms_per_step": e2e_mean, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "ms_per_step": e2e_mean, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                # device stages of the host-buffer path (ms_sketch spans the
+                # pipelined upload when load_pipelined)
+                "stages_ms": {k: statistics.mean(s[k] for s in e2e_st)
+                              for k in ("ms_sketch", "ms_bucket", "ms_pairs", "ms_align",
+                                        "ms_emit")},
+                "load_pipelined": int(min(s["load_pipelined"] for s in e2e_st))},
         "gpu_launches": launches // max(1, args.steps) * args.steps,
         "clocks": clk.summary(),
         "hbm_peak_gbs": peaks().get("hbm_gbs"),

@@ -147,6 +147,8 @@ typedef struct ngia_stats {
                                little wider than the band) times the column
                                blocks processed before a pair's score was
                                settled (see the early exit in common.cuh) */
+  uint32_t load_pipelined;  /* ngia_ctx_run_host: 1 when the upload overlapped
+                               the sketch (ms_sketch then spans both) */
 } ngia_stats;
 
 int ngia_ctx_create(ngia_ctx **ctx, void *stream);

@@ -49,7 +49,7 @@ class Stats(C.Structure):
                 ("aligned_cells", C.c_uint64), ("edges", C.c_uint64),
                 ("ms_sketch", C.c_double), ("ms_bucket", C.c_double),
                 ("ms_pairs", C.c_double), ("ms_align", C.c_double), ("ms_emit", C.c_double),
-                ("computed_cells", C.c_uint64)]
+                ("computed_cells", C.c_uint64), ("load_pipelined", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -265,13 +265,13 @@ dense_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__rest
 }
 
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
-                   uint32_t *presence, cudaStream_t s) {
+                   uint32_t *presence, cudaStream_t s, bool accumulate) {
   if (n == 0) return NGIA_OK;
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
-  NGIA_CUDA(cudaMemsetAsync(presence, 0, sizeof(uint32_t), s));
+  if (!accumulate) NGIA_CUDA(cudaMemsetAsync(presence, 0, sizeof(uint32_t), s));
   nibble_kernel<<<want < cap ? want : cap, 256, 0, s>>>(packed, offs, n, nib, presence);
   NGIA_LAUNCHED();
   return NGIA_OK;
@@ -289,17 +289,104 @@ int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_
   return NGIA_OK;
 }
 
-int launch_dense_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n,
-                         uint64_t map, uint32_t *dense_nib, uint32_t *dplanes,
-                         cudaStream_t s) {
-  if (n == 0) return NGIA_OK;
-  uint32_t bits[3] = {0u, 0u, 0u};
+// Every layout of a run of records in one pass over their planes, for loads
+// whose code map is known ahead (the pipelined load): nibbles, the codes
+// present (presence[0]), recoded nibbles and code planes, and presence[1] = 1
+// if a record is not inside words [w0, w1) (then it is left alone).
+__global__ void __launch_bounds__(256)
+load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
+                    uint32_t n, uint64_t w0, uint64_t w1, uint32_t bit0, uint32_t bit1,
+                    uint32_t bit2, uint32_t *__restrict__ nib, uint32_t *__restrict__ dense_nib,
+                    uint32_t *__restrict__ dplanes, uint32_t *__restrict__ presence) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  uint32_t mine = 0;
+  bool bad = false;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const uint64_t o = offs[i];
+    if (o < w0 || o >= w1) {
+      bad = true;
+      continue;
+    }
+    const uint32_t len = __ldg(packed + o);
+    const uint32_t blocks = (len + 31) >> 5;
+    if (o + 1 + 4ull * blocks > w1) {
+      bad = true;
+      continue;
+    }
+    if (lane == 0) {
+      nib[o] = len;
+      dense_nib[o] = len;
+      dplanes[o] = len;
+    }
+    for (uint32_t k = lane; k < blocks; k += 32) {
+      const uint64_t b = o + 1 + 4ull * k;
+      const uint32_t pl[4] = {__ldg(packed + b), __ldg(packed + b + 1), __ldg(packed + b + 2),
+                              __ldg(packed + b + 3)};
+      uint32_t w[4];
+      planes_to_nibbles(pl, 4, w);
+      const uint32_t left = len - 32 * k;
+      const uint32_t real = left >= 32 ? kFull : (1u << left) - 1u;
+      uint32_t d[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (uint32_t c = 0; c < 16; ++c) {
+        const uint32_t m = code_mask(pl, c);
+        if (m & real) mine |= 1u << c;
+        d[0] |= (bit0 >> c) & 1u ? m : 0u;
+        d[1] |= (bit1 >> c) & 1u ? m : 0u;
+        d[2] |= (bit2 >> c) & 1u ? m : 0u;
+      }
+      uint32_t dn[4];
+      planes_to_nibbles(d, 3, dn);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        nib[b + q] = w[q];
+        dense_nib[b + q] = dn[q];
+        dplanes[b + q] = d[q];
+      }
+    }
+  }
+  mine = __reduce_or_sync(kFull, mine);
+  const uint32_t any_bad = __ballot_sync(kFull, bad);
+  if (lane == 0) {
+    if (mine) atomicOr(presence, mine);
+    if (any_bad) atomicOr(presence + 1, 1u);
+  }
+}
+
+static int map_bits(uint64_t map, uint32_t (&bits)[3]) {
+  bits[0] = bits[1] = bits[2] = 0u;
   for (uint32_t c = 1; c < 16; ++c) {
     const uint32_t d = (uint32_t)(map >> (4 * c)) & 15u;
     if (d > 7) return NGIA_ERR_ARG;  // three planes hold aligner codes 0..7
     for (int b = 0; b < 3; ++b)
       if ((d >> b) & 1u) bits[b] |= 1u << c;
   }
+  return NGIA_OK;
+}
+
+int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint64_t w0,
+                        uint64_t w1, uint64_t map, uint32_t *nib, uint32_t *dense_nib,
+                        uint32_t *dplanes, uint32_t *presence, cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  uint32_t bits[3];
+  NGIA_TRY(map_bits(map, bits));
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
+  load_layouts_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
+      packed, offs, n, w0, w1, bits[0], bits[1], bits[2], nib, dense_nib, dplanes, presence);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+int launch_dense_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n,
+                         uint64_t map, uint32_t *dense_nib, uint32_t *dplanes,
+                         cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  uint32_t bits[3];
+  NGIA_TRY(map_bits(map, bits));
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

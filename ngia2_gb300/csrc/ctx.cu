@@ -1,5 +1,6 @@
 // ctx.cu -- the resident-database context (ngia_ctx), the batched graph build
 // and fast-mode driver, status handling, and the edge sort+unique entry point.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -35,7 +36,7 @@ DbView db_view(const ngia_ctx *c) {
                 c->lens.as<uint32_t>()};
 }
 
-int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
+int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_done) {
   if (c->n == 0) return NGIA_ERR_STATE;
   if (bands < 1 || bands > (uint32_t)kBands) return NGIA_ERR_ARG;
   cudaStream_t s = c->stream;
@@ -43,21 +44,25 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st) {
   NGIA_TRY(c->rep.reserve((size_t)kBands * c->n * 4));
   NGIA_TRY(c->sort_tmp.reserve(bucket_scratch_bytes(c->n, bands)));
   // the tables depend only on the aligner-code map: built once per map
-  if (c->use_table && c->table_ok && !(c->table_built && c->table_inv == c->ab.inv)) {
+  if (!sketch_done && c->use_table && c->table_ok &&
+      !(c->table_built && c->table_inv == c->ab.inv)) {
     NGIA_TRY(c->sketch_table.reserve(sketch_table_bytes()));
     NGIA_TRY(build_sketch_table(c->ab.inv, c->sketch_table.p, s));
     c->table_built = true;
     c->table_inv = c->ab.inv;
   }
-  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
-  if (c->use_table && c->table_ok)
-    NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
-                                 c->offs.as<uint64_t>(), c->n, c->ab.inv, c->sketch_table.p,
-                                 c->sigs.as<uint32_t>(), s, c->side, c->ev[6], c->ev[7]));
-  else
-    NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
-                                   c->sigs.as<uint32_t>(), s));
-  NGIA_CUDA(cudaEventRecord(c->ev[1], s));
+  if (!sketch_done) {  // (else ev[0], ev[1] bracket the pipelined load and sketch)
+    NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+    if (c->use_table && c->table_ok)
+      NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
+                                   c->offs.as<uint64_t>(), c->n, c->ab.inv, c->sketch_table.p,
+                                   c->sigs.as<uint32_t>(), c->n, s, c->side, c->ev[6],
+                                   c->ev[7]));
+    else
+      NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
+                                     c->sigs.as<uint32_t>(), s));
+    NGIA_CUDA(cudaEventRecord(c->ev[1], s));
+  }
   NGIA_TRY(bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(),
                   c->sort_tmp.p, s));
   NGIA_CUDA(cudaEventRecord(c->ev[2], s));
@@ -186,6 +191,56 @@ int ctx_fast_cluster(ngia_ctx *c, uint32_t identity, uint32_t bands, uint32_t *h
   return NGIA_OK;
 }
 
+// Dense recoding of the residue codes in use (code 0 stays 0): equality of
+// codes, all the aligner looks at, is unchanged by a bijection.
+struct AlphaChoice {
+  bool dense = false;
+  uint64_t map = 0, inv = 0;
+  int K = 16;
+  bool table_ok = false;
+  bool operator==(const AlphaChoice &o) const {
+    return dense == o.dense && map == o.map && inv == o.inv && K == o.K && table_ok == o.table_ok;
+  }
+};
+
+static AlphaChoice choose_alphabet(uint32_t present) {
+  AlphaChoice a;
+  a.table_ok = (present & 1u) == 0 && present != 0 && __builtin_popcount(present) <= 4;
+  if (__builtin_popcount(present & ~1u) <= 7) {
+    int next = 1;
+    for (int code = 1; code < 16; ++code) {
+      if (!((present >> code) & 1u)) continue;
+      a.map |= (uint64_t)next << (4 * code);
+      a.inv |= (uint64_t)code << (4 * next);
+      ++next;
+    }
+    a.dense = true;
+    a.K = next <= 5 ? 5 : 8;
+  }
+  return a;
+}
+
+// Makes `a` the context's alphabet; with `layouts`, writes the recoded
+// nibbles and code planes of all n records (dense alphabets).
+static int use_alphabet(ngia_ctx *c, const AlphaChoice &a, uint64_t words, uint32_t n,
+                        bool layouts) {
+  c->table_ok = a.table_ok;
+  c->align_nib = c->nib.as<uint32_t>();
+  c->ab = Alphabet{16, 0xFEDCBA9876543210ull};
+  c->recode_map = 0;
+  if (!a.dense) return NGIA_OK;
+  NGIA_TRY(c->nib_dense.reserve(words * 4));
+  NGIA_TRY(c->dplanes.reserve(words * 4));
+  if (layouts)
+    NGIA_TRY(launch_dense_layouts(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), n, a.map,
+                                  c->nib_dense.as<uint32_t>(), c->dplanes.as<uint32_t>(),
+                                  c->stream));
+  c->align_nib = c->nib_dense.as<uint32_t>();
+  c->ab = Alphabet{a.K, a.inv, c->dplanes.as<uint32_t>()};
+  c->recode_map = a.map;
+  return NGIA_OK;
+}
+
 int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64_t *h_offs,
              const uint32_t *h_lens, uint32_t n, const uint32_t *h_rep, uint32_t bands) {
   if (n == 0 || !h_packed || !h_offs || !h_lens) return NGIA_ERR_ARG;
@@ -205,29 +260,8 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
   NGIA_CUDA(cudaMemcpyAsync(&present, c->presence.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             s));
   NGIA_CUDA(cudaStreamSynchronize(s));
-  // Dense recoding of the residue codes in use (code 0 stays 0): equality of
-  // codes, all the aligner looks at, is unchanged by a bijection.
-  c->align_nib = c->nib.as<uint32_t>();
-  c->ab = Alphabet{16, 0xFEDCBA9876543210ull};
-  c->recode_map = 0;
-  c->table_ok = (present & 1u) == 0 && present != 0 && __builtin_popcount(present) <= 4;
-  if (__builtin_popcount(present & ~1u) <= 7) {
-    uint64_t map = 0, inv = 0;
-    int next = 1;
-    for (int code = 1; code < 16; ++code) {
-      if (!((present >> code) & 1u)) continue;
-      map |= (uint64_t)next << (4 * code);
-      inv |= (uint64_t)code << (4 * next);
-      ++next;
-    }
-    NGIA_TRY(c->nib_dense.reserve(words * 4));
-    NGIA_TRY(c->dplanes.reserve(words * 4));
-    NGIA_TRY(launch_dense_layouts(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), n, map,
-                                  c->nib_dense.as<uint32_t>(), c->dplanes.as<uint32_t>(), s));
-    c->align_nib = c->nib_dense.as<uint32_t>();
-    c->ab = Alphabet{next <= 5 ? 5 : 8, inv, c->dplanes.as<uint32_t>()};
-    c->recode_map = map;
-  }
+  NGIA_TRY(use_alphabet(c, choose_alphabet(present), words, n, true));
+  c->last_present = present;
   c->n = n;
   c->sigs_valid = false;
   c->packed_words = words;
@@ -239,6 +273,109 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
                               cudaMemcpyHostToDevice, s));
     c->rep_bands = bands;
   }
+  return NGIA_OK;
+}
+
+// Load and sketch in one pipeline (ngia_ctx_run_host): the records go to the
+// device in kLoadChunks pieces on their own stream, and each piece's layouts
+// and signatures are computed while the next pieces are in flight.  The
+// layouts and the sketch need the database's code map, known only once every
+// record has been seen; the pipeline assumes the previous load's map (its
+// sketch tables are cached) and checks it at the end.  Runs only when that map
+// takes the table sketch and the record offsets are in order; *sketched tells
+// whether the signatures are final (else the caller sketches as usual, the
+// load itself being complete either way).  *used = false: nothing was done.
+int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
+                    const uint64_t *h_offs, const uint32_t *h_lens, uint32_t n, bool *used,
+                    bool *sketched) {
+  *used = *sketched = false;
+  if (n < 4096 || !h_packed || !h_offs || !h_lens || !c->last_present || !c->use_table)
+    return NGIA_OK;
+  const AlphaChoice spec = choose_alphabet(c->last_present);
+  if (!spec.dense || !spec.table_ok || !c->table_built || c->table_inv != spec.inv)
+    return NGIA_OK;
+  *used = true;
+  cudaStream_t s = c->stream;
+  NGIA_TRY(c->packed.reserve(words * 4));
+  NGIA_TRY(c->offs.reserve((size_t)n * 8));
+  NGIA_TRY(c->lens.reserve((size_t)n * 4));
+  NGIA_TRY(c->nib.reserve(words * 4));
+  NGIA_TRY(c->nib_dense.reserve(words * 4));
+  NGIA_TRY(c->dplanes.reserve(words * 4));
+  NGIA_TRY(c->presence.reserve(2 * sizeof(uint32_t)));
+  NGIA_TRY(c->sigs.reserve((size_t)kBands * n * 4));
+  NGIA_CUDA(cudaMemcpyAsync(c->offs.p, h_offs, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+  NGIA_CUDA(cudaMemcpyAsync(c->lens.p, h_lens, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  NGIA_CUDA(cudaMemsetAsync(c->presence.p, 0, 2 * sizeof(uint32_t), s));
+  // pieces cut at record boundaries, taken from the end of the buffer and
+  // growing (the last 1/8 of the words, the 1/8 before, then 1/4, then the
+  // first half): the first copy, which nothing hides, is short, the later
+  // sketch launches have enough records per warp, and the shortest records
+  // (length order), whose signatures come from the short records' kernel on
+  // the side stream, arrive first, so that kernel runs beside the rest of the
+  // pipeline.  The cuts assume offsets in order; the layout kernel verifies
+  // every record lies in its piece.
+  constexpr int C = 4;
+  static_assert(C <= ngia_ctx::kLoadChunks, "pieces");
+  uint32_t first[C + 1];
+  uint64_t cut[C + 1];
+  cut[0] = 0;
+  for (int k = 1; k < C; ++k) cut[k] = words - (words >> k);
+  cut[C] = words;
+  first[0] = 0;
+  for (int k = 1; k < C; ++k) {
+    const uint64_t *p = std::lower_bound(h_offs, h_offs + n, cut[k]);
+    first[k] = (uint32_t)(p - h_offs);
+    if (first[k] < first[k - 1]) first[k] = first[k - 1];
+  }
+  first[C] = n;
+  uint32_t *packed = c->packed.as<uint32_t>();
+  // the copies overwrite records that earlier work on the stream may still read
+  NGIA_CUDA(cudaEventRecord(c->ev[5], s));
+  NGIA_CUDA(cudaStreamWaitEvent(c->copy, c->ev[5], 0));
+  for (int k = C - 1; k >= 0; --k) {
+    const uint64_t w0 = k == 0 ? 0 : (first[k] < n ? h_offs[first[k]] : words);
+    const uint64_t w1 = k + 1 == C ? words : (first[k + 1] < n ? h_offs[first[k + 1]] : words);
+    if (w1 > w0)
+      NGIA_CUDA(cudaMemcpyAsync(packed + w0, h_packed + w0, (w1 - w0) * 4,
+                                cudaMemcpyHostToDevice, c->copy));
+    NGIA_CUDA(cudaEventRecord(c->chunk_ev[k], c->copy));
+  }
+  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  const uint64_t *offs = c->offs.as<uint64_t>();
+  for (int k = C - 1; k >= 0; --k) {
+    const uint32_t r0 = first[k], cnt = first[k + 1] - first[k];
+    NGIA_CUDA(cudaStreamWaitEvent(s, c->chunk_ev[k], 0));
+    if (cnt == 0) continue;
+    const uint64_t w0 = k == 0 ? 0 : (first[k] < n ? h_offs[first[k]] : words);
+    const uint64_t w1 = k + 1 == C ? words : (first[k + 1] < n ? h_offs[first[k + 1]] : words);
+    NGIA_TRY(launch_load_layouts(packed, offs + r0, cnt, w0, w1, spec.map,
+                                 c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
+                                 c->dplanes.as<uint32_t>(), c->presence.as<uint32_t>(), s));
+    NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(), offs + r0,
+                                 cnt, spec.inv, c->sketch_table.p, c->sigs.as<uint32_t>() + r0,
+                                 n, s, c->side, c->ev[6], nullptr));
+  }
+  NGIA_CUDA(cudaEventRecord(c->ev[7], c->side));  // the short records' kernels
+  NGIA_CUDA(cudaStreamWaitEvent(s, c->ev[7], 0));
+  NGIA_CUDA(cudaEventRecord(c->ev[1], s));
+  uint32_t flags[2] = {0u, 0u};  // codes present, a record outside its piece
+  NGIA_CUDA(cudaMemcpyAsync(flags, c->presence.p, sizeof(flags), cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  if (flags[1]) {  // offsets out of order: the pieces did not hold their records
+    *used = false;
+    return NGIA_OK;
+  }
+  const uint32_t present = flags[0];
+  const AlphaChoice got = choose_alphabet(present);
+  *sketched = got == spec;
+  NGIA_TRY(use_alphabet(c, got, words, n, !*sketched));  // another map: its own layouts
+  c->last_present = present;
+  c->n = n;
+  c->sigs_valid = false;
+  c->packed_words = words;
+  c->rep_bands = 0;
+  c->n_edges = 0;
   return NGIA_OK;
 }
 
@@ -286,6 +423,9 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
   }
   for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+  for (int k = 0; k < ngia_ctx::kLoadChunks && e == cudaSuccess; ++k)
+    e = cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming);
   if (e != cudaSuccess) {
     ngia_ctx_destroy(c);
     return ngia::cuda_fail(e);
@@ -312,6 +452,9 @@ void ngia_ctx_destroy(ngia_ctx *c) {
   for (int k = 0; k < 8; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->copy) cudaStreamDestroy(c->copy);
+  for (cudaEvent_t e : c->chunk_ev)
+    if (e) cudaEventDestroy(e);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -533,8 +676,14 @@ int ngia_ctx_run_host(ngia_ctx *c, const uint32_t *h_packed, uint64_t packed_wor
                       uint64_t *h_n_edges, ngia_stats *stats) {
   if (!c || !h_n_edges) return NGIA_ERR_ARG;
   if (stats) std::memset(stats, 0, sizeof(*stats));
-  NGIA_TRY(ngia::ctx_load(c, h_packed, packed_words, h_rec_offsets, h_lens, n, nullptr, bands));
-  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats));
+  bool piped = false, sketched = false;
+  if (bands >= 1 && bands <= (uint32_t)ngia::kBands)
+    NGIA_TRY(ngia::ctx_load_sketch(c, h_packed, packed_words, h_rec_offsets, h_lens, n, &piped,
+                                   &sketched));
+  if (!piped)
+    NGIA_TRY(ngia::ctx_load(c, h_packed, packed_words, h_rec_offsets, h_lens, n, nullptr, bands));
+  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats, sketched));
+  if (stats) stats->load_pipelined = sketched ? 1u : 0u;
   NGIA_TRY(ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats));
   return ngia_ctx_edges(c, h_edges, cap);
 }

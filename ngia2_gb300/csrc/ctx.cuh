@@ -7,8 +7,14 @@
 struct ngia_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  cudaEvent_t ev[8] = {};  // 0-3 stage timing, 6-7 fork/join of `side`
+  cudaEvent_t ev[8] = {};  // 0-3 stage timing, 5 copy ordering, 6-7 fork/join of `side`
   cudaStream_t side = nullptr;  // work that runs beside the main stream's (sketch)
+  // pipelined loads (ngia_ctx_run_host): chunks of the records copied on `copy`
+  // while the previous chunks are sketched on `stream`
+  static constexpr int kLoadChunks = 8;  // at most
+  cudaStream_t copy = nullptr;
+  cudaEvent_t chunk_ev[kLoadChunks] = {};
+  uint32_t last_present = 0;  // residue codes of the previous load (0: none yet)
   // resident database
   uint32_t n = 0;
   uint64_t packed_words = 0;
@@ -37,7 +43,8 @@ struct ngia_ctx {
 
 namespace ngia {
 DbView db_view(const ngia_ctx *c);
-int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st);
+// sketch_done: the signatures are already in place (a pipelined load).
+int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_done = false);
 int ctx_fast_cluster(ngia_ctx *c, uint32_t identity, uint32_t bands, uint32_t *h_cluster,
                      ngia_stats *st);
 }  // namespace ngia

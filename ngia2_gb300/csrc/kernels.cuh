@@ -19,11 +19,13 @@ int launch_sketch_nibbles(const uint32_t *nib, const uint64_t *offs, uint32_t n,
 constexpr uint32_t kSketchTableEntries = 1u << 16;
 size_t sketch_table_bytes();
 int build_sketch_table(uint64_t inv, void *table, cudaStream_t s);
-// The short records' kernel runs on `side` (forked from and joined back into
-// s through the two events) beside the rank walk on s.
+// Records offs[0..n) (a run of a database's records), signatures at
+// sigs[band * stride + i].  The short records' kernel runs on `side` (forked
+// from s through `fork`, joined back through `join`; join = null: the caller
+// joins later) beside the rank walk on s.
 int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
                         uint32_t n, uint64_t inv, const void *table, uint32_t *sigs,
-                        cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
+                        uint32_t stride, cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
                         cudaEvent_t join);
 
 // sort.cu
@@ -67,8 +69,16 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const uint32_t *order, const uint32_t *bounds, uint32_t *scores,
                        uint32_t identity, unsigned long long *work, unsigned int *cursor,
                        cudaStream_t s);
+// All layouts of records offs[0..n) in one pass, the code map known ahead
+// (pipelined loads): nibbles, presence[0] |= the codes present, recoded
+// nibbles and code planes; presence[1] = 1 if a record is not inside words
+// [w0, w1) (such a record is skipped).
+int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint64_t w0,
+                        uint64_t w1, uint64_t map, uint32_t *nib, uint32_t *dense_nib,
+                        uint32_t *dplanes, uint32_t *presence, cudaStream_t s);
+// presence |= the codes seen (cleared first unless accumulate)
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
-                   uint32_t *presence, cudaStream_t s);
+                   uint32_t *presence, cudaStream_t s, bool accumulate = false);
 int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
                   uint32_t *out, cudaStream_t s);
 // Packed records and a code map with new codes 0..7 -> the recoded nibbles

@@ -260,7 +260,7 @@ __device__ __forceinline__ void for_each_index(const uint32_t *w, uint32_t pb, u
 __global__ void __launch_bounds__(kRankWarps * 32)
 sketch_rank_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restrict__ offs,
                    uint32_t n, uint64_t inv, const uint16_t *__restrict__ ranks,
-                   uint32_t *__restrict__ sigs) {
+                   uint32_t *__restrict__ sigs, uint32_t stride) {
   __shared__ __align__(16) uint32_t bitsets[kRankWarps * kBitsetWords];
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t *bits = bitsets + (threadIdx.x >> 5) * kBitsetWords;
@@ -326,8 +326,8 @@ sketch_rank_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restric
     const uint32_t lo = index_hash(hit[0], inv, lane);
     const uint32_t hi = index_hash(hit[1], inv, lane + 32);
     __syncwarp();
-    sigs[(size_t)lane * n + i] = lo;
-    sigs[(size_t)(lane + 32) * n + i] = hi;
+    sigs[(size_t)lane * stride + i] = lo;
+    sigs[(size_t)(lane + 32) * stride + i] = hi;
   }
 }
 
@@ -337,7 +337,8 @@ sketch_rank_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restric
 __global__ void __launch_bounds__(256)
 sketch_table_kernel(const uint32_t *__restrict__ nib, const uint32_t *__restrict__ dense,
                     const uint64_t *__restrict__ offs, uint32_t n,
-                    const uint4 *__restrict__ table, uint32_t *__restrict__ sigs) {
+                    const uint4 *__restrict__ table, uint32_t *__restrict__ sigs,
+                    uint32_t stride) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
@@ -389,8 +390,8 @@ sketch_table_kernel(const uint32_t *__restrict__ nib, const uint32_t *__restrict
         else hi = r;
       }
     }
-    sigs[(size_t)lane * n + i] = lo;
-    sigs[(size_t)(lane + 32) * n + i] = hi;
+    sigs[(size_t)lane * stride + i] = lo;
+    sigs[(size_t)(lane + 32) * stride + i] = hi;
   }
 }
 
@@ -437,7 +438,7 @@ static int rank_blocks_per_sm() {
 
 int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
                         uint32_t n, uint64_t inv, const void *table, uint32_t *sigs,
-                        cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
+                        uint32_t stride, cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
                         cudaEvent_t join) {
   if (n == 0) return NGIA_OK;
   int dev = 0, sms = 0;
@@ -451,15 +452,18 @@ int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64
   NGIA_CUDA(cudaStreamWaitEvent(side, fork, 0));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms;
   sketch_table_kernel<<<want < cap ? want : cap, 256, 0, side>>>(
-      nib, dense, offs, n, reinterpret_cast<const uint4 *>(base), sigs);
+      nib, dense, offs, n, reinterpret_cast<const uint4 *>(base), sigs, stride);
   NGIA_LAUNCHED();
   const uint32_t rank_want = ceil_div(n, kRankWarps);
   const uint32_t rank_cap = (uint32_t)(sms * rank_blocks_per_sm());
   sketch_rank_kernel<<<rank_want < rank_cap ? rank_want : rank_cap, kRankWarps * 32, 0, s>>>(
-      dense, offs, n, inv, reinterpret_cast<const uint16_t *>(base + kRowTableBytes), sigs);
+      dense, offs, n, inv, reinterpret_cast<const uint16_t *>(base + kRowTableBytes), sigs,
+      stride);
   NGIA_LAUNCHED();
-  NGIA_CUDA(cudaEventRecord(join, side));
-  NGIA_CUDA(cudaStreamWaitEvent(s, join, 0));
+  if (join) {
+    NGIA_CUDA(cudaEventRecord(join, side));
+    NGIA_CUDA(cudaStreamWaitEvent(s, join, 0));
+  }
   return NGIA_OK;
 }
 
