@@ -180,7 +180,7 @@ __global__ void accumulate_kernel(const Counters *__restrict__ rc,
 }
 
 struct StreamState {
-  DevBuf region_packed, region_nib, region_dense, region_dplanes, r_offs, r_lens;
+  DevBuf region_packed, region_nib, region_dplanes, r_offs, r_lens;
   DevBuf offs, lens, sigs, sig_tmp, rep, scratch, ucount, uoff, counters, pairs, scores,
       keys, keys_sorted, order, block_pairs, block_scores, chunk_first, presence, emit_tmp,
       edges;
@@ -188,8 +188,7 @@ struct StreamState {
   Stager stager;
   cudaStream_t s = nullptr;
   void destroy() {
-    DevBuf *bufs[] = {&region_packed, &region_nib, &region_dense, &region_dplanes, &r_offs,
-                      &r_lens,
+    DevBuf *bufs[] = {&region_packed, &region_nib, &region_dplanes, &r_offs, &r_lens,
                       &offs,          &lens,       &sigs,         &sig_tmp, &rep,
                       &scratch,       &ucount,     &uoff,         &counters, &pairs,
                       &scores,        &keys,       &keys_sorted,  &order,   &block_pairs,
@@ -209,9 +208,9 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
                         ngia_stream_stats *st) {
   const auto t_all = SClock::now();
   // ---- chunks: contiguous runs of records of at most chunk_words words
-  // (three chunk slots of planes, nibble codes, recoded codes and code planes in
-  // the budget)
-  const uint64_t chunk_words = chunk_bytes / (3ull * 4 * 4);
+  // (three chunk slots of planes, nibble codes -- the recoded ones in pass 2 --
+  // and code planes in the budget)
+  const uint64_t chunk_words = chunk_bytes / (3ull * 4 * 3);
   std::vector<Chunk> chunks;
   for (uint32_t i = 0; i < n; ++i) {
     const uint64_t w = 1 + 4ull * ((h_lens[i] + 31) / 32);
@@ -260,9 +259,10 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
   uint64_t *roffs = S.r_offs.as<uint64_t>();
   uint32_t *rlens = S.r_lens.as<uint32_t>();
 
-  // Loads chunk k into region slot `slot` (planes and nibble codes, and the
-  // recoded codes when the alphabet is dense) with its record table at
-  // entries [at, at + count); the work is ordered on s.
+  // Loads chunk k into region slot `slot` (planes, and the nibble codes; once
+  // the alphabet is known to be dense (pass 2) the recoded codes in their place
+  // and the code planes) with its record table at entries [at, at + count);
+  // the work is ordered on s.
   uint64_t map = 0;
   bool dense = false;
   auto load_chunk = [&](uint32_t k, int slot, uint32_t at, uint32_t *presence) -> int {
@@ -275,10 +275,11 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
         S.offs.as<uint64_t>(), S.lens.as<uint32_t>(), c.first, c.count, c.word_first, base, at,
         roffs, rlens);
     NGIA_LAUNCHED();
-    NGIA_TRY(launch_nibbles(rp, roffs + at, c.count, rn, presence, s));
     if (dense)
-      NGIA_TRY(launch_dense_layouts(rp, roffs + at, c.count, map, S.region_dense.as<uint32_t>(),
+      NGIA_TRY(launch_dense_layouts(rp, roffs + at, c.count, map, rn,
                                     S.region_dplanes.as<uint32_t>(), s));
+    else
+      NGIA_TRY(launch_nibbles(rp, roffs + at, c.count, rn, presence, s));
     return NGIA_OK;
   };
 
@@ -371,7 +372,6 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
       ++next;
     }
     dense = true;
-    NGIA_TRY(S.region_dense.reserve(3 * chunk_words * 4));
     NGIA_TRY(S.region_dplanes.reserve(3 * chunk_words * 4));
     ab = Alphabet{next <= 5 ? 5 : 8, inv, S.region_dplanes.as<uint32_t>()};
   }
@@ -385,7 +385,7 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
   NGIA_TRY(S.block_scores.reserve(mb * 4));
   NGIA_TRY(S.round.reserve(max_block));
   NGIA_CUDA(cudaMemsetAsync(S.scores.p, 0, mm * 4, s));
-  const DbView view{rp, dense ? S.region_dense.as<uint32_t>() : rn, ab, roffs, rlens};
+  const DbView view{rp, rn, ab, roffs, rlens};
   NGIA_CUDA(cudaMemsetAsync(acc, 0, 16, s));
   uint64_t loads = 0;
   int inner = 1;  // slot of the current inner chunk (1 and 2 alternate)
