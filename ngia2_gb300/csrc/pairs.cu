@@ -199,21 +199,90 @@ positive_flags_kernel(const uint32_t *__restrict__ scores, uint32_t stride, uint
   if (p < count) flags[p] = scores[(size_t)p * stride] > 0 ? 1u : 0u;
 }
 
-// Pairs with score > 0, compacted in pair order into (rep keys, tar, score).
+// Ordered compaction of the pairs with score > 0 in three passes that touch
+// the scores twice and nothing per pair besides: per-block counts over runs
+// of kEmitRun pairs, their exclusive scan (one block), then each block writes
+// its hits from its offset in pair order (ballots within a warp, warp counts
+// across the block).
+constexpr uint32_t kEmitRun = 4096;
+
 __global__ void __launch_bounds__(256)
-compact_pairs_kernel(const uint2 *__restrict__ pairs, const uint32_t *__restrict__ scores,
-                     uint32_t count, const uint64_t *__restrict__ off,
-                     uint32_t *__restrict__ erep, uint32_t *__restrict__ etar,
-                     uint32_t *__restrict__ escore) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= count) return;
-  const uint32_t sc = scores[p];
-  if (sc == 0) return;
-  const uint64_t e = off[p];
-  const uint2 pr = pairs[p];
-  erep[e] = pr.x;
-  etar[e] = pr.y;
-  escore[e] = sc;
+count_hits_kernel(const uint32_t *__restrict__ scores, uint32_t count,
+                  uint32_t *__restrict__ bcount) {
+  __shared__ uint32_t wsum[8];
+  const uint32_t beg = blockIdx.x * kEmitRun, end = min(beg + kEmitRun, count);
+  uint32_t c = 0;
+  for (uint32_t p = beg + threadIdx.x; p < end; p += 256) c += scores[p] > 0 ? 1u : 0u;
+  c = __reduce_add_sync(kFull, c);
+  if ((threadIdx.x & 31u) == 0) wsum[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < 8; ++w) t += wsum[w];
+    bcount[blockIdx.x] = t;
+  }
+}
+
+// exclusive scan of nb counts in place (one block of 1024), total -> *m
+__global__ void __launch_bounds__(1024)
+scan_hits_kernel(uint32_t *__restrict__ b, uint32_t nb, uint64_t *__restrict__ m) {
+  __shared__ uint32_t part[32];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t run = 0;
+  for (uint32_t base = 0; base < nb; base += 1024) {  // block-uniform
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < nb ? b[i] : 0u;
+    uint32_t x = v;
+#pragma unroll
+    for (int k = 1; k < 32; k <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, x, k);
+      if (lane >= (uint32_t)k) x += y;
+    }
+    if (lane == 31) part[warp] = x;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (uint32_t w = 0; w < 32; ++w) {
+      before += w < warp ? part[w] : 0u;
+      total += part[w];
+    }
+    if (i < nb) b[i] = run + before + x - v;
+    run += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *m = run;
+}
+
+__global__ void __launch_bounds__(256)
+compact_hits_kernel(const uint2 *__restrict__ pairs, const uint32_t *__restrict__ scores,
+                    uint32_t count, const uint32_t *__restrict__ boff,
+                    uint32_t *__restrict__ erep, uint32_t *__restrict__ etar,
+                    uint32_t *__restrict__ escore) {
+  __shared__ uint32_t wsum[8];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t beg = blockIdx.x * kEmitRun, end = min(beg + kEmitRun, count);
+  uint32_t run = boff[blockIdx.x];
+  for (uint32_t p0 = beg; p0 < end; p0 += 256) {  // block-uniform
+    const uint32_t p = p0 + threadIdx.x;
+    const uint32_t sc = p < end ? scores[p] : 0u;
+    const uint32_t hits = __ballot_sync(kFull, sc > 0);
+    if (lane == 0) wsum[warp] = __popc(hits);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < 8; ++w) {
+      before += w < warp ? wsum[w] : 0u;
+      total += wsum[w];
+    }
+    if (sc > 0) {
+      const uint32_t e = run + before + __popc(hits & ((1u << lane) - 1u));
+      const uint2 pr = pairs[p];
+      erep[e] = pr.x;
+      etar[e] = pr.y;
+      escore[e] = sc;
+    }
+    run += total;
+    __syncthreads();
+  }
 }
 
 __global__ void __launch_bounds__(256)
@@ -283,11 +352,14 @@ int emit_sorted(const uint2 *pairs, const uint32_t *scores, uint32_t count,
       (reinterpret_cast<uintptr_t>(sort_scratch + radix_sort_scratch_bytes(count, 1)) + 15) &
       ~uintptr_t(15));
   uint64_t *d_total = scan_tmp + ceil_div<size_t>(count, 2048) + 1;
-  const uint32_t blocks = ceil_div(count, 256u);
-  positive_flags_kernel<<<blocks, 256, 0, s>>>(scores, 1, count, flags);
+  (void)off;
+  const uint32_t runs = ceil_div(count, kEmitRun);
+  uint32_t *bcount = flags;  // runs words (count >= runs)
+  count_hits_kernel<<<runs, 256, 0, s>>>(scores, count, bcount);
   NGIA_LAUNCHED();
-  NGIA_TRY(exclusive_scan_u64(flags, off, count, d_total, scan_tmp, s));
-  compact_pairs_kernel<<<blocks, 256, 0, s>>>(pairs, scores, count, off, erep, etar, escore);
+  scan_hits_kernel<<<1, 1024, 0, s>>>(bcount, runs, d_total);
+  NGIA_LAUNCHED();
+  compact_hits_kernel<<<runs, 256, 0, s>>>(pairs, scores, count, bcount, erep, etar, escore);
   NGIA_LAUNCHED();
   uint64_t m = 0;
   NGIA_CUDA(cudaMemcpyAsync(&m, d_total, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
