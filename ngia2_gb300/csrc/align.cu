@@ -290,28 +290,30 @@ int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_
 }
 
 // Every layout of a run of records in one pass over their planes, for loads
-// whose code map is known ahead (the pipelined load): nibbles, the codes
-// present (presence[0]), recoded nibbles and code planes, and presence[1] = 1
-// if a record is not inside words [w0, w1) (then it is left alone).
+// whose code map is assumed ahead (the pipelined load): nibbles, recoded
+// nibbles and code planes.  Only the map's own codes are looked at: a residue
+// of another code (or a record outside words [w0, w1), which is then left
+// alone) sets *bad, and the load falls back.  Any subset of the map's codes
+// is served by the same map (it stays one-to-one on the codes present).
+// codes[k], k < ncodes: the residue codes of the map, aligner code k + 1.
 __global__ void __launch_bounds__(256)
 load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
-                    uint32_t n, uint64_t w0, uint64_t w1, uint32_t bit0, uint32_t bit1,
-                    uint32_t bit2, uint32_t *__restrict__ nib, uint32_t *__restrict__ dense_nib,
-                    uint32_t *__restrict__ dplanes, uint32_t *__restrict__ presence) {
+                    uint32_t n, uint64_t w0, uint64_t w1, uint32_t codes, uint32_t ncodes,
+                    uint32_t *__restrict__ nib, uint32_t *__restrict__ dense_nib,
+                    uint32_t *__restrict__ dplanes, uint32_t *__restrict__ bad) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  uint32_t mine = 0;
-  bool bad = false;
+  bool wrong = false;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
     if (o < w0 || o >= w1) {
-      bad = true;
+      wrong = true;
       continue;
     }
     const uint32_t len = __ldg(packed + o);
     const uint32_t blocks = (len + 31) >> 5;
     if (o + 1 + 4ull * blocks > w1) {
-      bad = true;
+      wrong = true;
       continue;
     }
     if (lane == 0) {
@@ -327,15 +329,16 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
       planes_to_nibbles(pl, 4, w);
       const uint32_t left = len - 32 * k;
       const uint32_t real = left >= 32 ? kFull : (1u << left) - 1u;
-      uint32_t d[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-      for (uint32_t c = 0; c < 16; ++c) {
-        const uint32_t m = code_mask(pl, c);
-        if (m & real) mine |= 1u << c;
-        d[0] |= (bit0 >> c) & 1u ? m : 0u;
-        d[1] |= (bit1 >> c) & 1u ? m : 0u;
-        d[2] |= (bit2 >> c) & 1u ? m : 0u;
+      uint32_t d[4] = {0u, 0u, 0u, 0u}, known = 0u;
+      for (uint32_t j = 0; j < ncodes; ++j) {
+        const uint32_t m = code_mask(pl, (codes >> (4 * j)) & 15u);
+        const uint32_t a = j + 1;  // aligner code
+        known |= m;
+        d[0] |= a & 1u ? m : 0u;
+        d[1] |= a & 2u ? m : 0u;
+        d[2] |= a & 4u ? m : 0u;
       }
+      if (real & ~known) wrong = true;
       uint32_t dn[4];
       planes_to_nibbles(d, 3, dn);
 #pragma unroll
@@ -346,12 +349,7 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
       }
     }
   }
-  mine = __reduce_or_sync(kFull, mine);
-  const uint32_t any_bad = __ballot_sync(kFull, bad);
-  if (lane == 0) {
-    if (mine) atomicOr(presence, mine);
-    if (any_bad) atomicOr(presence + 1, 1u);
-  }
+  if (__ballot_sync(kFull, wrong) && lane == 0) atomicOr(bad, 1u);
 }
 
 static int map_bits(uint64_t map, uint32_t (&bits)[3]) {
@@ -366,17 +364,21 @@ static int map_bits(uint64_t map, uint32_t (&bits)[3]) {
 }
 
 int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint64_t w0,
-                        uint64_t w1, uint64_t map, uint32_t *nib, uint32_t *dense_nib,
-                        uint32_t *dplanes, uint32_t *presence, cudaStream_t s) {
+                        uint64_t w1, uint64_t inv, uint32_t *nib, uint32_t *dense_nib,
+                        uint32_t *dplanes, uint32_t *bad, cudaStream_t s) {
   if (n == 0) return NGIA_OK;
-  uint32_t bits[3];
-  NGIA_TRY(map_bits(map, bits));
+  uint32_t codes = 0, ncodes = 0;  // inv nibble d = residue code of aligner code d
+  for (uint32_t d = 1; d < 8; ++d) {
+    const uint32_t c = (uint32_t)(inv >> (4 * d)) & 15u;
+    if (c == 0) break;
+    codes |= c << (4 * ncodes++);
+  }
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
   load_layouts_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
-      packed, offs, n, w0, w1, bits[0], bits[1], bits[2], nib, dense_nib, dplanes, presence);
+      packed, offs, n, w0, w1, codes, ncodes, nib, dense_nib, dplanes, bad);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

@@ -277,14 +277,15 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
 }
 
 // Load and sketch in one pipeline (ngia_ctx_run_host): the records go to the
-// device in kLoadChunks pieces on their own stream, and each piece's layouts
-// and signatures are computed while the next pieces are in flight.  The
-// layouts and the sketch need the database's code map, known only once every
-// record has been seen; the pipeline assumes the previous load's map (its
-// sketch tables are cached) and checks it at the end.  Runs only when that map
-// takes the table sketch and the record offsets are in order; *sketched tells
-// whether the signatures are final (else the caller sketches as usual, the
-// load itself being complete either way).  *used = false: nothing was done.
+// device in pieces on their own stream, and each piece's layouts and
+// signatures are computed while the next pieces are in flight.  The layouts
+// and the sketch need the database's code map, known only once every record
+// has been seen; the pipeline assumes the previous load's map (its sketch
+// tables are cached) and checks at the end that every residue's code is one of
+// the map's and every record lay inside its piece (offsets in order).  Runs
+// only when that map takes the table sketch.  *used = false: nothing usable
+// was done (the caller loads as usual); else the load is complete and
+// *sketched tells whether the signatures are in place.
 int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
                     const uint64_t *h_offs, const uint32_t *h_lens, uint32_t n, bool *used,
                     bool *sketched) {
@@ -306,7 +307,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
   NGIA_TRY(c->sigs.reserve((size_t)kBands * n * 4));
   NGIA_CUDA(cudaMemcpyAsync(c->offs.p, h_offs, (size_t)n * 8, cudaMemcpyHostToDevice, s));
   NGIA_CUDA(cudaMemcpyAsync(c->lens.p, h_lens, (size_t)n * 4, cudaMemcpyHostToDevice, s));
-  NGIA_CUDA(cudaMemsetAsync(c->presence.p, 0, 2 * sizeof(uint32_t), s));
+  NGIA_CUDA(cudaMemsetAsync(c->presence.p, 0, sizeof(uint32_t), s));
   // pieces cut at record boundaries, taken from the end of the buffer and
   // growing (the last 1/8 of the words, the 1/8 before, then 1/4, then the
   // first half): the first copy, which nothing hides, is short, the later
@@ -315,12 +316,13 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
   // the side stream, arrive first, so that kernel runs beside the rest of the
   // pipeline.  The cuts assume offsets in order; the layout kernel verifies
   // every record lies in its piece.
-  constexpr int C = 4;
+  constexpr uint32_t kCuts[] = {4, 8, 12, 14};  // cut points, in sixteenths of the words
+  constexpr int C = (int)(sizeof(kCuts) / sizeof(kCuts[0])) + 1;
   static_assert(C <= ngia_ctx::kLoadChunks, "pieces");
   uint32_t first[C + 1];
   uint64_t cut[C + 1];
   cut[0] = 0;
-  for (int k = 1; k < C; ++k) cut[k] = words - (words >> k);
+  for (int k = 1; k < C; ++k) cut[k] = words / 16 * kCuts[k - 1];
   cut[C] = words;
   first[0] = 0;
   for (int k = 1; k < C; ++k) {
@@ -349,7 +351,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
     if (cnt == 0) continue;
     const uint64_t w0 = k == 0 ? 0 : (first[k] < n ? h_offs[first[k]] : words);
     const uint64_t w1 = k + 1 == C ? words : (first[k + 1] < n ? h_offs[first[k + 1]] : words);
-    NGIA_TRY(launch_load_layouts(packed, offs + r0, cnt, w0, w1, spec.map,
+    NGIA_TRY(launch_load_layouts(packed, offs + r0, cnt, w0, w1, spec.inv,
                                  c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
                                  c->dplanes.as<uint32_t>(), c->presence.as<uint32_t>(), s));
     NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(), offs + r0,
@@ -359,18 +361,16 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
   NGIA_CUDA(cudaEventRecord(c->ev[7], c->side));  // the short records' kernels
   NGIA_CUDA(cudaStreamWaitEvent(s, c->ev[7], 0));
   NGIA_CUDA(cudaEventRecord(c->ev[1], s));
-  uint32_t flags[2] = {0u, 0u};  // codes present, a record outside its piece
-  NGIA_CUDA(cudaMemcpyAsync(flags, c->presence.p, sizeof(flags), cudaMemcpyDeviceToHost, s));
+  uint32_t bad = 0;  // a code outside the map, or a record outside its piece
+  NGIA_CUDA(cudaMemcpyAsync(&bad, c->presence.p, sizeof(bad), cudaMemcpyDeviceToHost, s));
   NGIA_CUDA(cudaStreamSynchronize(s));
-  if (flags[1]) {  // offsets out of order: the pieces did not hold their records
+  if (bad) {  // the plain load takes over from the start
     *used = false;
     return NGIA_OK;
   }
-  const uint32_t present = flags[0];
-  const AlphaChoice got = choose_alphabet(present);
-  *sketched = got == spec;
-  NGIA_TRY(use_alphabet(c, got, words, n, !*sketched));  // another map: its own layouts
-  c->last_present = present;
+  // the codes present are among the map's: the same map serves them
+  *sketched = true;
+  NGIA_TRY(use_alphabet(c, spec, words, n, false));
   c->n = n;
   c->sigs_valid = false;
   c->packed_words = words;

@@ -69,13 +69,13 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
                        const uint32_t *order, const uint32_t *bounds, uint32_t *scores,
                        uint32_t identity, unsigned long long *work, unsigned int *cursor,
                        cudaStream_t s);
-// All layouts of records offs[0..n) in one pass, the code map known ahead
-// (pipelined loads): nibbles, presence[0] |= the codes present, recoded
-// nibbles and code planes; presence[1] = 1 if a record is not inside words
-// [w0, w1) (such a record is skipped).
+// All layouts of records offs[0..n) in one pass under an assumed code map
+// (inv: nibble d = residue code of aligner code d, pipelined loads): nibbles,
+// recoded nibbles and code planes.  *bad = 1 if a residue has a code outside
+// the map or a record is not inside words [w0, w1) (such a record is skipped).
 int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint64_t w0,
-                        uint64_t w1, uint64_t map, uint32_t *nib, uint32_t *dense_nib,
-                        uint32_t *dplanes, uint32_t *presence, cudaStream_t s);
+                        uint64_t w1, uint64_t inv, uint32_t *nib, uint32_t *dense_nib,
+                        uint32_t *dplanes, uint32_t *bad, cudaStream_t s);
 // presence |= the codes seen (cleared first unless accumulate)
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
                    uint32_t *presence, cudaStream_t s, bool accumulate = false);

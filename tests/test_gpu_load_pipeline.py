@@ -76,3 +76,17 @@ def test_pipelined_load_falls_back_on_another_alphabet(cuda, built, golden):
     assert np.array_equal(got_n, resident_edges(with_n, 90))
     assert np.array_equal(got_p, resident_edges(prot_db, 50))
     assert np.array_equal(got_d, resident_edges(dna_db, 90))
+
+
+def test_pipelined_load_serves_a_subset_of_the_codes(cuda, built):
+    """A database with only A, C, G after an A, C, G, T one: the assumed map is
+    still one-to-one on the codes present, so the pipeline keeps it; the edges
+    are the resident path's (which recodes to three codes)."""
+    s = synth.dna_families(10_000, 1_000, seed=34)
+    three = database([s.seq(i).replace(b"T", b"G") for i in range(len(s))])
+    with ng.Context() as ctx:
+        host_edges(ctx, dna(10_000, 1_000, 35), 90)
+        host_edges(ctx, dna(10_000, 1_000, 35), 90)
+        got, st = host_edges(ctx, three, 85)
+    assert st["load_pipelined"] == 1
+    assert np.array_equal(got, resident_edges(three, 85))
