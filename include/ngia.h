@@ -351,7 +351,12 @@ int ngia_ctx_rep_rows(ngia_ctx *ctx, uint32_t *h_rep, uint32_t bands);
 /* End-to-end call on host buffers: copy the database in, sketch + bucket,
  * build the graph, copy the edges out (the reference's makedb grouping plus
  * buildGraph in one call).  Device buffers of the context are reused across
- * calls.  Synchronises. */
+ * calls.  When the previous load's residue codes took the table sketch (four
+ * codes or fewer, none 0), the upload goes in pieces that are sketched as they
+ * land, under that code map; a database whose codes fall outside it, or whose
+ * record offsets are not in order, is loaded the plain way (same result;
+ * stats->load_pipelined tells which).  Pinned host buffers give the upload
+ * the link's full bandwidth.  Synchronises. */
 int ngia_ctx_run_host(ngia_ctx *ctx, const uint32_t *h_packed,
                       uint64_t packed_words, const uint64_t *h_rec_offsets,
                       const uint32_t *h_lens, uint32_t n, uint32_t identity,
