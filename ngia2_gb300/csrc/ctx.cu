@@ -91,23 +91,22 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   Counters *dc = c->counters.as<Counters>();
   NGIA_CUDA(cudaMemsetAsync(dc, 0, sizeof(Counters), s));
   NGIA_CUDA(cudaEventRecord(c->ev[0], s));
-  // 1. candidates: per-target unique counts, offsets, total
-  NGIA_TRY(collect_count(rep, lens, n, bands, identity, c->ucount.as<uint32_t>(),
-                         &dc->cand_total, s));
-  NGIA_TRY(c->scan_tmp.reserve(scan_scratch_bytes(n)));
-  NGIA_TRY(exclusive_scan_u64(c->ucount.as<uint32_t>(), c->uoff.as<uint64_t>(), n,
-                              &dc->unique_total, c->scan_tmp.as<uint64_t>(), s));
+  // 1. candidates: distinct pairs grouped by target, in one pass (the pair
+  // buffer holds the worst case, bands x n)
+  NGIA_TRY(c->pairs.reserve((size_t)bands * n * 8));
+  uint2 *pairs = c->pairs.as<uint2>();
+  NGIA_TRY(collect_scan(rep, lens, n, bands, identity, &dc->collect_ticket,
+                        reinterpret_cast<unsigned long long *>(c->uoff.p), &dc->cand_total,
+                        &dc->unique_total, &dc->collect_error, pairs, s));
   Counters hc;
   NGIA_CUDA(cudaMemcpyAsync(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
   NGIA_CUDA(cudaStreamSynchronize(s));
+  if (hc.collect_error) return NGIA_ERR_CUDA;  // a look-back gave up (never seen)
   const uint64_t total = hc.unique_total;
   if (total > 0xFFFFFFFFull) return NGIA_ERR_NOMEM;  // beyond one launch's index range
   const uint32_t m = (uint32_t)total;
-  NGIA_TRY(c->pairs.reserve((size_t)(m ? m : 1) * 8));
   NGIA_TRY(c->scores.reserve((size_t)(m ? m : 1) * 4));
-  uint2 *pairs = c->pairs.as<uint2>();
   uint32_t *scores = c->scores.as<uint32_t>();
-  NGIA_TRY(collect_write(rep, lens, n, bands, identity, c->uoff.as<uint64_t>(), pairs, s));
   // 2-3. width classes, then one persistent launch per class (the round is
   // on the context's stream)
   NGIA_TRY(c->round.reserve(m));

@@ -89,6 +89,13 @@ int launch_dense_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t 
                          cudaStream_t s);
 
 // pairs.cu
+// Candidate pairs in one pass (see pairs.cu): pairs[] must hold bands * n;
+// *ticket and *unique_total zero before the call, status[] holds
+// ceil(n / 32) words (cleared here); *error set if a look-back gave up.
+int collect_scan(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
+                 uint32_t identity, unsigned int *ticket, unsigned long long *status,
+                 unsigned long long *cand_total, uint64_t *unique_total, unsigned int *error,
+                 uint2 *pairs, cudaStream_t s);
 int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
                   uint32_t identity, uint32_t *ucount, unsigned long long *cand_total,
                   cudaStream_t s);

@@ -99,6 +99,129 @@ collect_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict__ le
   if (MODE == 0 && lane == 0 && cand_sum) atomicAdd(cand_total, (unsigned long long)cand_sum);
 }
 
+// Both passes in one (the resident path): blocks of targets take tickets in
+// order, count their distinct pairs, find their offset by a decoupled look-back
+// over the earlier blocks' published counts, and write their pairs -- the same
+// output as collect_count + scan + collect_write, with the rep rows and the
+// length gathers read once.  status[] (zero before the launch): per block,
+// bits 62-63 = 0 not ready / 1 its own count / 2 the prefix through it, bits
+// 0-61 the value.  A look-back that waits too long sets *error and the block
+// writes nothing.
+constexpr unsigned long long kStAgg = 1ull << 62, kStIncl = 2ull << 62;
+constexpr unsigned long long kStValue = (1ull << 62) - 1;
+constexpr uint32_t kLookbackSpins = 1u << 22;
+
+__global__ void __launch_bounds__(kPairThreads)
+collect_scan_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict__ lens,
+                    uint32_t n, uint32_t bands, float t, unsigned int *__restrict__ ticket,
+                    unsigned long long *__restrict__ status,
+                    unsigned long long *__restrict__ cand_total,
+                    uint64_t *__restrict__ unique_total, unsigned int *__restrict__ error,
+                    uint2 *__restrict__ pairs) {
+  __shared__ uint32_t tile[kBands * kTargetsPerBlock];
+  __shared__ uint32_t vals[kPairThreads / 32][32];
+  __shared__ uint32_t toff[kTargetsPerBlock];
+  __shared__ unsigned long long excl_sh;
+  __shared__ uint32_t blk_sh, ok_sh;
+  constexpr uint32_t kPer = kTargetsPerBlock / (kPairThreads / 32);  // targets per warp
+  if (threadIdx.x == 0) blk_sh = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const uint32_t blk = blk_sh, i0 = blk * kTargetsPerBlock;
+  const uint32_t nblocks = ceil_div(n, kTargetsPerBlock);
+  for (uint32_t e = threadIdx.x; e < bands * kTargetsPerBlock; e += kPairThreads) {
+    const uint32_t b = e / kTargetsPerBlock, c = e % kTargetsPerBlock;
+    tile[e] = (i0 + c < n) ? rep[(size_t)b * n + i0 + c] : 0u;
+  }
+  __syncthreads();
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  TargetScan ts[kPer];
+  uint32_t cand_sum = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kPer; ++k) {
+    const uint32_t c = warp + k * (kPairThreads / 32), i = i0 + c;
+    uint32_t u = 0;
+    if (i < n) {
+      ts[k] = scan_target(tile, c, i, lens, bands, t, vals[warp]);
+      cand_sum += ts[k].cand;
+      u = __popc(ts[k].first0) + __popc(ts[k].first1);
+    } else {
+      ts[k] = TargetScan{0u, 0u, 0u, 0u, 0u};
+    }
+    if (lane == 0) toff[c] = u;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t v = toff[lane];  // the block's 32 targets
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    toff[lane] = x - v;
+    const uint32_t agg = __shfl_sync(kFull, x, 31);
+    if (lane == 0) {
+      unsigned long long excl = 0;
+      uint32_t ok = 1;
+      if (blk == 0) {
+        atomicExch(status, kStIncl | agg);
+      } else {
+        atomicExch(status + blk, kStAgg | agg);
+        uint32_t spins = 0;
+        for (int j = (int)blk - 1; j >= 0;) {
+          const unsigned long long s = *(volatile unsigned long long *)(status + j);
+          if ((s >> 62) == 0) {
+            if (++spins > kLookbackSpins) {  // a predecessor never published
+              atomicOr(error, 1u);
+              ok = 0;
+              break;
+            }
+            continue;
+          }
+          excl += s & kStValue;
+          if ((s >> 62) == 2) break;
+          --j;
+        }
+        if (ok) atomicExch(status + blk, kStIncl | (excl + agg));
+      }
+      if (ok && blk + 1 == nblocks) *unique_total = excl + agg;
+      excl_sh = excl;
+      ok_sh = ok;
+    }
+  }
+  __syncthreads();
+  if (ok_sh) {
+    const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; ++k) {
+      const uint32_t c = warp + k * (kPairThreads / 32), i = i0 + c;
+      if (i >= n) continue;
+      const uint64_t base = excl_sh + toff[c];
+      if (ts[k].first0 >> lane & 1u)
+        pairs[base + __popc(ts[k].first0 & lt_mask)] = make_uint2(ts[k].v0, i);
+      if (ts[k].first1 >> lane & 1u)
+        pairs[base + __popc(ts[k].first0) + __popc(ts[k].first1 & lt_mask)] =
+            make_uint2(ts[k].v1, i);
+    }
+  }
+  if (lane == 0 && cand_sum) atomicAdd(cand_total, (unsigned long long)cand_sum);
+}
+
+int collect_scan(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
+                 uint32_t identity, unsigned int *ticket, unsigned long long *status,
+                 unsigned long long *cand_total, uint64_t *unique_total, unsigned int *error,
+                 uint2 *pairs, cudaStream_t s) {
+  if (n == 0) return NGIA_OK;
+  const uint32_t nblocks = ceil_div(n, kTargetsPerBlock);
+  NGIA_CUDA(cudaMemsetAsync(status, 0, (size_t)nblocks * 8, s));
+  collect_scan_kernel<<<nblocks, kPairThreads, 0, s>>>(rep, lens, n, bands,
+                                                       identity_threshold(identity), ticket,
+                                                       status, cand_total, unique_total, error,
+                                                       pairs);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
 int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
                   uint32_t identity, uint32_t *ucount, unsigned long long *cand_total,
                   cudaStream_t s) {
@@ -122,6 +245,8 @@ int collect_write(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_
 }
 
 // ---- width classes ------------------------------------------------------------------
+constexpr uint32_t kClassifyUnroll = 4;
+
 __global__ void __launch_bounds__(256)
 classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pairs,
                 uint64_t count, float t, int fma_mode, ClassPlan plan,
@@ -135,25 +260,42 @@ classify_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pai
   __syncthreads();
   unsigned long long my_cells = 0;
   const uint32_t lt_mask = (1u << (threadIdx.x & 31u)) - 1u;
-  // block-uniform trips, so that the class counts can be summed per warp
-  for (uint64_t p0 = (uint64_t)blockIdx.x * blockDim.x; p0 < count;
-       p0 += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t p = p0 + threadIdx.x;
-    uint32_t c = kFull;
-    if (p < count) {
-      const uint2 pr = pairs[p];
-      if (pr.x == kFull) {  // an empty pair slot (serving): never aligned
-        c = kSkipClass;
-        cls[p] = skip_sort_key();
-      } else {
-        const Band b = make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode);
-        c = (uint32_t)width_class(b, plan);
-        cls[p] = class_sort_key((int)c, b);
-        my_cells += band_blocks(b);
-      }
+  // block-uniform trips of kClassifyUnroll pairs per thread (their loads in
+  // flight together), so that the class counts can be summed per warp
+  constexpr uint32_t U = kClassifyUnroll;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t p0 = (uint64_t)blockIdx.x * blockDim.x; p0 < count; p0 += U * stride) {
+    uint2 pr[U];
+#pragma unroll
+    for (uint32_t u = 0; u < U; ++u) {
+      const uint64_t p = p0 + u * stride + threadIdx.x;
+      pr[u] = p < count ? pairs[p] : make_uint2(kFull, kFull);
     }
-    const uint32_t peers = __match_any_sync(kFull, c);
-    if (c != kFull && (peers & lt_mask) == 0) atomicAdd(&sc[c], (unsigned int)__popc(peers));
+    uint32_t lr[U], lt[U];
+#pragma unroll
+    for (uint32_t u = 0; u < U; ++u) {
+      const bool real = pr[u].x != kFull;
+      lr[u] = real ? __ldg(lens + pr[u].x) : 0u;
+      lt[u] = real ? __ldg(lens + pr[u].y) : 0u;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < U; ++u) {
+      const uint64_t p = p0 + u * stride + threadIdx.x;
+      uint32_t c = kFull;
+      if (p < count) {
+        if (pr[u].x == kFull) {  // an empty pair slot (serving): never aligned
+          c = kSkipClass;
+          cls[p] = skip_sort_key();
+        } else {
+          const Band b = make_band(lr[u], lt[u], t, fma_mode);
+          c = (uint32_t)width_class(b, plan);
+          cls[p] = class_sort_key((int)c, b);
+          my_cells += band_blocks(b);
+        }
+      }
+      const uint32_t peers = __match_any_sync(kFull, c);
+      if (c != kFull && (peers & lt_mask) == 0) atomicAdd(&sc[c], (unsigned int)__popc(peers));
+    }
   }
   atomicAdd(&scells, my_cells);
   __syncthreads();

@@ -38,6 +38,7 @@ struct Counters {  // device-side counters of one graph build or round
   unsigned long long work;  // 32x32 blocks the aligners computed
   unsigned int cursor[kNumClasses];  // pairs taken from each class's queue
   uint32_t bounds[kNumClasses + 1];  // class ranges of the queue order
+  unsigned int collect_ticket, collect_error;  // the one-pass candidate collection
 };
 
 // The records the aligners read (one index space: offs[i], lens[i]).
