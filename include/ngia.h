@@ -252,7 +252,8 @@ int ngia_pack_records(const uint8_t *h_residues, uint64_t residue_bytes,
  * The graph build of ngia_ctx_group_align (sketch + bucket of `bands` rows,
  * candidates, batched alignment, sorted unique edges) for records held in
  * host memory, streamed through at most `chunk_bytes` of device memory for
- * records (three chunk slots of planes, nibble codes and recoded codes; the
+ * records (three chunk slots of planes, nibble codes -- recoded ones while
+ * aligning -- and code planes; the
  * rest -- signatures, rep rows, lengths, offsets, pairs, scores -- grows with
  * the record count only and stays on the device).  The records pass through
  * pinned double-buffered copies twice: once to sketch them, once per block

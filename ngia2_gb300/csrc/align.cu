@@ -201,30 +201,8 @@ nibble_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ 
   if (lane == 0 && mine) atomicOr(presence, mine);
 }
 
-// Rewrites nibble codes through a 16-entry map (map nibble c = new code of c).
-__global__ void __launch_bounds__(256)
-recode_kernel(const uint32_t *__restrict__ nib, const uint64_t *__restrict__ offs, uint32_t n,
-              uint64_t map, uint32_t *__restrict__ out) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-    const uint64_t o = offs[i];
-    const uint32_t len = __ldg(nib + o);
-    if (lane == 0) out[o] = len;
-    const uint32_t words = ((len + 31) >> 5) * 4;
-    for (uint32_t w = lane; w < words; w += 32) {
-      const uint32_t x = __ldg(nib + o + 1 + w);
-      uint32_t y = 0;
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-        y |= (uint32_t)((map >> (4 * ((x >> (4 * j)) & 15u))) & 15u) << (4 * j);
-      out[o + 1 + w] = y;
-    }
-  }
-}
-
 // Recoded databases from their packed planes, in one pass: the aligner-code
-// nibbles (as recode_kernel writes them) and the planes of the aligner codes
+// nibbles (each residue code c replaced by map nibble c) and the planes of the aligner codes
 // (planes 0-2, plane 3 zero).  bits[b] = the residue codes whose aligner code
 // has bit b set.
 __global__ void __launch_bounds__(256)
@@ -273,18 +251,6 @@ int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uin
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
   if (!accumulate) NGIA_CUDA(cudaMemsetAsync(presence, 0, sizeof(uint32_t), s));
   nibble_kernel<<<want < cap ? want : cap, 256, 0, s>>>(packed, offs, n, nib, presence);
-  NGIA_LAUNCHED();
-  return NGIA_OK;
-}
-
-int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
-                  uint32_t *out, cudaStream_t s) {
-  if (n == 0) return NGIA_OK;
-  int dev = 0, sms = 0;
-  NGIA_CUDA(cudaGetDevice(&dev));
-  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
-  recode_kernel<<<want < cap ? want : cap, 256, 0, s>>>(nib, offs, n, map, out);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

@@ -79,10 +79,8 @@ int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n
 // presence |= the codes seen (cleared first unless accumulate)
 int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
                    uint32_t *presence, cudaStream_t s, bool accumulate = false);
-int launch_recode(const uint32_t *nib, const uint64_t *offs, uint32_t n, uint64_t map,
-                  uint32_t *out, cudaStream_t s);
 // Packed records and a code map with new codes 0..7 -> the recoded nibbles
-// (as launch_recode of their nibbles) and the planes of the new codes
+// (residue code c -> map nibble c) and the planes of the new codes
 // (Alphabet::dplanes), in one pass.
 int launch_dense_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n,
                          uint64_t map, uint32_t *dense_nib, uint32_t *dplanes,
