@@ -342,17 +342,27 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
                                 cudaMemcpyHostToDevice, c->copy));
     NGIA_CUDA(cudaEventRecord(c->chunk_ev[k], c->copy));
   }
-  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  // each piece's layouts on their own stream right behind its copy, so they
+  // can run while the main stream sketches the previous piece
   const uint64_t *offs = c->offs.as<uint64_t>();
   for (int k = C - 1; k >= 0; --k) {
     const uint32_t r0 = first[k], cnt = first[k + 1] - first[k];
-    NGIA_CUDA(cudaStreamWaitEvent(s, c->chunk_ev[k], 0));
+    NGIA_CUDA(cudaStreamWaitEvent(c->layout, c->chunk_ev[k], 0));
+    if (cnt) {
+      const uint64_t w0 = k == 0 ? 0 : (first[k] < n ? h_offs[first[k]] : words);
+      const uint64_t w1 = k + 1 == C ? words : (first[k + 1] < n ? h_offs[first[k + 1]] : words);
+      NGIA_TRY(launch_load_layouts(packed, offs + r0, cnt, w0, w1, spec.inv,
+                                   c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
+                                   c->dplanes.as<uint32_t>(), c->presence.as<uint32_t>(),
+                                   c->layout));
+    }
+    NGIA_CUDA(cudaEventRecord(c->layout_ev[k], c->layout));
+  }
+  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  for (int k = C - 1; k >= 0; --k) {
+    const uint32_t r0 = first[k], cnt = first[k + 1] - first[k];
+    NGIA_CUDA(cudaStreamWaitEvent(s, c->layout_ev[k], 0));
     if (cnt == 0) continue;
-    const uint64_t w0 = k == 0 ? 0 : (first[k] < n ? h_offs[first[k]] : words);
-    const uint64_t w1 = k + 1 == C ? words : (first[k + 1] < n ? h_offs[first[k + 1]] : words);
-    NGIA_TRY(launch_load_layouts(packed, offs + r0, cnt, w0, w1, spec.inv,
-                                 c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
-                                 c->dplanes.as<uint32_t>(), c->presence.as<uint32_t>(), s));
     NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(), offs + r0,
                                  cnt, spec.inv, c->sketch_table.p, c->sigs.as<uint32_t>() + r0,
                                  n, s, c->side, c->ev[6], nullptr));
@@ -423,8 +433,11 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
   for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
-  for (int k = 0; k < ngia_ctx::kLoadChunks && e == cudaSuccess; ++k)
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->layout, cudaStreamNonBlocking);
+  for (int k = 0; k < ngia_ctx::kLoadChunks && e == cudaSuccess; ++k) {
     e = cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->layout_ev[k], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     ngia_ctx_destroy(c);
     return ngia::cuda_fail(e);
@@ -452,7 +465,10 @@ void ngia_ctx_destroy(ngia_ctx *c) {
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->side) cudaStreamDestroy(c->side);
   if (c->copy) cudaStreamDestroy(c->copy);
+  if (c->layout) cudaStreamDestroy(c->layout);
   for (cudaEvent_t e : c->chunk_ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->layout_ev)
     if (e) cudaEventDestroy(e);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;

@@ -12,8 +12,8 @@ struct ngia_ctx {
   // pipelined loads (ngia_ctx_run_host): chunks of the records copied on `copy`
   // while the previous chunks are sketched on `stream`
   static constexpr int kLoadChunks = 8;  // at most
-  cudaStream_t copy = nullptr;
-  cudaEvent_t chunk_ev[kLoadChunks] = {};
+  cudaStream_t copy = nullptr, layout = nullptr;  // copies; each piece's layouts
+  cudaEvent_t chunk_ev[kLoadChunks] = {}, layout_ev[kLoadChunks] = {};
   uint32_t last_present = 0;  // residue codes of the previous load (0: none yet)
   // resident database
   uint32_t n = 0;
