@@ -64,7 +64,7 @@ SKETCH_ALU_OPS_PER_HASH = 10
 # to a full launch by the units it processes (both grow in proportion).
 SKETCH_DRAM_BYTES_PER_POSITION = 0.553
 SKETCH_TABLE_DRAM_BYTES_PER_POSITION = 0.537  # sketch_rank_kernel, per signed position
-ALIGN_DRAM_BYTES_PER_CELL = 5.9e-4
+ALIGN_DRAM_BYTES_PER_CELL = 1.13e-3  # all width classes of one step (profiles/align_*)
 # The reference's host code clusters about 650 families (6,500 sequences) of
 # this generator per second on 16 Grace cores; samples are sized from that.
 CPU_FAMILIES_PER_S = 650
