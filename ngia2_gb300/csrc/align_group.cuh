@@ -33,10 +33,16 @@
 //
 // Early exit.  With a zero carry into the band's lowest row, a column step
 // never lowers the number of zeros below any row, and the total rises by at
-// most one per column.  So the zeros of all slices, each counted after its own
-// latest column block, bound the LCS after column c_top of the highest slice
-// entered so far, and that plus the columns left bounds the final LCS: once
-// that bound fails the identity test the score is 0.
+// most one per column.  Let qhi be the highest slice with rows in the band and
+// c the column where slice qhi + 1 stands (one block behind qhi): at c no row
+// above slice qhi is in the band, so the zeros of the slices through any row
+// j, each counted after its own latest block, bound the banded LCS through
+// row j at c (the slices below run ahead).  (At qhi's own column that fails:
+// the next slice's rows may have entered there, all rs words of them at the
+// first block, uncounted.)  The final LCS then stays within
+//   max over rows j of  zeros through j + min(columns after c, Lr - j),
+// taken per word (zeros through its last row, rows above its first) plus the
+// retired rows' term; once that fails the identity test the score is 0.
 #pragma once
 
 #include "align_lds.cuh"
@@ -99,6 +105,42 @@ __device__ __forceinline__ uint32_t group_max(uint32_t v) {
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
   return v;
+}
+
+// The early-exit bound of the group's pair (every lane of the warp calls it;
+// the values of groups without a pair are never used).  The lanes hold G
+// consecutive slices, slice q in lane q % G: the lowest is the one whose ring
+// neighbour below does not hold q - 1, and a lane's rank is its distance
+// above it.  Suffix sums of the live zeros by rank give each lane the zeros of
+// every row below its slice (S holds all of them plus the retired rows'), and
+// each of its words bounds the LCS through its rows plus min(left, rows above
+// its first row); the lowest lane adds the retired rows' term.
+template <int G, int K>
+__device__ __forceinline__ uint32_t group_row_bound(const uint32_t (&V)[K], uint32_t q,
+                                                    uint32_t lane, uint32_t sub, uint32_t src,
+                                                    uint32_t S, uint32_t live, uint32_t left,
+                                                    uint32_t lr) {
+  constexpr uint32_t kGroupBits = G == 32 ? kFull : (1u << G) - 1u;
+  const bool lowest = __shfl_sync(kFull, q, src) != q - 1u;
+  const uint32_t bits = (__ballot_sync(kFull, lowest) >> (lane - sub)) & kGroupBits;
+  const uint32_t low = (uint32_t)(__ffs(bits) - 1) & (uint32_t)(G - 1);
+  const uint32_t rank = (sub + G - low) % G;
+  uint32_t above = live;  // live zeros of this slice and the ones above it
+#pragma unroll
+  for (int o = 1; o < G; o <<= 1) {
+    const uint32_t v = __shfl_sync(kFull, above, lane - sub + (sub + o) % G);
+    if (rank + o < (uint32_t)G) above += v;
+  }
+  uint32_t acc = S - above;
+  uint32_t best = rank == 0 ? acc + min(left, lr) : 0u;
+  const uint32_t row0 = 32u * K * q;
+#pragma unroll
+  for (int m = 0; m < K; ++m) {
+    acc += __popc(~V[m]);
+    const uint32_t row = row0 + 32u * m;
+    best = max(best, acc + min(left, lr > row ? lr - row : 0u));
+  }
+  return group_max<G>(best);
 }
 
 // The persistent kernel body of one group class: groups take pairs from
@@ -262,13 +304,17 @@ __device__ inline uint32_t align_group(const uint32_t *__restrict__ packed,
     ++wstep;
     const bool last = active && tau + 1 >= tau_end;
     const bool check = (wstep & 3u) == 0 || __any_sync(kFull, last);
-    uint32_t S = 0, qhi1 = 0;
+    uint32_t S = 0, qhi1 = 0, ub = 0;
     if (check) {
-      uint32_t zl = zret;
+      uint32_t live = 0;
 #pragma unroll
-      for (int m = 0; m < K; ++m) zl += __popc(~V[m]);
-      S = group_sum<G>(zl);
+      for (int m = 0; m < K; ++m) live += __popc(~V[m]);
+      S = group_sum<G>(zret + live);
       qhi1 = group_max<G>((active && q < ns && e > 0) ? q + 1 : 0u);
+      // column blocks done where slice qhi + 1 stands (qhi + 1 <= tau + 1)
+      const uint32_t ref = qhi1 && qhi1 <= tau + 1 ? tau + 1 - qhi1 : 0u;
+      const uint32_t cols = 32 * ref < lt ? 32 * ref : lt;
+      ub = group_row_bound<G, K>(V, q, lane, sub, src, S, live, lt - cols, lr);
     }
     if (active) {
       ++tau;
@@ -277,9 +323,7 @@ __device__ inline uint32_t align_group(const uint32_t *__restrict__ packed,
       if (fin) {
         score = identity_score(S, lr, lt, t);
       } else if (check && qhi1) {
-        const uint32_t blocks = tau - (qhi1 - 1);  // column blocks done by the top slice
-        const uint32_t cols = 32 * blocks < lt ? 32 * blocks : lt;
-        fin = !stream_may_reach(S, cols, lr, lt, t);
+        fin = !lcs_may_reach(ub, lr, lt, t);
       }
       if (fin) {
         if (sub == 0) scores[p] = score;

@@ -98,6 +98,41 @@ def test_batched_pairs_match_oracle(cuda, built, identity):
     assert classes & set(range(11, 17)), sorted(classes)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("identity", [50, 90])
+def test_group_exit_when_the_path_runs_high(cuda, built, identity):
+    """Targets that are a suffix of their rep, just above the identity cut:
+    the LCS path runs Lr - Lt rows above the diagonal, near the band's upper
+    edge, where rows enter the band before the slice holding them has run its
+    first block.  The early exit must not end such pairs: scores equal the
+    oracle's with the default plan and with narrow bands sent to the group
+    classes."""
+    from gpu_util import build_db
+    rng = np.random.default_rng(4242 + identity)
+    seqs: list[bytes] = []
+    pairs = []
+    for _ in range(400):
+        lr = int(rng.integers(200, 1500))
+        lt = min(lr, int(np.ceil(lr * identity / 100 * rng.uniform(1.005, 1.08))))
+        rep = synth._draw(rng, synth.AMINO, synth.AMINO_FREQ, lr).tobytes()
+        seqs += [rep, rep[lr - lt:]]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    pairs = np.array(pairs, np.uint32)
+    packed, offs, lens = build_db(seqs)
+    want = oracle.align_pairs(packed, offs, pairs, identity, oracle.ROUND_FMA)
+    assert (want > 0).mean() > 0.9
+    with ng.Context() as ctx:
+        ctx.load(packed, offs, lens)
+        default = ctx.plan()
+        for plan in (default, {"stream_max": 4, "group_limit": default["group_limit"]}):
+            ctx.set_plan(plan)
+            got, _ = ctx.align_pairs(pairs, identity)
+            bad = np.nonzero(got != want)[0]
+            assert len(bad) == 0, (plan["stream_max"], [
+                (int(lens[pairs[i, 0]]), int(lens[pairs[i, 1]]), int(got[i]), int(want[i]))
+                for i in bad[:8]])
+
+
 def test_every_group_class_is_covered(built):
     """Across the identities above, every class is reached (host-side check
     of the test data, no GPU)."""
