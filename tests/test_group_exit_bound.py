@@ -16,7 +16,9 @@ This restates the banded recurrence (rows i - ls .. i + rs of column block i,
 retired rows frozen), replays the group's lanes on its per-block states -- the
 slice walk, the retirements, the ring-neighbour test, the ballot, the suffix
 scan by rank -- and checks at every step that the bound never falls below the
-final LCS, and never rises above the whole-band bound it replaces.  No GPU."""
+final LCS, and never rises above the whole-band bound it replaces.  The replay
+also checks the binning's premise: within a class's limit every slice with rows
+in the band is the one its lane holds.  No GPU."""
 from __future__ import annotations
 
 import math
@@ -116,6 +118,14 @@ def replay(rep, tar, t, G, K):
                     e[l] = max(e[l], min(j1 - lo, K))
                     for m in range(r[l], e[l]):
                         V[l][m] = word(i, lo + m)
+        # one live slice per lane: every slice with rows in the band at its
+        # block is the one its lane holds (the class limits guarantee it)
+        for s in range(ns):
+            i = tau - s
+            if 0 <= i < nc:
+                j0 = i - ls if i > ls else 0
+                if max(j0, s * K) < min(i + rs, nr, s * K + K):
+                    assert q[s % G] == s, (tau, s, q)
         live = [sum(zeros(v) for v in V[l]) for l in range(G)]
         S = sum(zret) + sum(live)
         qhi1 = max((q[l] + 1) if (q[l] < ns and e[l] > 0) else 0 for l in range(G))
