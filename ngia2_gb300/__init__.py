@@ -540,9 +540,12 @@ def read_packed(path) -> dict:
     pack_off = raw[o:o + 8 * n].view(np.uint64); o += 8 * n
     fasta_off = raw[o:o + 8 * n].view(np.uint64); o += 8 * n
     rep = raw[o:o + 4 * BANDS * n].view(np.uint32).reshape(BANDS, n); o += 4 * BANDS * n
-    p0, f0 = int(pack_off[0]), int(fasta_off[0])
-    packed = raw[p0:f0].view(np.uint32)
-    offsets = ((pack_off - np.uint64(p0)) // np.uint64(4)).astype(np.uint64)
+    if n == 0:  # a database with no records: the count and nothing else
+        packed, offsets = np.zeros(0, np.uint32), np.zeros(0, np.uint64)
+    else:
+        p0, f0 = int(pack_off[0]), int(fasta_off[0])
+        packed = raw[p0:f0].view(np.uint32)
+        offsets = ((pack_off - np.uint64(p0)) // np.uint64(4)).astype(np.uint64)
     return {"n": n, "name_lens": name_lens, "lens": lens, "pack_off": pack_off,
             "fasta_off": fasta_off, "rep": rep, "packed": packed, "offsets": offsets,
             "raw": raw}

@@ -94,6 +94,14 @@ def test_read_packed_layout(golden):
         assert np.all(rep <= np.arange(n))
 
 
+def test_read_packed_without_records(tmp_path):
+    path = tmp_path / "empty.packed"
+    path.write_bytes(np.zeros(1, np.uint32).tobytes())
+    db = ng.read_packed(path)
+    assert db["n"] == 0 and db["packed"].size == 0 and db["offsets"].size == 0
+    assert db["rep"].shape == (ng.BANDS, 0)
+
+
 def run_cli(*args):
     return subprocess.run([str(ng.CLI_PATH), *args], capture_output=True, text=True,
                           timeout=60)
