@@ -38,8 +38,8 @@
 // above slice qhi is in the band, so the zeros of the slices through any row
 // j, each counted after its own latest block, bound the banded LCS through
 // row j at c (the slices below run ahead).  (At qhi's own column that fails:
-// the next slice's rows may have entered there, all rs words of them at the
-// first block, uncounted.)  The final LCS then stays within
+// rows of the slices above may be in the band there uncounted -- at a pair's
+// first block every row word below rs.)  The final LCS then stays within
 //   max over rows j of  zeros through j + min(columns after c, Lr - j),
 // taken per word (zeros through its last row, rows above its first) plus the
 // retired rows' term; once that fails the identity test the score is 0.
