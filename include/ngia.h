@@ -160,8 +160,9 @@ void ngia_ctx_destroy(ngia_ctx *ctx);
  * The records are trusted as a packed file's are: record i starts at word
  * h_rec_offsets[i] with its length word equal to h_lens[i], and its
  * 1 + 4*ceil(len/32) words end inside the region (makedb's files and
- * ngia_pack_records' output are so; ngia_ctx_load_packed_file checks it).
- * The same holds for ngia_ctx_run_host and ngia_stream_graph. */
+ * ngia_pack_records' output are so; ngia_ctx_load_packed_file checks the
+ * offsets against the read lengths, not the length words).  The same holds
+ * for ngia_ctx_run_host and ngia_stream_graph. */
 int ngia_ctx_load(ngia_ctx *ctx, const uint32_t *h_packed, uint64_t packed_words,
                   const uint64_t *h_rec_offsets, const uint32_t *h_lens,
                   uint32_t n, const uint32_t *h_rep, uint32_t bands);
