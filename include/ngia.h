@@ -319,7 +319,9 @@ typedef struct ngia_request_stats {
 int ngia_server_create(ngia_server **srv, ngia_ctx *db, const uint32_t *h_cluster,
                        const ngia_server_config *cfg);
 /* Queues a request (the arrays are copied before return): count packed
- * records (h_offs: word offset of each in h_packed, h_lens: lengths). */
+ * records (h_offs: word offset of each in h_packed, h_lens: lengths).  Each
+ * record is checked: inside the words given (else NGIA_ERR_ARG), its length
+ * word equal to h_lens[i] (else NGIA_ERR_FORMAT). */
 int ngia_server_submit(ngia_server *srv, const uint32_t *h_packed, uint64_t words,
                        const uint64_t *h_offs, const uint32_t *h_lens, uint32_t count,
                        uint64_t *ticket);
