@@ -80,12 +80,35 @@ PAIRS_MAX_STEPS = 5
 SERVE_DB, SERVE_QUERIES, SERVE_FAMILIES, SERVE_SEED, SERVE_IDENTITY = (
     2_000_000, 300_000, 100_000, 4, 90)
 SERVE_MAX_BATCH, SERVE_SLOTS, SERVE_LOAD, SERVE_REPLAY = 50_000, 8, 3.0, 10
+# Small requests first: requests of at most SERVE_SMALL queries are admitted
+# ahead of larger ones, with SERVE_SMALL_SLOTS of the slots kept for them.
+SERVE_SMALL, SERVE_SMALL_SLOTS = 256, 2
+# Request-size buckets of the latency split (queries per request).
+SERVE_SIZE_BUCKETS = ((1, 9), (10, 99), (100, 999), (1000, 9999), (10000, 50000))
+# A second serving workload whose queries are close relatives of database
+# sequences (families with 0-4 % substitutions and 0.5 % indels of mean 2),
+# so that alignment and assignment, not the lookup, dominate.
+SERVE_CLOSE_SEED, SERVE_CLOSE_SUBS, SERVE_CLOSE_INDELS = 6, (0.0, 0.04), (0.005, 2.0)
 # Streaming leg: a protein database held in host memory (the small-protein
 # generator, 12 sequences per family) clustered through 1 GiB of device memory
 # for records, 3 rehash rounds at identities 50 and 90; the out-of-HBM
 # configuration names 60,000,000 sequences (--stream-seqs 60000000).
 STREAM_SEQS, STREAM_PER_FAMILY, STREAM_SEED, STREAM_BANDS = 6_000_000, 12, 5, 3
 STREAM_IDENTITIES, STREAM_CHUNK_BYTES = (50, 90), 1 << 30
+# The same device step on the small protein configuration: 20,000 proteins
+# from 2,000 families (log-normal roots median 300 sigma 0.5, 5-35 % substitutions,
+# 2 % indels, seed 1) at identity 90.
+PROT_SEQS, PROT_FAMILIES, PROT_SEED, PROT_IDENTITY = 20_000, 2_000, 1, 90
+# The command line end to end (FASTA -> packed file -> result file) against the
+# reference's own GPU build on the same GPU: both configurations, median of
+# REFGPU_REPS runs of each command.
+REFGPU_REPS = 3
+# The bit-parallel LCS update counted the survey's way: AND, add with carry in,
+# carry out, AND-NOT, OR per 32 cells.
+ALIGN_OPS_PER_WORD_STEP_5 = 5
+# Single-thread row of the CPU baseline: families of the sample (about 10 s of
+# the reference's host code on one core).
+CPU_SAMPLE_FAMILIES_1T = 500
 
 
 def log(*a):
@@ -122,6 +145,12 @@ def parse():
                    help="1: compare the streamed edges with the resident path's")
     p.add_argument("--stream-chunk-bytes", type=int, default=STREAM_CHUNK_BYTES,
                    help="device bytes for record chunks in the streaming leg")
+    p.add_argument("--protein", type=int, default=1,
+                   help="1: the device step on the small protein configuration too")
+    p.add_argument("--reference-gpu", type=int, default=1,
+                   help="1: the command line end to end against the reference's GPU build")
+    p.add_argument("--ref-gpu-only", action="store_true",
+                   help="run only the command-line comparison and print its object")
     return p.parse_args()
 
 
@@ -457,12 +486,10 @@ def run_ours(args, world, rank, local, pg):
     rs = {
         "sketch": sketch_roof,
         # the align phase: one launch per populated width class, timed as a whole
-        "align": roof("align phase (align_stream_kernel / align_group_kernel / align_general_kernel per width class)",
-                      cells / 32 * ALIGN_OPS_PER_WORD_STEP, align_ms, cells, "computed_cells",
-                      ALIGN_DRAM_BYTES_PER_CELL,
-                      # the pair list and scores once + every record's codes once
-                      st["unique_pairs"] * 12 + int(db["lens"].sum()) / 2, 1),
+        "align": align_roof(roof, cells, align_ms, int_peak,
+                            st["unique_pairs"] * 12 + int(db["lens"].sum()) / 2),
     }
+    rs.update(hbm_rooflines(stats, st, n, hbm))
     dominant = max(rs, key=lambda k: rs[k]["ms"])
     line = {
         "metric": "seqs clustered/s", "value": world * n / (mean_ms_max * 1e-3),
@@ -496,12 +523,20 @@ def run_ours(args, world, rank, local, pg):
         "hbm_peak_gbs": peaks().get("hbm_gbs"),
     }
     ctx.close()
+    if world == 1 and args.protein:
+        # the same device step on the small protein configuration at identity 90
+        line["protein"] = run_protein(args, int_peak, hbm)
+    if world == 1 and args.reference_gpu:
+        # the command line end to end against the reference's own GPU build
+        line["reference_gpu"] = run_reference_gpu(fasta)
     if world == 1 and args.pairs > 0:
         # the batched-vs-plain leg on heavy-tailed protein pairs (one GPU)
         line["pairs"] = run_pairs(args)
     if world == 1 and args.serve_db > 0:
-        # the serving leg: continuous batching vs per-request plain runs
+        # the serving leg: continuous batching vs per-request plain runs, on the
+        # serving configuration and on queries that are close relatives
         line["serving"] = run_serving(args)
+        line["serving_close"] = run_serving(args, close=True)
     if world == 1 and args.stream_seqs > 0:
         # the streaming leg: records in host memory, a bounded device budget
         line["stream"] = run_stream(args)
@@ -512,7 +547,228 @@ def run_ours(args, world, rank, local, pg):
             line["cpu_baseline"] = run_cpu_baseline(workdir, 1, 0, fam)
         except Exception as e:  # reported, never silently dropped
             line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+        try:
+            # the same code on one core, on a smaller sample
+            line["cpu_baseline"]["single_thread"] = run_cpu_single_thread(workdir)
+        except Exception as e:
+            line["cpu_baseline"]["single_thread"] = {"value": None, "error": str(e)[:200]}
     return line
+
+
+def align_roof(roof, cells, align_ms, int_peak, algo_bytes) -> dict:
+    """The align phase against the integer-logic peak, with both op counts per
+    32 cells: 3 (the update's irreducible ops) and 5 (each of AND, add with
+    carry in, carry out, AND-NOT, OR counted)."""
+    r = roof("align phase (align_stream_kernel / align_group_kernel / align_general_kernel "
+             "per width class)", cells / 32 * ALIGN_OPS_PER_WORD_STEP, align_ms, cells,
+             "computed_cells", ALIGN_DRAM_BYTES_PER_CELL, algo_bytes, 1)
+    ops5 = cells / 32 * ALIGN_OPS_PER_WORD_STEP_5
+    r["ops_per_word_step"] = ALIGN_OPS_PER_WORD_STEP
+    r["frac_5_ops_per_word_step"] = ops5 / (align_ms * 1e-3) / int_peak
+    return r
+
+
+def hbm_rooflines(stats, st, n, hbm) -> dict:
+    """Bucketing and emission against the measured HBM bandwidth: bucketing
+    reads each band's signatures and writes its rep row (4 + 4 bytes per
+    sequence and band, 512 per sequence over 64 bands); emission reads each
+    distinct pair and its score (8 + 4 bytes) and writes each edge (12 bytes)."""
+    out = {}
+    for name, ms_key, algo, kernel in (
+            ("bucket", "ms_bucket", 8 * BANDS * n,
+             "rs_hist/rs_scatter (segmented radix sort) + rep_chain_kernel"),
+            ("emit", "ms_emit", 12 * st["unique_pairs"] + 12 * st["edges"],
+             "emit_sorted (run counts, ordered compaction, radix sort by rep)")):
+        ms = statistics.mean(s[ms_key] for s in stats)
+        achieved = algo / (ms * 1e-3) if ms > 0 else 0.0
+        out[name] = {"bound": "hbm", "kernel": kernel, "achieved": achieved / 1e9,
+                     "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / (hbm * 1e9) if hbm else None,
+                     "peak_source": "measured: MEASURED_PEAKS hbm_gbs", "ms": ms,
+                     "algorithmic_bytes": algo, "traffic": None}
+    return out
+
+
+def run_cpu_single_thread(workdir: Path) -> dict:
+    """The reference's host build (makedb + clustering through its command
+    line) with one OpenMP thread, on a sample of the workload's generator."""
+    import oracle
+    cli = oracle.REF / "ngia2_cpu_fma"
+    if not cli.exists():
+        return {"value": None, "error": "reference host build missing"}
+    fasta, n = cpu_sample(CPU_SAMPLE_FAMILIES_1T, workdir)
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    t0 = time.perf_counter()
+    for cmd in (["-m", "makedb", "-f", fasta, "-p", workdir / "st.packed"],
+                ["-m", "clustering", "-p", workdir / "st.packed", "-r", workdir / "st.txt",
+                 "-i", str(IDENTITY), "-b", str(BANDS)]):
+        subprocess.run([str(cli), *map(str, cmd)], check=True, capture_output=True, env=env,
+                       timeout=600)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "seqs/s", "cores": 1, "kind": "reference",
+            "sample": f"{n} sequences ({CPU_SAMPLE_FAMILIES_1T} families) of the same generator, "
+                      f"identity {IDENTITY}, {BANDS} bands; makedb + clustering (align, "
+                      "Leiden, result file) through the reference's command line",
+            "seconds": dt}
+
+
+def run_protein(args, int_peak, hbm) -> dict:
+    """The device step (sketch, bucket, candidates, align, emit) on the small
+    protein configuration at identity 90, database resident, L2 flushed before
+    every step."""
+    import torch
+
+    import ngia2_gb300 as ng
+    from ngia2_gb300 import synth
+    workdir = Path(tempfile.mkdtemp(prefix="ngia_prot_"))
+    fa, packed = workdir / "prot.fa", workdir / "prot.packed"
+    synth.protein_families(PROT_SEQS, PROT_FAMILIES, PROT_SEED).write_fasta(fa)
+    ng.makedb(fa, packed)
+    db = ng.read_packed(packed)
+    n = db["n"]
+    stream = torch.cuda.Stream()
+    ctx = ng.Context(stream.cuda_stream)
+    ctx.load(db["packed"], db["offsets"], db["lens"])
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = ctx.group_align(PROT_IDENTITY, BANDS)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b), out
+
+    for _ in range(max(3, args.warmup)):
+        timed()
+    ms, stats = [], []
+    for _ in range(args.steps):
+        t, (_, st) = timed()
+        ms.append(t)
+        stats.append(st)
+    ctx.close()
+    st = stats[-1]
+    mean_ms = statistics.mean(ms)
+    align_ms = statistics.mean(s["ms_align"] for s in stats)
+    sketch_ms = statistics.mean(s["ms_sketch"] for s in stats)
+    positions = signed_positions(db["lens"])
+    cells = st["computed_cells"]
+
+    def roof(kernel, ops, ms_, units, unit_name, bytes_per_unit, algo_bytes, launches_):
+        achieved = ops / (ms_ * 1e-3)
+        return {"bound": "int32_alu", "kernel": kernel, "achieved": achieved / 1e12,
+                "peak": int_peak / 1e12, "unit": "Tops/s (32-bit lane ops)",
+                "frac": achieved / int_peak, "units": {unit_name: units}, "ms": ms_,
+                "traffic": None, "algorithmic_bytes": algo_bytes}
+    rs = {"sketch": roof("sketch_kernel<NibbleKmers>", positions * BANDS * SKETCH_ALU_OPS_PER_HASH,
+                         sketch_ms, positions, "signed_positions", None,
+                         int(db["lens"].sum()) / 2 + 4 * BANDS * n, 1),
+          "align": align_roof(roof, cells, align_ms, int_peak,
+                              st["unique_pairs"] * 12 + int(db["lens"].sum()) / 2)}
+    rs.update(hbm_rooflines(stats, st, n, hbm))
+    return {"workload": f"protein_{n}_seqs_{PROT_FAMILIES}_families_id{PROT_IDENTITY}_{BANDS}bands",
+            "data": "synthetic: protein families (log-normal roots median 300 sigma 0.5 clipped "
+                    "50-1500, background amino-acid frequencies, 5-35% substitutions, 2% indels "
+                    "mean 3), shuffled, seed 1",
+            "metric": "seqs clustered/s", "value": n / (mean_ms * 1e-3), "unit": "seqs/s",
+            "ms_per_step": mean_ms, "steps": args.steps,
+            "stages_ms": {k: statistics.mean(s[k] for s in stats)
+                          for k in ("ms_sketch", "ms_bucket", "ms_pairs", "ms_align", "ms_emit")},
+            "work": {"candidate_pairs": st["candidate_pairs"], "unique_pairs": st["unique_pairs"],
+                     "band_cells": st["aligned_cells"], "computed_cells": cells,
+                     "edges": st["edges"]},
+            "rooflines": rs}
+
+
+def _timed_cli(cmd) -> tuple[float, str]:
+    t0 = time.perf_counter()
+    r = subprocess.run([str(c) for c in cmd], capture_output=True, text=True, timeout=1800)
+    dt = time.perf_counter() - t0
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd[0]} {cmd[1:3]} failed ({r.returncode}): {r.stdout[-400:]}")
+    return dt, r.stdout
+
+
+def _ref_timer(out: str, tag: str):
+    """Seconds of the reference's Timer line that follows `tag`."""
+    import re
+    m = re.search(re.escape(tag) + r"\s*Consuming:\s*(\d+) h\s*(\d+) m\s*(\d+) s\s*(\d+) ms"
+                  r"\s*(\d+) us", out)
+    if not m:
+        return None
+    h, mi, sec, ms, us = map(int, m.groups())
+    return h * 3600 + mi * 60 + sec + ms / 1e3 + us / 1e6
+
+
+def run_reference_gpu(dna_fasta: Path) -> dict:
+    """FASTA -> packed file -> result file through the command line, this
+    build against the reference's own GPU build (its src/main.cu built
+    unmodified by nvcc for this GPU), on the same GPU one process at a time:
+    makedb then -m clustering (the drop-in flow, two processes each), and this
+    build's one-process makedb+clustering.  Median wall time of REFGPU_REPS
+    runs per command; packed and result files compared byte for byte."""
+    import hashlib
+
+    import ngia2_gb300 as ng
+    import oracle
+    from ngia2_gb300 import synth
+    ref = oracle.ref_gpu_cli()
+    if not ref.exists():
+        return {"unavailable": "the reference GPU build (oracle/build.sh) is missing"}
+    sha = lambda p: hashlib.sha256(Path(p).read_bytes()).hexdigest()  # noqa: E731
+    workdir = Path(tempfile.mkdtemp(prefix="ngia_refgpu_"))
+    prot_fa = workdir / "prot.fa"
+    synth.protein_families(PROT_SEQS, PROT_FAMILIES, PROT_SEED).write_fasta(prot_fa)
+    configs = [("protein_20k_seqs_2k_families_id90", prot_fa, PROT_IDENTITY, PROT_SEQS),
+               (WORKLOAD, dna_fasta, IDENTITY, N_SEQS)]
+    out = {"gpu": "same GPU, one process at a time",
+           "reference": "src/main.cu built unmodified: nvcc -O3 -Xcompiler -fopenmp "
+                        "-gencode arch=compute_103,code=sm_103 (oracle/build.sh)",
+           "reps": REFGPU_REPS, "configs": {}}
+    for name, fa, identity, n in configs:
+        d = workdir / name
+        d.mkdir()
+        t = {k: [] for k in ("ref_makedb", "ref_clustering", "ours_makedb", "ours_clustering",
+                             "ours_one_process")}
+        ref_align = []
+        for _ in range(REFGPU_REPS):
+            dt, _ = _timed_cli([ref, "-m", "makedb", "-f", fa, "-p", d / "ref.packed"])
+            t["ref_makedb"].append(dt)
+            dt, o = _timed_cli([ref, "-m", "clustering", "-p", d / "ref.packed", "-r",
+                                d / "ref.txt", "-i", identity, "-b", BANDS])
+            t["ref_clustering"].append(dt)
+            ref_align.append(_ref_timer(o, f"[align {BANDS} bands]"))
+            dt, _ = _timed_cli([ng.CLI_PATH, "-m", "makedb", "-f", fa, "-p", d / "ours.packed"])
+            t["ours_makedb"].append(dt)
+            dt, _ = _timed_cli([ng.CLI_PATH, "-m", "clustering", "-p", d / "ours.packed", "-r",
+                                d / "ours.txt", "-i", identity, "-b", BANDS])
+            t["ours_clustering"].append(dt)
+            dt, _ = _timed_cli([ng.CLI_PATH, "-m", "makedb+clustering", "-f", fa, "-p",
+                                d / "one.packed", "-r", d / "one.txt", "-i", identity,
+                                "-b", BANDS])
+            t["ours_one_process"].append(dt)
+        med = {k: statistics.median(v) for k, v in t.items()}
+        ref_total = med["ref_makedb"] + med["ref_clustering"]
+        ours_total = med["ours_makedb"] + med["ours_clustering"]
+        ref_packed = sha(d / "ref.packed")
+        out["configs"][name] = {
+            "sequences": n, "identity": identity, "bands": BANDS,
+            "seconds_median": med,
+            "ref_align_seconds_median": statistics.median(a for a in ref_align if a is not None)
+            if any(a is not None for a in ref_align) else None,
+            "reference_seqs_per_s": n / ref_total,
+            "ours_seqs_per_s": n / ours_total,
+            "ours_one_process_seqs_per_s": n / med["ours_one_process"],
+            "e2e_ratio": ref_total / ours_total,
+            "e2e_ratio_one_process": ref_total / med["ours_one_process"],
+            "packed_identical": sha(d / "ours.packed") == ref_packed
+            and sha(d / "one.packed") == ref_packed,
+            "result_identical": sha(d / "ours.txt") == sha(d / "ref.txt")
+            and sha(d / "one.txt") == sha(d / "ref.txt"),
+        }
+    return out
 
 
 def reference_sample_families(steps: int, warmup: int) -> int:
@@ -750,21 +1006,24 @@ def run_stream(args) -> dict:
 
 
 # ---- serving: continuous batching vs per-request plain runs ---------------------------
-def make_serving(n_db: int, workdir: Path):
-    """Database (packed through makedb) and query records of the serving leg."""
+def make_serving(n_db: int, workdir: Path, close: bool = False):
+    """Database (packed through makedb) and query records of the serving leg;
+    close: the close-relatives workload."""
     import ngia2_gb300 as ng
     from ngia2_gb300 import synth
     t0 = time.time()
     scale = n_db / SERVE_DB
     n_q = max(1000, int(SERVE_QUERIES * scale))
     n_fam = max(100, int(SERVE_FAMILIES * scale))
+    seed = SERVE_CLOSE_SEED if close else SERVE_SEED
     cache = os.environ.get("NGIA_BENCH_CACHE")
     if cache:
-        workdir = Path(cache) / f"serve_{n_db}_{SERVE_SEED}"
+        workdir = Path(cache) / f"serve_{n_db}_{seed}"
         workdir.mkdir(parents=True, exist_ok=True)
     dbp, qp = workdir / "db.packed", workdir / "queries.packed"
     if not (cache and dbp.exists() and qp.exists()):
-        db, q = synth.serving_set(n_db, n_q, n_fam, seed=SERVE_SEED)
+        kw = {"subs": SERVE_CLOSE_SUBS, "indels": SERVE_CLOSE_INDELS} if close else {}
+        db, q = synth.serving_set(n_db, n_q, n_fam, seed=seed, **kw)
         db.write_fasta(workdir / "db.fa")
         q.write_fasta(workdir / "queries.fa")
         ng.makedb(workdir / "db.fa", dbp)
@@ -797,20 +1056,68 @@ def serving_requests(q, seed: int = SERVE_SEED):
     return reqs
 
 
-def run_serving(args) -> dict:
-    """p50/p99 latency and queries/s of the serving engine (continuous batching
-    over SERVE_SLOTS slots, Poisson arrivals at SERVE_LOAD x the plain form's
-    request rate) against the same requests run one at a time in the plain form;
-    per-request results compared."""
+def latency_split(sizes, lat_ms) -> dict:
+    """p50/p99 latency (ms) per request-size bucket."""
+    import numpy as np
+    sizes, lat_ms = np.asarray(sizes), np.asarray(lat_ms)
+    out = {}
+    for lo, hi in SERVE_SIZE_BUCKETS:
+        sel = (sizes >= lo) & (sizes <= hi)
+        if sel.any():
+            out[f"{lo}-{hi}"] = {"requests": int(sel.sum()),
+                                 "p50_ms": float(np.percentile(lat_ms[sel], 50)),
+                                 "p99_ms": float(np.percentile(lat_ms[sel], 99))}
+    return out
+
+
+def serve_poisson(srv, reqs, rate: float, seed: int):
+    """Requests submitted as Poisson arrivals at `rate` per second; returns the
+    per-request (results, stats) and the makespan (first submit -> last done)."""
     import threading
 
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=len(reqs))
+    tickets: list = [None] * len(reqs)
+    ready = [threading.Event() for _ in reqs]
+    results: list = [None] * len(reqs)
+    done_at = [0.0] * len(reqs)
+
+    def waiter():
+        for k in range(len(reqs)):
+            ready[k].wait()
+            results[k] = srv.wait(tickets[k], len(reqs[k][2]))
+            done_at[k] = time.perf_counter()
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t_begin = time.perf_counter()
+    t_next = t_begin
+    for k, r in enumerate(reqs):
+        t_next += gaps[k]
+        delay = t_next - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        tickets[k] = srv.submit(*r)
+        ready[k].set()
+    th.join()
+    return results, max(done_at) - t_begin
+
+
+def run_serving(args, close: bool = False) -> dict:
+    """p50/p99 latency (overall and per request size) and queries/s of the
+    serving engine (continuous batching over SERVE_SLOTS slots, Poisson
+    arrivals at SERVE_LOAD x the plain form's request rate), in arrival order
+    and with small requests first, against the same requests run one at a
+    time in the plain form; per-request results compared."""
     import numpy as np
     import torch
 
     import ngia2_gb300 as ng
     workdir = Path(tempfile.mkdtemp(prefix="ngia_serve_"))
-    db, q = make_serving(args.serve_db, workdir)
+    db, q = make_serving(args.serve_db, workdir, close)
     reqs = serving_requests(q) * SERVE_REPLAY  # the stream, replayed
+    sizes = [len(r[2]) for r in reqs]
     stream = torch.cuda.Stream()
     ctx = ng.Context(stream.cuda_stream)
     ctx.load(db["packed"], db["offsets"], db["lens"])
@@ -818,7 +1125,7 @@ def run_serving(args) -> dict:
     ctx.sketch_bucket(BANDS)
     cluster = ctx.fast_cluster(SERVE_IDENTITY)  # the database's clusters (fast mode)
     t_setup = time.time() - t0
-    nq = sum(len(r[2]) for r in reqs)
+    nq = sum(sizes)
 
     # plain: one request at a time, plain kernel, no overlap
     plain_out, plain_ms = [], []
@@ -832,67 +1139,54 @@ def run_serving(args) -> dict:
         plain_s = time.perf_counter() - t_begin
     plain_rate = len(reqs) / plain_s
 
-    # serving: Poisson arrivals at SERVE_LOAD x the plain request rate
-    rng = np.random.default_rng(SERVE_SEED + 11)
-    gaps = rng.exponential(1.0 / (SERVE_LOAD * plain_rate), size=len(reqs))
-    with ng.Server(ctx, cluster, SERVE_IDENTITY, slots=SERVE_SLOTS,
-                   max_queries=SERVE_MAX_BATCH) as srv:
-        srv.wait(srv.submit(*reqs[0]), len(reqs[0][2]))  # warm-up
-        tickets: list = [None] * len(reqs)
-        ready = [threading.Event() for _ in reqs]
-        results: list = [None] * len(reqs)
-        done_at = [0.0] * len(reqs)
-
-        def waiter():
-            for k in range(len(reqs)):
-                ready[k].wait()
-                results[k] = srv.wait(tickets[k], len(reqs[k][2]))
-                done_at[k] = time.perf_counter()
-
-        th = threading.Thread(target=waiter)
-        th.start()
-        t_begin = time.perf_counter()
-        t_next = t_begin
-        for k, r in enumerate(reqs):
-            t_next += gaps[k]
-            delay = t_next - time.perf_counter()
-            if delay > 0:
-                time.sleep(delay)
-            tickets[k] = srv.submit(*r)
-            ready[k].set()
-        th.join()
-        serve_s = max(done_at) - t_begin
-        # capacity: every request submitted at once
-        t_begin = time.perf_counter()
-        ts = [srv.submit(*r) for r in reqs]
-        for t, r in zip(ts, reqs):
-            srv.wait(t, len(r[2]))
-        burst_s = time.perf_counter() - t_begin
-    lat = np.array([res[1]["total_ms"] for res in results])
+    runs = {}
+    for name, kw in (("arrival_order", {}),
+                     ("small_first", {"small_queries": SERVE_SMALL,
+                                      "small_slots": SERVE_SMALL_SLOTS})):
+        with ng.Server(ctx, cluster, SERVE_IDENTITY, slots=SERVE_SLOTS,
+                       max_queries=SERVE_MAX_BATCH, **kw) as srv:
+            srv.wait(srv.submit(*reqs[0]), len(reqs[0][2]))  # warm-up
+            results, serve_s = serve_poisson(srv, reqs, SERVE_LOAD * plain_rate, SERVE_SEED + 11)
+            # capacity: every request submitted at once
+            t_begin = time.perf_counter()
+            ts = [srv.submit(*r) for r in reqs]
+            for t, r in zip(ts, reqs):
+                srv.wait(t, len(r[2]))
+            burst_s = time.perf_counter() - t_begin
+        lat = np.array([res[1]["total_ms"] for res in results])
+        runs[name] = {
+            "value": nq / serve_s, "slots": SERVE_SLOTS,
+            "arrivals": f"Poisson, {SERVE_LOAD} x the plain request rate",
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "by_request_size": latency_split(sizes, lat),
+            "makespan_s": serve_s, "capacity": nq / burst_s,
+            "over_plain": plain_s / serve_s,
+            "results_identical": all(np.array_equal(a, b[0])
+                                     for a, b in zip(plain_out, results)),
+            **({"small_queries": SERVE_SMALL, "small_slots": SERVE_SMALL_SLOTS} if kw else {})}
     pl = np.array(plain_ms)
-    identical = all(np.array_equal(a, b[0]) for a, b in zip(plain_out, results))
     assigned = int(sum(int((o != ng.NEW_CLUSTER).sum()) for o in plain_out))
     ctx.close()
+    best = max(runs, key=lambda k: runs[k]["value"])
     return {
-        "workload": f"serving_db{db['n']}_queries{nq}_id{SERVE_IDENTITY}",
-        "data": "synthetic: small-protein generator (log-normal roots median 300 sigma 0.5, "
-                "5-35% subs, 2% indels) scaled to "
-                f"{int(SERVE_FAMILIES * args.serve_db / SERVE_DB)} families; queries held out "
-                "of the same families plus 10% unrelated; requests log-uniform 1-50,000 queries",
+        "workload": f"serving_db{db['n']}_queries{nq}_id{SERVE_IDENTITY}" +
+                    ("_close_relatives" if close else ""),
+        "data": "synthetic: small-protein generator (log-normal roots median 300 sigma 0.5, " +
+                ("0-4% subs, 0.5% indels mean 2" if close else "5-35% subs, 2% indels") +
+                f") scaled to {int(SERVE_FAMILIES * args.serve_db / SERVE_DB)} families; "
+                "queries held out of the same families plus 10% unrelated; requests "
+                "log-uniform 1-50,000 queries",
         "metric": "queries/s (and request latency)", "unit": "queries/s",
         "requests": len(reqs), "queries": nq, "assigned": assigned,
-        "replayed": SERVE_REPLAY,
+        "assignment_rate": assigned / nq, "replayed": SERVE_REPLAY,
         "setup_s": t_setup,
-        "serving": {"value": nq / serve_s, "slots": SERVE_SLOTS,
-                    "arrivals": f"Poisson, {SERVE_LOAD} x the plain request rate",
-                    "p50_ms": float(np.percentile(lat, 50)),
-                    "p99_ms": float(np.percentile(lat, 99)), "makespan_s": serve_s,
-                    "capacity": nq / burst_s},
+        "serving": runs[best], "serving_runs": runs,
         "plain": {"value": nq / plain_s, "p50_ms": float(np.percentile(pl, 50)),
                   "p99_ms": float(np.percentile(pl, 99)), "total_s": plain_s,
+                  "by_request_size": latency_split(sizes, pl),
                   "form": "one request at a time, one-thread-per-pair kernel"},
-        "serving_over_plain": plain_s / serve_s,
-        "results_identical": identical,
+        "serving_over_plain": runs[best]["over_plain"],
+        "results_identical": all(r["results_identical"] for r in runs.values()),
     }
 
 
@@ -902,7 +1196,8 @@ def main():
     if args.serve_only:
         import torch
         torch.cuda.set_device(local)
-        print(json.dumps(run_serving(args)), flush=True)
+        print(json.dumps({"serving": run_serving(args),
+                          "serving_close": run_serving(args, close=True)}), flush=True)
         return
     if args.stream_only:
         import torch
@@ -913,6 +1208,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         print(json.dumps(run_pairs(args)), flush=True)
+        return
+    if args.ref_gpu_only:
+        _, fasta, _ = make_database(args.n_seqs, max(1, args.n_seqs // (N_SEQS // N_FAMILIES)),
+                                    SEED, Path(tempfile.mkdtemp(prefix="ngia_bench_")))
+        print(json.dumps(run_reference_gpu(fasta)), flush=True)
         return
     if args.impl == "reference":
         line = run_reference(args, world, rank)

@@ -103,7 +103,9 @@ int ngia_bucket(const uint32_t *d_sigs, uint32_t n, uint32_t bands,
  * any stream capture).  All calls share the array: calls that overlap on the
  * GPU (other streams, other host threads) race and must be serialised by the
  * caller.  Every scratch word is written before it is read, so nothing needs
- * clearing between calls. */
+ * clearing between calls.  The looked-up address is kept per device ordinal;
+ * after a reset of the device (cudaDeviceReset) it is looked up again once a
+ * call has failed with NGIA_ERR_CUDA, so reset only between calls. */
 int ngia_bucket_noalloc(const uint32_t *d_sigs, uint32_t n, uint32_t bands,
                         uint32_t *d_rep, void *stream);
 
@@ -180,11 +182,37 @@ int ngia_ctx_sketch_bucket(ngia_ctx *ctx, uint32_t bands);
 int ngia_ctx_build_graph(ngia_ctx *ctx, uint32_t identity, uint32_t bands,
                          uint64_t *h_n_edges, ngia_stats *stats);
 
+/* One device's share of ngia_ctx_build_graph when the graph of one database
+ * is built by `parts` devices (each holding the database): the distinct
+ * candidate pairs, in the order the collection writes them, are cut into
+ * `parts` contiguous ranges of about equal band cells (the reference's 32x32
+ * blocks, src/buildGraph.hpp:208-217), and this call aligns and emits range
+ * `part` only.  h_range (optional) receives the range's [first, end); the
+ * edges stay on the device (ngia_ctx_edges), sorted and unique.  The union of
+ * all parts' edges, sorted by (rep, tar), is ngia_ctx_build_graph's edge list:
+ * the exchange is one gather of the compacted edges before the host's sort and
+ * Leiden.  The reference runs on one device (src/buildGraph.hpp:101-102).
+ * Synchronises. */
+int ngia_ctx_build_graph_part(ngia_ctx *ctx, uint32_t identity, uint32_t bands, uint32_t part,
+                              uint32_t parts, uint64_t *h_range, uint64_t *h_n_edges,
+                              ngia_stats *stats);
+
 /* The whole device hot path on the resident planes: sketch + bucket of
  * `bands` rep rows, then ngia_ctx_build_graph.  Fills every stats field.
  * Synchronises. */
 int ngia_ctx_group_align(ngia_ctx *ctx, uint32_t identity, uint32_t bands,
                          uint64_t *h_n_edges, ngia_stats *stats);
+
+/* A check of the candidate collection's bounded wait (the decoupled look-back
+ * of ngia_ctx_build_graph, in which each block of targets waits for the
+ * earlier blocks' counts): runs the collection with its ticket counter
+ * started at 1, so the first block's count is never published and every
+ * block gives up after spin_limit polls (1 .. 2^22).  Returns NGIA_ERR_CUDA,
+ * the error the graph build reports when a wait gives up, and leaves the
+ * context usable; NGIA_OK would mean a wait did not give up.  Testing aid,
+ * no counterpart in the reference.  Synchronises. */
+int ngia_ctx_test_lookback_timeout(ngia_ctx *ctx, uint32_t identity, uint32_t bands,
+                                   uint32_t spin_limit);
 
 /* Copy the last graph's edges to the host (cap entries at most). */
 int ngia_ctx_edges(ngia_ctx *ctx, ngia_edge *h_edges, uint64_t cap);
@@ -292,12 +320,15 @@ int ngia_stream_graph(const uint32_t *h_packed, uint64_t words, const uint64_t *
  * see each other, so a result does not depend on what else is in flight.
  *
  * Requests (batches of queries as packed records) are admitted in arrival
- * order while a slot is free and the working bytes of the requests in flight
- * stay within the HBM budget (a request larger than the budget runs alone).
+ * order (or small ones first, see ngia_server_config) while a slot is free
+ * and the working bytes of the requests in flight stay within the HBM budget
+ * (a request larger than the budget runs alone).
  * Each slot runs its request -- copy in, sketch, signature lookup, batched
  * alignment, selection, copy out -- on its own stream, so requests overlap on
  * the device.  plain = 1 gives the per-request plain form to compare with: one
- * slot, and the one-thread-per-pair drop-in kernel over the request's pairs. */
+ * slot, and the one-thread-per-pair drop-in kernel over the request's pairs.
+ * A server belongs to the device current when it is created: its dispatcher
+ * thread makes that device current, and destroy frees on it. */
 #define NGIA_NEW_CLUSTER 0xFFFFFFFFu
 typedef struct ngia_server ngia_server;
 typedef struct ngia_server_config {
@@ -307,6 +338,13 @@ typedef struct ngia_server_config {
   uint64_t max_words;   /* packed-record words per request */
   uint64_t hbm_budget;  /* bytes of request working memory in flight */
   int plain;
+  /* Admission order.  small_queries = 0: arrival order, any free slot.  Else
+   * a request of at most small_queries queries is admitted ahead of the
+   * larger ones queued before it, and slots 0..small_slots-1 take only such
+   * requests, so small requests never wait behind large ones for a slot
+   * (small_slots < slots). */
+  uint32_t small_queries;
+  uint32_t small_slots;
 } ngia_server_config;
 typedef struct ngia_request_stats {
   double queue_ms, run_ms, total_ms; /* submit->admit, admit->done, submit->done */

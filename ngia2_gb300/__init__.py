@@ -36,6 +36,7 @@ EDGE_DTYPE = np.dtype([("rep", "<i4"), ("tar", "<i4"), ("weight", "<f4")])
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
           -4: "I/O error", -5: "malformed input", -6: "call out of order"}
+OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_IO, ERR_FORMAT, ERR_STATE = 0, -1, -2, -3, -4, -5, -6
 
 
 class NgiaError(RuntimeError):
@@ -92,7 +93,8 @@ class StreamStats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("identity", C.c_uint32), ("slots", C.c_uint32), ("max_queries", C.c_uint32),
-                ("max_words", C.c_uint64), ("hbm_budget", C.c_uint64), ("plain", C.c_int)]
+                ("max_words", C.c_uint64), ("hbm_budget", C.c_uint64), ("plain", C.c_int),
+                ("small_queries", C.c_uint32), ("small_slots", C.c_uint32)]
 
 
 class RequestStats(C.Structure):
@@ -134,6 +136,11 @@ _SIGNATURES = {
     "ngia_ctx_group_align": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32,
                                        C.POINTER(C.c_uint64), C.POINTER(Stats)]),
     "ngia_ctx_edges": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "ngia_ctx_build_graph_part": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                            C.c_uint32, C.c_void_p, C.POINTER(C.c_uint64),
+                                            C.POINTER(Stats)]),
+    "ngia_ctx_test_lookback_timeout": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32,
+                                                 C.c_uint32]),
     "ngia_ctx_align_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                        C.c_void_p, C.POINTER(Stats)]),
     "ngia_ctx_align_pairs_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
@@ -335,6 +342,18 @@ class Context:
                "ngia_ctx_build_graph")
         return int(m.value), st.as_dict()
 
+    def build_graph_part(self, identity: int, part: int, parts: int,
+                         bands: int = BANDS) -> tuple[int, dict, tuple[int, int]]:
+        """This device's share (part of parts, by band cells) of build_graph:
+        the edge count, the stats and the range of distinct pairs aligned."""
+        m = C.c_uint64()
+        st = Stats()
+        rng = (C.c_uint64 * 2)()
+        _check(lib().ngia_ctx_build_graph_part(self._h, identity, bands, part, parts, rng,
+                                               C.byref(m), C.byref(st)),
+               "ngia_ctx_build_graph_part")
+        return int(m.value), st.as_dict(), (int(rng[0]), int(rng[1]))
+
     def group_align(self, identity: int, bands: int = BANDS) -> tuple[int, dict]:
         """Sketch + bucket + graph build on the resident planes."""
         m = C.c_uint64()
@@ -422,9 +441,11 @@ class Server:
 
     def __init__(self, ctx: "Context", cluster: np.ndarray, identity: int = 90, slots: int = 4,
                  max_queries: int = 50_000, max_words: int = 16 << 20,
-                 hbm_budget: int = 8 << 30, plain: bool = False):
+                 hbm_budget: int = 8 << 30, plain: bool = False, small_queries: int = 0,
+                 small_slots: int = 0):
         cluster = np.ascontiguousarray(cluster, dtype=np.uint32)
-        cfg = ServerConfig(identity, slots, max_queries, max_words, hbm_budget, 1 if plain else 0)
+        cfg = ServerConfig(identity, slots, max_queries, max_words, hbm_budget, 1 if plain else 0,
+                           small_queries, small_slots)
         h = C.c_void_p()
         _check(lib().ngia_server_create(C.byref(h), ctx._h, _ptr(cluster), C.byref(cfg)),
                "ngia_server_create")

@@ -24,7 +24,7 @@ OBJDIR = ROOT / "_build" / "ngia"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["sketch.cu", "sort.cu", "bucket.cu", "align.cu", "pairs.cu", "edges.cu", "ctx.cu",
               "round.cu", "serve.cu", "stream.cu", "pack.cu", "probe.cu"]
-CPP_SOURCES = ["packed_io.cpp", "leiden.cpp", "cluster.cpp"]
+CPP_SOURCES = ["packed_io.cpp", "leiden.cpp", "cluster.cpp", "device_session.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 
 

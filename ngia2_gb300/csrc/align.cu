@@ -5,6 +5,7 @@
 
 #include "align.cuh"
 #include "align_group.cuh"
+#include "align_group_cta.cuh"
 #include "align_stream.cuh"
 #include "kernels.cuh"
 
@@ -117,6 +118,23 @@ align_group_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restri
   count_work(done, work);
 }
 
+// The widest group classes: one block of W warps per pair
+// (align_group_cta.cuh).
+template <int W, int K, int KC>
+__global__ void __launch_bounds__(32 * W)
+align_group_cta_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ nib,
+                       uint64_t inv, const uint64_t *__restrict__ offs,
+                       const uint2 *__restrict__ pairs, const uint32_t *__restrict__ order,
+                       const uint32_t *__restrict__ bounds, int cls,
+                       unsigned int *__restrict__ cursor, uint32_t *__restrict__ scores, float t,
+                       int fma_mode, unsigned long long *__restrict__ work) {
+  extern __shared__ uint32_t smem[];
+  const uint32_t done = align_group_cta<W, K, KC>(packed, nib, inv, offs, pairs, order,
+                                                  bounds[cls], bounds[cls + 1], cursor, scores,
+                                                  t, fma_mode, smem);
+  count_work(done, work);
+}
+
 // Batched form, streaming shared-memory table kernel (align_stream.cuh):
 // a persistent grid whose lanes take pairs of one class from its queue.
 template <int W, int K>
@@ -170,16 +188,28 @@ __device__ __forceinline__ uint32_t code_mask(const uint32_t (&pl)[4], uint32_t 
 
 // Planes -> nibbles: the same record layout, with each block's four plane
 // words replaced by four words of eight 4-bit codes.  The length word is
-// copied.  presence |= bit c for every code c of a real residue.
+// copied.  presence |= bit c for every code c of a real residue.  A record
+// whose offset lies outside the `words` of the region, whose length word is
+// not lens[i], or whose blocks run past the region is left alone and sets
+// kBadRecord in presence.
 __global__ void __launch_bounds__(256)
 nibble_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
-              uint32_t n, uint32_t *__restrict__ nib, uint32_t *__restrict__ presence) {
+              const uint32_t *__restrict__ lens, uint32_t n, uint64_t words,
+              uint32_t *__restrict__ nib, uint32_t *__restrict__ presence) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   uint32_t mine = 0;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
+    if (o >= words) {
+      mine |= kBadRecord;
+      continue;
+    }
     const uint32_t len = __ldg(packed + o);
+    if (len != lens[i] || o + 1 + 4ull * ((len + 31) >> 5) > words) {
+      mine |= kBadRecord;
+      continue;
+    }
     if (lane == 0) nib[o] = len;
     const uint32_t blocks = (len + 31) >> 5;
     for (uint32_t k = lane; k < blocks; k += 32) {
@@ -242,15 +272,17 @@ dense_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__rest
   }
 }
 
-int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
-                   uint32_t *presence, cudaStream_t s, bool accumulate) {
+int launch_nibbles(const uint32_t *packed, const uint64_t *offs, const uint32_t *lens,
+                   uint32_t n, uint64_t words, uint32_t *nib, uint32_t *presence, cudaStream_t s,
+                   bool accumulate) {
   if (n == 0) return NGIA_OK;
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
   if (!accumulate) NGIA_CUDA(cudaMemsetAsync(presence, 0, sizeof(uint32_t), s));
-  nibble_kernel<<<want < cap ? want : cap, 256, 0, s>>>(packed, offs, n, nib, presence);
+  nibble_kernel<<<want < cap ? want : cap, 256, 0, s>>>(packed, offs, lens, n, words, nib,
+                                                        presence);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
@@ -264,7 +296,8 @@ int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uin
 // codes[k], k < ncodes: the residue codes of the map, aligner code k + 1.
 __global__ void __launch_bounds__(256)
 load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
-                    uint32_t n, uint64_t w0, uint64_t w1, uint32_t codes, uint32_t ncodes,
+                    const uint32_t *__restrict__ lens, uint32_t n, uint64_t w0, uint64_t w1,
+                    uint32_t codes, uint32_t ncodes,
                     uint32_t *__restrict__ nib, uint32_t *__restrict__ dense_nib,
                     uint32_t *__restrict__ dplanes, uint32_t *__restrict__ bad) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -278,7 +311,7 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
     }
     const uint32_t len = __ldg(packed + o);
     const uint32_t blocks = (len + 31) >> 5;
-    if (o + 1 + 4ull * blocks > w1) {
+    if (len != lens[i] || o + 1 + 4ull * blocks > w1) {
       wrong = true;
       continue;
     }
@@ -329,9 +362,9 @@ static int map_bits(uint64_t map, uint32_t (&bits)[3]) {
   return NGIA_OK;
 }
 
-int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint64_t w0,
-                        uint64_t w1, uint64_t inv, uint32_t *nib, uint32_t *dense_nib,
-                        uint32_t *dplanes, uint32_t *bad, cudaStream_t s) {
+int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint32_t *lens,
+                        uint32_t n, uint64_t w0, uint64_t w1, uint64_t inv, uint32_t *nib,
+                        uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad, cudaStream_t s) {
   if (n == 0) return NGIA_OK;
   uint32_t codes = 0, ncodes = 0;  // inv nibble d = residue code of aligner code d
   for (uint32_t d = 1; d < 8; ++d) {
@@ -344,7 +377,7 @@ int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
   load_layouts_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
-      packed, offs, n, w0, w1, codes, ncodes, nib, dense_nib, dplanes, bad);
+      packed, offs, lens, n, w0, w1, codes, ncodes, nib, dense_nib, dplanes, bad);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
@@ -442,6 +475,34 @@ static int launch_group_k(const RoundArgs &a, int cls, unsigned int *cursor, cud
   return NGIA_OK;
 }
 
+template <int W, int K, int KC>
+static int launch_group_cta_k(const RoundArgs &a, int cls, unsigned int *cursor,
+                              cudaStream_t s) {
+  constexpr size_t smem = group_cta_smem_bytes<W, K, KC>();
+  uint32_t grid = 0;
+  NGIA_TRY(persistent_grid(align_group_cta_kernel<W, K, KC>, 32 * W, smem, kFull, &grid));
+  if (KC == 8 && !a.dplanes) return NGIA_ERR_STATE;
+  align_group_cta_kernel<W, K, KC><<<grid, 32 * W, smem, s>>>(
+      KC == 8 ? a.dplanes : a.packed, a.nib, a.inv, a.offs, a.pairs, a.order, a.bounds, cls,
+      cursor, a.scores, a.t, a.fm, a.work);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+// A class of (32 lanes, K words) on one block of kCtaWarps warps per pair
+// (32 * kCtaWarps lanes, K / kCtaWarps words): the same rows per ring turn and
+// a wider span, so the class's binning holds (align_group_cta.cuh).
+constexpr int kCtaWarps = 4;
+template <int K>
+static int launch_group_cta(const RoundArgs &a, int KC, int cls, unsigned int *cursor,
+                            cudaStream_t s) {
+  static_assert(K % kCtaWarps == 0, "slices of K / kCtaWarps words");
+  constexpr int KW = K / kCtaWarps;
+  static_assert((32 * kCtaWarps - 1) * KW + 32 * kCtaWarps >= 31 * K + 32, "span");
+  return KC <= 8 ? launch_group_cta_k<kCtaWarps, KW, 8>(a, cls, cursor, s)
+                 : launch_group_cta_k<kCtaWarps, KW, 16>(a, cls, cursor, s);
+}
+
 template <int W>
 static int launch_stream(const RoundArgs &a, int K, int cls, unsigned int *cursor,
                          cudaStream_t s) {
@@ -506,9 +567,11 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
     NGIA_GROUP_CASE(12)
     NGIA_GROUP_CASE(13)
     NGIA_GROUP_CASE(14)
-    NGIA_GROUP_CASE(15)
-    NGIA_GROUP_CASE(16)
 #undef NGIA_GROUP_CASE
+    case 15:
+      static_assert(group_shape(15).G == 32 && group_shape(16).G == 32, "block-wide classes");
+      return launch_group_cta<group_shape(15).K>(a, ab.K, cls, cursor, s);
+    case 16: return launch_group_cta<group_shape(16).K>(a, ab.K, cls, cursor, s);
     case kGeneralClass: {
       uint32_t grid = 0;
       NGIA_TRY(persistent_grid(align_general_kernel, 128, 0, kFull, &grid));

@@ -6,26 +6,50 @@
 // run:  rep[b][idx] = previous idx if the signatures are equal, else idx.
 // Equivalently rep[b][i] is the largest j < i with sig[b][j] == sig[b][i].
 //
-// Device form: all bands are sorted together as 64 segments by the segmented
-// radix sort (sort.cu), then one coalesced pass over the sorted runs writes
-// the predecessor links.
+// Device form, per band:
+//   1. partition: stable 8-bit radix passes on the signature's low bits, as
+//      many as keep the runs of equal low bits (buckets) at about four
+//      entries on average -- two passes up to 2^18 sequences, three up to
+//      2^26, else all four; each bucket holds its entries in index order;
+//   2. resolve (rep_resolve_kernel): one thread per sorted entry scans back
+//      through its bucket to the nearest entry with the same signature, which
+//      is its predecessor in index order; none: the entry is its own rep.
+// Two or three sort passes instead of four, and the chain written by the
+// resolve pass itself.  Equal signatures always share a bucket, so a scan
+// only passes entries of other signatures whose low bits collide -- a few on
+// average; the loop is bounded by the bucket's start.
 #include <mutex>
 
 #include "kernels.cuh"
 
 namespace ngia {
 
+// Partition passes: buckets of n / 2^(8P) <= 4 entries on average.
+static int partition_passes(uint32_t n) {
+  return n <= (1u << 10) ? 1 : n <= (1u << 18) ? 2 : n <= (1u << 26) ? 3 : 4;
+}
+
+// sk, sv: each band's (signature, index) pairs ordered stably by the
+// signature's low bits (low_mask).
 __global__ void __launch_bounds__(256)
-rep_chain_kernel(const uint32_t *__restrict__ skeys, const uint32_t *__restrict__ svals,
-                 uint32_t n, uint32_t bands, uint32_t *__restrict__ rep) {
+rep_resolve_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__ sv,
+                   uint32_t n, uint32_t bands, uint32_t low_mask, uint32_t *__restrict__ rep) {
   const size_t total = (size_t)n * bands;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (size_t)gridDim.x * blockDim.x) {
     const size_t band = e / n;
-    const uint32_t p = (uint32_t)(e - band * n);
-    const uint32_t idx = svals[e];
-    const uint32_t r = (p > 0 && skeys[e - 1] == skeys[e]) ? svals[e - 1] : idx;
-    rep[band * n + idx] = r;
+    const size_t first = band * n;  // the band's first entry
+    const uint32_t sig = sk[e], bkt = sig & low_mask;
+    uint32_t r = sv[e];
+    for (size_t q = e; q-- > first;) {
+      const uint32_t s = __ldg(sk + q);
+      if ((s & low_mask) != bkt) break;  // the bucket's start
+      if (s == sig) {
+        r = __ldg(sv + q);
+        break;
+      }
+    }
+    rep[first + sv[e]] = r;
   }
 }
 
@@ -39,13 +63,17 @@ int bucket(const uint32_t *sigs, uint32_t n, uint32_t bands, uint32_t *rep,
   const size_t total = (size_t)n * bands;
   uint32_t *sk = static_cast<uint32_t *>(scratch);
   uint32_t *sv = sk + total;
-  NGIA_TRY(radix_sort_pairs(sigs, nullptr, sk, sv, n, bands, 0, 32, sv + total, s));
+  void *sort_scratch = sv + total;
+  const int passes = partition_passes(n);
+  NGIA_TRY(radix_sort_pairs(sigs, nullptr, sk, sv, n, bands, 0, 8 * passes, sort_scratch, s));
+  const uint32_t low_mask = 8 * passes >= 32 ? kFull : (1u << (8 * passes)) - 1u;
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const size_t want = ceil_div<size_t>(total, 256);
   const size_t cap = (size_t)sms * 8;
-  rep_chain_kernel<<<(uint32_t)(want < cap ? want : cap), 256, 0, s>>>(sk, sv, n, bands, rep);
+  rep_resolve_kernel<<<(uint32_t)(want < cap ? want : cap), 256, 0, s>>>(sk, sv, n, bands,
+                                                                         low_mask, rep);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
@@ -97,10 +125,11 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 static void *g_noalloc_ptr[128] = {};
 static std::mutex g_noalloc_mutex;
 
-static int noalloc_scratch(void **out) {
+static int noalloc_scratch(void **out, int *dev_out) {
   int dev = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 128) return NGIA_ERR_ARG;
+  *dev_out = dev;
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   if (!g_noalloc_ptr[dev]) {
     void *p = nullptr;
@@ -122,6 +151,14 @@ extern "C" int ngia_bucket_noalloc(const uint32_t *d_sigs, uint32_t n, uint32_t 
   if ((uint64_t)n * bands > kNoAllocMaxElems) return NGIA_ERR_ARG;
   if (bucket_scratch_bytes(n, bands) > kNoAllocScratchBytes) return NGIA_ERR_ARG;
   void *scratch = nullptr;
-  NGIA_TRY(noalloc_scratch(&scratch));
-  return bucket(d_sigs, n, bands, d_rep, scratch, as_stream(stream));
+  int dev = 0;
+  NGIA_TRY(noalloc_scratch(&scratch, &dev));
+  const int st = bucket(d_sigs, n, bands, d_rep, scratch, as_stream(stream));
+  if (st == NGIA_ERR_CUDA) {
+    // a failed launch may follow a reset of the device's context, which reloads
+    // the module and can move the array: look its address up again next time
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    g_noalloc_ptr[dev] = nullptr;
+  }
+  return st;
 }

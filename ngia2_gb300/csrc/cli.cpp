@@ -6,11 +6,20 @@
 //   ngia2 -m fast       -p <packed> -r <result> [-i 95] [-b 64]
 //   ngia2 cluster -i <identity> -p <packed> -r <result>   (README spelling)
 //   ngia2 makeDB  -f <fasta> -p <packed>                  (README spelling)
+//   ngia2 -m makedb+clustering -f <fasta> -p <packed> -r <result> [-i] [-b]
+//   ngia2 -m makedb+fast       -f <fasta> -p <packed> -r <result> [-i] [-b]
+// The last two run makedb and the clustering in one process (the same packed
+// file and result file as the two commands), with the database kept on the
+// device in between; the reference has no such mode.
 //
 // Flag grammar of Parser (src/parser.hpp:37-56): "-name value" pairs, the last
 // occurrence wins, the final token is never read as a flag name, a missing
 // required flag prints the usage.  Invalid arguments print the usage and exit
 // 0; runtime failures exit 1 (src/main.cu:56-60, :88-93, :96-98).
+//
+// The process owns device 0 (the reference's cudaSetDevice(0)): its CUDA
+// context is created on a helper thread while the host reads its input, and
+// released on a helper thread while the host writes its output.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -90,16 +99,38 @@ int main(int argc, char **argv) {
                     result = flags[3].value;
   const uint32_t identity = to_u32(flags[4].value), bands = to_u32(flags[5].value);
   int rc = 0;
-  if (mode == "makedb") {
+  const bool both = mode == "makedb+clustering" || mode == "makedb+fast";
+  if (both && (identity < 1 || identity > 99 || bands < 1 || bands > NGIA_BANDS)) {
+    std::printf("identity should be 1-99, bands 1-%d\n\nUsage:\n%s -m %s -f fastaFile "
+                "-p packedFile -r resultFile -i identity -b bands\n",
+                NGIA_BANDS, argv[0], mode.c_str());
+    return 0;
+  }
+  if (mode == "makedb" || both) {
     std::string why;
     if (ngia::check_fasta(fasta, why) != NGIA_OK) {
       std::printf("%s\n\nUsage:\n%s -m makedb -f fastaFile -p packedFile\n", why.c_str(),
                   argv[0]);
       return 0;
     }
+    ngia::device_warmup_start(0);
     std::printf("fasta:\t%s\npacked:\t%s\n", fasta.c_str(), packed.c_str());
-    uint32_t n = 0;
-    const int st = ngia_makedb(fasta.c_str(), packed.c_str(), &n);
+    ngia::PhaseClock timer;
+    ngia::Makedb m;
+    int st = ngia::makedb_prepare(fasta, packed, m);
+    timer.lap("index + records");
+    ngia_ctx *ctx = nullptr;
+    if (st == NGIA_OK) st = ngia::device_warmup_join();
+    if (st == NGIA_OK) st = ngia_ctx_create(&ctx, nullptr);
+    timer.lap("device ready");
+    if (st == NGIA_OK) st = ngia::makedb_device(ctx, m);
+    timer.lap("pack + sketch + bucket");
+    if (st != NGIA_OK || !both) {
+      ngia_ctx_destroy(ctx);
+      ngia::device_release_start(0);
+    }
+    if (st == NGIA_OK) st = ngia::makedb_finish(m);
+    timer.lap("file");
     if (st == NGIA_ERR_FORMAT) {
       std::printf("no valid sequence (empty file or all reads >= 65535)\n");
       rc = 1;
@@ -107,8 +138,28 @@ int main(int argc, char **argv) {
       std::printf("makedb failed: %s\n", ngia_status_string(st));
       rc = 1;
     } else {
-      std::printf("valid:\t%u\n", n);
+      std::printf("total:\t%llu\nvalid:\t%u\n", (unsigned long long)m.scanned, m.n);
     }
+    if (both && rc == 0) {
+      std::printf("result file:\t%s\nidentity:\t%u\n", result.c_str(), identity);
+      ngia_stats cst;
+      std::memset(&cst, 0, sizeof(cst));
+      const auto t1 = std::chrono::steady_clock::now();
+      const bool fast = mode == "makedb+fast";
+      const int s = ngia::cluster_loaded(ctx, packed.c_str(), result.c_str(), identity, bands,
+                                         fast ? 1 : 0, &cst, true, 0, m.n);
+      if (s != NGIA_OK) {
+        std::printf("%s failed: %s\n", fast ? "fast clustering" : "clustering",
+                    ngia_status_string(s));
+        rc = 1;
+      } else {
+        print_duration(fast ? "[fast]" : "[clustering]", since(t1));
+      }
+    } else if (both) {
+      ngia_ctx_destroy(ctx);
+      ngia::device_release_start(0);
+    }
+    ngia::device_release_join();
   } else if (mode == "clustering" || mode == "fast") {
     const bool fast = mode == "fast";
     bool ok = true;
@@ -138,12 +189,14 @@ int main(int argc, char **argv) {
                   argv[0], mode.c_str());
       return 0;
     }
+    ngia::device_warmup_start(0);
     std::printf("packed file:\t%s\nresult file:\t%s\nidentity:\t%u\n", packed.c_str(),
                 result.c_str(), identity);
     ngia_stats st;
     const auto t1 = std::chrono::steady_clock::now();
-    const int s = ngia_cluster_file(packed.c_str(), result.c_str(), identity, bands,
-                                    fast ? 1 : 0, &st);
+    const int s = ngia::cluster_file_run(packed.c_str(), result.c_str(), identity, bands,
+                                         fast ? 1 : 0, &st, true, 0);
+    ngia::device_release_join();
     if (s != NGIA_OK) {
       std::printf("%s failed: %s\n", fast ? "fast clustering" : "clustering",
                   ngia_status_string(s));

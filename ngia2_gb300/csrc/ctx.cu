@@ -77,7 +77,7 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_d
 }
 
 int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_n_edges,
-                    ngia_stats *st) {
+                    ngia_stats *st, uint32_t part, uint32_t parts, uint64_t *h_range) {
   if (c->n == 0 || c->rep_bands == 0) return NGIA_ERR_STATE;
   if (identity < 1 || identity > 99) return NGIA_ERR_ARG;
   if (bands < 1 || bands > c->rep_bands) return NGIA_ERR_ARG;
@@ -104,7 +104,18 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
   if (hc.collect_error) return NGIA_ERR_CUDA;  // a look-back gave up (never seen)
   const uint64_t total = hc.unique_total;
   if (total > 0xFFFFFFFFull) return NGIA_ERR_NOMEM;  // beyond one launch's index range
-  const uint32_t m = (uint32_t)total;
+  uint32_t cut[2] = {0u, (uint32_t)total};
+  if (parts > 1) {  // this device's share of the pairs, by band cells
+    NGIA_TRY(c->part_tmp.reserve(share_scratch_bytes((uint32_t)total)));
+    NGIA_TRY(share_range(lens, pairs, (uint32_t)total, identity, part, parts, c->part_tmp.p, cut,
+                         s));
+    pairs += cut[0];
+  }
+  if (h_range) {
+    h_range[0] = cut[0];
+    h_range[1] = cut[1];
+  }
+  const uint32_t m = cut[1] - cut[0];
   NGIA_TRY(c->scores.reserve((size_t)(m ? m : 1) * 4));
   uint32_t *scores = c->scores.as<uint32_t>();
   // 2-3. width classes, then one persistent launch per class (the round is
@@ -125,7 +136,7 @@ int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_
     Counters rc;
     NGIA_CUDA(cudaMemcpy(&rc, c->round.counters(), sizeof(Counters), cudaMemcpyDeviceToHost));
     st->candidate_pairs = hc.cand_total;
-    st->unique_pairs = total;
+    st->unique_pairs = m;
     st->aligned_cells = rc.cells;
     st->computed_cells = rc.work * 1024ull;
     st->edges = ne;
@@ -240,10 +251,24 @@ static int use_alphabet(ngia_ctx *c, const AlphaChoice &a, uint64_t words, uint3
   return NGIA_OK;
 }
 
+// Every record inside the region by its offset and read length, and no read
+// longer than the format allows (one pass over the two arrays, before any
+// copy); the device checks each record's length word as it lays it out.
+static bool records_inside(const uint64_t *h_offs, const uint32_t *h_lens, uint32_t n,
+                           uint64_t words) {
+  bool bad = false;
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint64_t end = h_offs[i] + 1 + 4ull * ((h_lens[i] + 31u) >> 5);
+    bad |= (h_lens[i] > NGIA_MAX_READ) | (end > words) | (h_offs[i] >= words);
+  }
+  return !bad;
+}
+
 int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64_t *h_offs,
              const uint32_t *h_lens, uint32_t n, const uint32_t *h_rep, uint32_t bands) {
   if (n == 0 || !h_packed || !h_offs || !h_lens) return NGIA_ERR_ARG;
   if (h_rep && (bands < 1 || bands > (uint32_t)kBands)) return NGIA_ERR_ARG;
+  if (!records_inside(h_offs, h_lens, n, words)) return NGIA_ERR_ARG;
   cudaStream_t s = c->stream;
   NGIA_TRY(c->packed.reserve(words * 4));
   NGIA_TRY(c->offs.reserve((size_t)n * 8));
@@ -253,12 +278,17 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
   NGIA_CUDA(cudaMemcpyAsync(c->lens.p, h_lens, (size_t)n * 4, cudaMemcpyHostToDevice, s));
   NGIA_TRY(c->nib.reserve(words * 4));
   NGIA_TRY(c->presence.reserve(sizeof(uint32_t)));
-  NGIA_TRY(launch_nibbles(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(), n,
-                          c->nib.as<uint32_t>(), c->presence.as<uint32_t>(), s));
+  NGIA_TRY(launch_nibbles(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(),
+                          c->lens.as<uint32_t>(), n, words, c->nib.as<uint32_t>(),
+                          c->presence.as<uint32_t>(), s));
   uint32_t present = 0;
   NGIA_CUDA(cudaMemcpyAsync(&present, c->presence.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             s));
   NGIA_CUDA(cudaStreamSynchronize(s));
+  if (present & kBadRecord) {  // a length word that is not the record's read length
+    c->n = 0;
+    return NGIA_ERR_FORMAT;
+  }
   NGIA_TRY(use_alphabet(c, choose_alphabet(present), words, n, true));
   c->last_present = present;
   c->n = n;
@@ -272,6 +302,58 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
                               cudaMemcpyHostToDevice, s));
     c->rep_bands = bands;
   }
+  return NGIA_OK;
+}
+
+int ctx_load_text(ngia_ctx *c, const char *h_text, uint64_t text_bytes,
+                  const uint64_t *h_starts, const uint32_t *h_lens, const uint64_t *h_offs,
+                  uint32_t n, uint64_t words) {
+  if (n == 0 || !h_text || !h_starts || !h_lens || !h_offs) return NGIA_ERR_ARG;
+  cudaStream_t s = c->stream;
+  NGIA_TRY(c->packed.reserve(words * 4));
+  NGIA_TRY(c->nib.reserve(words * 4));
+  NGIA_TRY(c->offs.reserve((size_t)n * 8));
+  NGIA_TRY(c->lens.reserve((size_t)n * 4));
+  NGIA_TRY(c->presence.reserve(sizeof(uint32_t)));
+  const size_t starts_at = (text_bytes + 15) & ~(size_t)15;
+  NGIA_TRY(c->staging.reserve(starts_at + (size_t)n * 8));
+  char *d_text = c->staging.as<char>();
+  uint64_t *d_starts = reinterpret_cast<uint64_t *>(d_text + starts_at);
+  NGIA_CUDA(cudaMemcpyAsync(d_text, h_text, text_bytes, cudaMemcpyHostToDevice, s));
+  NGIA_CUDA(cudaMemcpyAsync(d_starts, h_starts, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+  NGIA_CUDA(cudaMemcpyAsync(c->offs.p, h_offs, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+  NGIA_CUDA(cudaMemcpyAsync(c->lens.p, h_lens, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  NGIA_TRY(launch_pack_layout(reinterpret_cast<const uint8_t *>(d_text), d_starts,
+                              c->lens.as<uint32_t>(), n, c->offs.as<uint64_t>(),
+                              c->packed.as<uint32_t>(), c->nib.as<uint32_t>(),
+                              c->presence.as<uint32_t>(), s));
+  uint32_t present = 0;
+  NGIA_CUDA(cudaMemcpyAsync(&present, c->presence.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  c->staging.release();
+  NGIA_TRY(use_alphabet(c, choose_alphabet(present), words, n, true));
+  c->last_present = present;
+  c->n = n;
+  c->sigs_valid = false;
+  c->packed_words = words;
+  c->rep_bands = 0;
+  c->n_edges = 0;
+  return NGIA_OK;
+}
+
+int makedb_device(ngia_ctx *c, Makedb &m) {
+  if (!c || m.n == 0 || !m.file.data) return NGIA_ERR_ARG;
+  cudaStream_t s = c->stream;
+  NGIA_TRY(ctx_load_text(c, m.file.data + m.fasta0, m.size - m.fasta0, m.text_starts.data(),
+                         m.lens.data(), m.offsets.data(), m.n, m.words));
+  NGIA_TRY(ctx_sketch_bucket(c, kBands, nullptr));
+  // the 64 rep rows (band-major) over the signature area, then the planes
+  NGIA_CUDA(cudaMemcpyAsync(m.file.data + sig_area_offset(m.n), c->rep.p,
+                            (size_t)kBands * m.n * 4, cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaMemcpyAsync(m.file.data + m.pack0, c->packed.p, m.words * 4,
+                            cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
   return NGIA_OK;
 }
 
@@ -294,6 +376,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
   const AlphaChoice spec = choose_alphabet(c->last_present);
   if (!spec.dense || !spec.table_ok || !c->table_built || c->table_inv != spec.inv)
     return NGIA_OK;
+  if (!records_inside(h_offs, h_lens, n, words)) return NGIA_ERR_ARG;
   *used = true;
   cudaStream_t s = c->stream;
   NGIA_TRY(c->packed.reserve(words * 4));
@@ -351,7 +434,8 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
     if (cnt) {
       const uint64_t w0 = k == 0 ? 0 : (first[k] < n ? h_offs[first[k]] : words);
       const uint64_t w1 = k + 1 == C ? words : (first[k + 1] < n ? h_offs[first[k + 1]] : words);
-      NGIA_TRY(launch_load_layouts(packed, offs + r0, cnt, w0, w1, spec.inv,
+      NGIA_TRY(launch_load_layouts(packed, offs + r0, c->lens.as<uint32_t>() + r0, cnt, w0, w1,
+                                   spec.inv,
                                    c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
                                    c->dplanes.as<uint32_t>(), c->presence.as<uint32_t>(),
                                    c->layout));
@@ -455,6 +539,7 @@ void ngia_ctx_destroy(ngia_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   ngia::DevBuf *bufs[] = {&c->packed,   &c->nib,   &c->nib_dense, &c->dplanes,  &c->presence,
+                          &c->staging,  &c->part_tmp,
                           &c->offs,     &c->lens,  &c->rep,       &c->sigs,     &c->ucount,
                           &c->uoff,
                           &c->counters, &c->pairs, &c->scores,    &c->sort_tmp, &c->emit_tmp,
@@ -511,12 +596,46 @@ int ngia_ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands,
   return ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats);
 }
 
+int ngia_ctx_build_graph_part(ngia_ctx *c, uint32_t identity, uint32_t bands, uint32_t part,
+                              uint32_t parts, uint64_t *h_range, uint64_t *h_n_edges,
+                              ngia_stats *stats) {
+  if (!c || parts < 1 || part >= parts) return NGIA_ERR_ARG;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  return ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats, part, parts, h_range);
+}
+
 int ngia_ctx_group_align(ngia_ctx *c, uint32_t identity, uint32_t bands,
                          uint64_t *h_n_edges, ngia_stats *stats) {
   if (!c) return NGIA_ERR_ARG;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats));
   return ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats);
+}
+
+int ngia_ctx_test_lookback_timeout(ngia_ctx *c, uint32_t identity, uint32_t bands,
+                                   uint32_t spin_limit) {
+  using namespace ngia;
+  if (!c) return NGIA_ERR_ARG;
+  if (c->n == 0 || c->rep_bands == 0) return NGIA_ERR_STATE;
+  if (identity < 1 || identity > 99 || bands < 1 || bands > c->rep_bands) return NGIA_ERR_ARG;
+  if (spin_limit < 1 || spin_limit > kLookbackSpins) return NGIA_ERR_ARG;
+  cudaStream_t s = c->stream;
+  const uint32_t n = c->n;
+  NGIA_TRY(c->counters.reserve(sizeof(Counters)));
+  NGIA_TRY(c->uoff.reserve((size_t)n * 8));
+  NGIA_TRY(c->pairs.reserve((size_t)bands * n * 8));
+  Counters *dc = c->counters.as<Counters>();
+  NGIA_CUDA(cudaMemsetAsync(dc, 0, sizeof(Counters), s));
+  const unsigned int one = 1;  // the first ticket handed out is 1: block 0 never publishes
+  NGIA_CUDA(cudaMemcpyAsync(&dc->collect_ticket, &one, sizeof(one), cudaMemcpyHostToDevice, s));
+  NGIA_TRY(collect_scan(c->rep.as<uint32_t>(), c->lens.as<uint32_t>(), n, bands, identity,
+                        &dc->collect_ticket, reinterpret_cast<unsigned long long *>(c->uoff.p),
+                        &dc->cand_total, &dc->unique_total, &dc->collect_error,
+                        c->pairs.as<uint2>(), s, spin_limit));
+  Counters hc;
+  NGIA_CUDA(cudaMemcpyAsync(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
+  return hc.collect_error ? NGIA_ERR_CUDA : NGIA_OK;
 }
 
 int ngia_ctx_edges(ngia_ctx *c, ngia_edge *h_edges, uint64_t cap) {

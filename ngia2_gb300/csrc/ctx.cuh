@@ -20,6 +20,8 @@ struct ngia_ctx {
   uint64_t packed_words = 0;
   uint32_t rep_bands = 0;
   ngia::DevBuf packed, nib, offs, lens, rep, sigs;
+  ngia::DevBuf staging;  // residue text of a load from text (released after it)
+  ngia::DevBuf part_tmp;  // band blocks and their prefix (a graph build split over devices)
   bool sigs_valid = false;  // sigs hold all 64 bands of the loaded records
   // targets as the aligner reads them: densely recoded when the database uses
   // at most 7 nonzero residue codes (aligner tables of 8 entries), else `nib`
@@ -47,4 +49,15 @@ DbView db_view(const ngia_ctx *c);
 int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_done = false);
 int ctx_fast_cluster(ngia_ctx *c, uint32_t identity, uint32_t bands, uint32_t *h_cluster,
                      ngia_stats *st);
+// Load from residue text (makedb): record i's h_lens[i] residues start at byte
+// h_starts[i] of h_text; the device packs them into planes at word offsets
+// h_offs[i] (`words` in all) and writes the nibble layout in the same pass.
+int ctx_load_text(ngia_ctx *c, const char *h_text, uint64_t text_bytes,
+                  const uint64_t *h_starts, const uint32_t *h_lens, const uint64_t *h_offs,
+                  uint32_t n, uint64_t words);
+// parts > 1: only the part-th share of the distinct pairs by band cells is
+// aligned and emitted; h_range (optional) receives its [first, end).
+int ctx_build_graph(ngia_ctx *c, uint32_t identity, uint32_t bands, uint64_t *h_n_edges,
+                    ngia_stats *st, uint32_t part = 0, uint32_t parts = 1,
+                    uint64_t *h_range = nullptr);
 }  // namespace ngia

@@ -73,12 +73,17 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
 // (inv: nibble d = residue code of aligner code d, pipelined loads): nibbles,
 // recoded nibbles and code planes.  *bad = 1 if a residue has a code outside
 // the map or a record is not inside words [w0, w1) (such a record is skipped).
-int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint64_t w0,
-                        uint64_t w1, uint64_t inv, uint32_t *nib, uint32_t *dense_nib,
-                        uint32_t *dplanes, uint32_t *bad, cudaStream_t s);
-// presence |= the codes seen (cleared first unless accumulate)
-int launch_nibbles(const uint32_t *packed, const uint64_t *offs, uint32_t n, uint32_t *nib,
-                   uint32_t *presence, cudaStream_t s, bool accumulate = false);
+// (A record whose length word is not lens[i] sets *bad too.)
+int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint32_t *lens,
+                        uint32_t n, uint64_t w0, uint64_t w1, uint64_t inv, uint32_t *nib,
+                        uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad, cudaStream_t s);
+// presence |= the codes seen (cleared first unless accumulate); a record
+// outside the region's `words`, or whose length word is not lens[i], is
+// skipped and sets kBadRecord.
+constexpr uint32_t kBadRecord = 1u << 31;
+int launch_nibbles(const uint32_t *packed, const uint64_t *offs, const uint32_t *lens,
+                   uint32_t n, uint64_t words, uint32_t *nib, uint32_t *presence, cudaStream_t s,
+                   bool accumulate = false);
 // Packed records and a code map with new codes 0..7 -> the recoded nibbles
 // (residue code c -> map nibble c) and the planes of the new codes
 // (Alphabet::dplanes), in one pass.
@@ -86,14 +91,23 @@ int launch_dense_layouts(const uint32_t *packed, const uint64_t *offs, uint32_t 
                          uint64_t map, uint32_t *dense_nib, uint32_t *dplanes,
                          cudaStream_t s);
 
+// pack.cu
+// Residue text -> packed records (planes), their nibble layout and the codes
+// present (cleared first), in one pass; record i's residues at res + starts[i].
+int launch_pack_layout(const uint8_t *res, const uint64_t *starts, const uint32_t *lens,
+                       uint32_t n, const uint64_t *offs, uint32_t *packed, uint32_t *nib,
+                       uint32_t *presence, cudaStream_t s);
+
 // pairs.cu
 // Candidate pairs in one pass (see pairs.cu): pairs[] must hold bands * n;
 // *ticket and *unique_total zero before the call, status[] holds
-// ceil(n / 32) words (cleared here); *error set if a look-back gave up.
+// ceil(n / 32) words (cleared here); *error set if a look-back gave up after
+// spin_limit polls of a predecessor's status.
+constexpr uint32_t kLookbackSpins = 1u << 22;
 int collect_scan(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
                  uint32_t identity, unsigned int *ticket, unsigned long long *status,
                  unsigned long long *cand_total, uint64_t *unique_total, unsigned int *error,
-                 uint2 *pairs, cudaStream_t s);
+                 uint2 *pairs, cudaStream_t s, uint32_t spin_limit = kLookbackSpins);
 int collect_count(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
                   uint32_t identity, uint32_t *ucount, unsigned long long *cand_total,
                   cudaStream_t s);
@@ -108,6 +122,14 @@ int classify(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t 
              const ClassPlan &plan, uint32_t *cls, unsigned int *class_count,
              unsigned long long *cells, uint32_t *bounds, cudaStream_t s);
 int bits_for(uint32_t max_value);
+// The part-th of `parts` contiguous ranges [h_cut[0], h_cut[1]) of the pairs,
+// cut so that each holds about 1/parts of their band blocks (the first pair
+// whose exclusive prefix reaches total * k / parts starts range k).
+// Synchronises s.
+size_t share_scratch_bytes(uint32_t count);
+int share_range(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t identity,
+                uint32_t part, uint32_t parts, void *scratch, uint32_t h_cut[2],
+                cudaStream_t s);
 size_t emit_scratch_bytes(uint32_t count, uint32_t n_nodes);
 int emit_sorted(const uint2 *pairs, const uint32_t *scores, uint32_t count,
                 uint32_t n_nodes, ngia_edge *out, uint64_t *h_m, void *scratch,

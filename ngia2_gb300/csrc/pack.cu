@@ -52,6 +52,49 @@ pack_kernel(const uint8_t *__restrict__ res, const uint64_t *__restrict__ starts
   }
 }
 
+// The same packing, plus the nibble layout the sketch and the aligners read
+// (word q of a block: residues 8q..8q+7, the first in the high nibble; the
+// length word copied) and the set of residue codes present, in one pass: a
+// database loaded from residue text (makedb) never reads its planes back.
+// Lane j's code shifted to its nibble and OR-ed across each group of eight
+// lanes gives nibble word j / 8 in lanes 0, 8, 16, 24.
+__global__ void __launch_bounds__(256)
+pack_layout_kernel(const uint8_t *__restrict__ res, const uint64_t *__restrict__ starts,
+                   const uint32_t *__restrict__ lens, uint32_t n,
+                   const uint64_t *__restrict__ offs, uint32_t *__restrict__ packed,
+                   uint32_t *__restrict__ nib, uint32_t *__restrict__ presence) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  uint32_t mine = 0;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const uint32_t len = lens[i];
+    const uint8_t *r = res + starts[i];
+    const uint64_t o = offs[i];
+    if (lane == 0) {
+      packed[o] = len;
+      nib[o] = len;
+    }
+    const uint32_t blocks = (len + 31) >> 5;
+    for (uint32_t k = 0; k < blocks; ++k) {
+      const uint32_t p = 32 * k + lane;
+      const bool real = p < len;
+      const uint32_t code = real ? c_code[__ldg(r + p)] : 0u;
+      if (real) mine |= 1u << code;
+      const uint32_t b0 = __ballot_sync(kFull, code & 1u), b1 = __ballot_sync(kFull, code & 2u);
+      const uint32_t b2 = __ballot_sync(kFull, code & 4u), b3 = __ballot_sync(kFull, code & 8u);
+      uint32_t x = code << (4u * (7u - (lane & 7u)));
+      x |= __shfl_xor_sync(kFull, x, 1);
+      x |= __shfl_xor_sync(kFull, x, 2);
+      x |= __shfl_xor_sync(kFull, x, 4);
+      const uint64_t blk = o + 1 + 4ull * k;
+      if (lane < 4) packed[blk + lane] = lane == 0 ? b0 : lane == 1 ? b1 : lane == 2 ? b2 : b3;
+      if ((lane & 7u) == 0) nib[blk + (lane >> 3)] = x;
+    }
+  }
+  mine = __reduce_or_sync(kFull, mine);
+  if (lane == 0 && mine) atomicOr(presence, mine);
+}
+
 static int upload_table() {
   static bool done[64] = {};
   int dev = 0;
@@ -73,6 +116,22 @@ int launch_pack(const uint8_t *res, const uint64_t *starts, const uint32_t *lens
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
   pack_kernel<<<want < cap ? want : cap, 256, 0, s>>>(res, starts, lens, n, offs, packed);
+  NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+int launch_pack_layout(const uint8_t *res, const uint64_t *starts, const uint32_t *lens,
+                       uint32_t n, const uint64_t *offs, uint32_t *packed, uint32_t *nib,
+                       uint32_t *presence, cudaStream_t s) {
+  NGIA_CUDA(cudaMemsetAsync(presence, 0, sizeof(uint32_t), s));
+  if (n == 0) return NGIA_OK;
+  NGIA_TRY(upload_table());
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
+  pack_layout_kernel<<<want < cap ? want : cap, 256, 0, s>>>(res, starts, lens, n, offs, packed,
+                                                             nib, presence);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

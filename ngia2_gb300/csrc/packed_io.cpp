@@ -1,10 +1,13 @@
 // packed_io.cpp -- host side of makedb and of the packed/result files.
 //
 // makedb (src/main.cu:54-83) = check (src/makedb.hpp:59-91) + makeIndex
-// (:94-156) + packData (:159-286) + groupSignatures (:289-364).  Indexing and
-// packing are file-bound and stay on the host (multi-threaded, the input
-// mapped read-only); sketching and bucketing run on the device through the C
-// ABI; the file layout and every byte of it are the reference's.
+// (:94-156) + packData (:159-286) + groupSignatures (:289-364).  The host
+// indexes the FASTA (all threads: record starts found per chunk, records
+// measured in parallel), creates the packed file at its final size and writes
+// its header and cleaned FASTA records into the mapped file; the device packs
+// the residues of that FASTA area into bit planes, sketches and buckets them,
+// and its planes and rep rows are copied into the mapped file -- every byte of
+// the file is written once, and every byte is the reference's.
 #include <fcntl.h>
 #include <sys/mman.h>
 #include <sys/stat.h>
@@ -12,6 +15,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <thread>
@@ -20,44 +24,71 @@
 
 namespace ngia {
 
-namespace {
+bool InFile::open(const std::string &path) {
+  fd = ::open(path.c_str(), O_RDONLY);
+  if (fd < 0) return false;
+  struct stat st;
+  if (fstat(fd, &st) != 0) return false;
+  size = (uint64_t)st.st_size;
+  if (size == 0) return true;
+  void *p = mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
+  if (p == MAP_FAILED) return false;
+  data = static_cast<const char *>(p);
+  madvise(p, size, MADV_WILLNEED);
+  return true;
+}
 
-struct MappedFile {
-  const char *data = nullptr;
-  size_t size = 0;
-  int fd = -1;
-  bool open(const std::string &path) {
-    fd = ::open(path.c_str(), O_RDONLY);
-    if (fd < 0) return false;
-    struct stat st;
-    if (fstat(fd, &st) != 0) return false;
-    size = (size_t)st.st_size;
-    if (size == 0) return true;
-    void *p = mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
-    if (p == MAP_FAILED) return false;
-    data = static_cast<const char *>(p);
-    madvise(p, size, MADV_WILLNEED);
-    return true;
-  }
-  ~MappedFile() {
-    if (data) munmap(const_cast<char *>(data), size);
-    if (fd >= 0) ::close(fd);
-  }
-};
+void InFile::close_file() {
+  if (data) munmap(const_cast<char *>(data), size);
+  if (fd >= 0) ::close(fd);
+  data = nullptr;
+  fd = -1;
+  size = 0;
+}
 
-unsigned worker_count() {
+InFile::~InFile() { close_file(); }
+
+int OutFile::create(const std::string &path, uint64_t bytes) {
+  fd = ::open(path.c_str(), O_RDWR | O_CREAT | O_TRUNC, 0644);
+  if (fd < 0) return NGIA_ERR_IO;
+  size = bytes;
+  if (bytes == 0) return NGIA_OK;
+  if (ftruncate(fd, (off_t)bytes) != 0) return NGIA_ERR_IO;
+  void *p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_SHARED, fd, 0);
+  if (p == MAP_FAILED) return NGIA_ERR_IO;
+  data = static_cast<char *>(p);
+  return NGIA_OK;
+}
+
+int OutFile::close_file() {
+  bool ok = true;
+  if (data) ok = munmap(data, size) == 0;
+  data = nullptr;
+  if (fd >= 0) ok = (::close(fd) == 0) && ok;
+  fd = -1;
+  return ok ? NGIA_OK : NGIA_ERR_IO;
+}
+
+OutFile::~OutFile() { close_file(); }
+
+static unsigned worker_count() {
   unsigned t = std::thread::hardware_concurrency();
   return t ? t : 4;
 }
 
-template <typename F>
-void parallel_for(size_t n, F &&f) {  // f(begin, end) over chunks, dynamic
-  const unsigned nt = worker_count();
-  const size_t chunk = std::max<size_t>(1, std::min<size_t>(4096, n / (nt * 8) + 1));
-  std::atomic<size_t> next(0);
+void host_parallel_for(uint64_t n, uint64_t grain,
+                       const std::function<void(uint64_t, uint64_t)> &f) {
+  if (n == 0) return;
+  const unsigned nt = (unsigned)std::min<uint64_t>(worker_count(), (n + grain - 1) / grain);
+  if (nt <= 1) {
+    f(0, n);
+    return;
+  }
+  const uint64_t chunk = std::max<uint64_t>(grain, std::min<uint64_t>(1 << 16, n / (nt * 8) + 1));
+  std::atomic<uint64_t> next(0);
   auto work = [&]() {
     for (;;) {
-      const size_t b = next.fetch_add(chunk);
+      const uint64_t b = next.fetch_add(chunk);
       if (b >= n) return;
       f(b, std::min(n, b + chunk));
     }
@@ -68,12 +99,16 @@ void parallel_for(size_t n, F &&f) {  // f(begin, end) over chunks, dynamic
   for (auto &th : pool) th.join();
 }
 
-bool write_at(FILE *f, uint64_t off, const void *p, size_t bytes) {
-  if (fseeko(f, (off_t)off, SEEK_SET) != 0) return false;
-  return bytes == 0 || fwrite(p, 1, bytes, f) == bytes;
-}
+PhaseClock::PhaseClock()
+    : t0(std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+             .count()) {}
 
-}  // namespace
+void PhaseClock::lap(const char *what) {
+  const double t1 =
+      std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  std::printf("  [%s]\t%.6f s\n", what, t1 - t0);
+  t0 = t1;
+}
 
 uint32_t residue_code(unsigned char c) {
   // A reduced 15-letter alphabet shared by protein and nucleotide letters;
@@ -98,199 +133,258 @@ uint32_t residue_code(unsigned char c) {
   }
 }
 
-int check_fasta(const std::string &path, std::string &why) {
-  MappedFile f;
-  if (!f.open(path)) {
-    why = path + " does not exist.";
-    return NGIA_ERR_IO;
-  }
-  // first line must not end with '\r'
-  size_t eol = 0;
-  while (eol < f.size && f.data[eol] != '\n') ++eol;
-  if (eol > 0 && f.data[eol - 1] == '\r') {
+static int check_fasta_text(const char *d, uint64_t size, std::string &why) {
+  // first line must not end with '\r'; the file must end with '\n'
+  const void *nl = size ? memchr(d, '\n', size) : nullptr;
+  const uint64_t eol = nl ? (uint64_t)(static_cast<const char *>(nl) - d) : size;
+  if (eol > 0 && d[eol - 1] == '\r') {
     why = "Please remove the \\r at the end of lines.";
     return NGIA_ERR_FORMAT;
   }
-  if (f.size > 0 && f.data[f.size - 1] != '\n') {
+  if (size > 0 && d[size - 1] != '\n') {
     why = "File must end with \\n.";
     return NGIA_ERR_FORMAT;
   }
   return NGIA_OK;
 }
 
-int make_index(const std::string &path, std::vector<SeqIndex> &idx, uint64_t *scanned) {
-  MappedFile f;
-  if (!f.open(path)) return NGIA_ERR_IO;
-  idx.clear();
-  uint64_t whole = 0;
-  size_t pos = 0;
-  const char *d = f.data;
-  const size_t n = f.size;
-  while (pos < n) {
-    SeqIndex s;
-    s.fasta_offset = pos;
-    size_t e = pos;
-    while (e < n && d[e] != '\n') ++e;
-    s.name_len = (uint32_t)(e - pos);
-    uint64_t rec = (e - pos) + 1;
-    uint64_t rl = 0;
-    pos = e < n ? e + 1 : n;
-    while (pos < n && d[pos] != '>') {  // sequence lines
-      size_t q = pos;
-      const void *nl = memchr(d + pos, '\n', n - pos);
-      q = nl ? (size_t)(static_cast<const char *>(nl) - d) : n;
-      rl += q - pos;
-      rec += (q - pos) + 1;
-      pos = q < n ? q + 1 : n;
-    }
-    s.read_len = rl > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)rl;
-    s.record_bytes = rec;
-    ++whole;
-    if (rl < 0xFFFF) idx.push_back(s);
+int check_fasta(const std::string &path, std::string &why) {
+  InFile f;
+  if (!f.open(path)) {
+    why = path + " does not exist.";
+    return NGIA_ERR_IO;
   }
-  std::stable_sort(idx.begin(), idx.end(), [](const SeqIndex &a, const SeqIndex &b) {
-    return a.read_len > b.read_len;
+  return check_fasta_text(f.data, f.size, why);
+}
+
+// MakeDB::makeIndex (src/makedb.hpp:94-156).  A record starts at offset 0 and
+// at every line that begins with '>'; its first line is the name, the lines up
+// to the next record are the read.  The record starts are found per chunk of
+// the text, the records are measured in parallel, then reads of length >=
+// 0xFFFF are dropped and the rest ordered by length, longest first, stably (a
+// counting sort over the 65,535 possible lengths).
+int make_index_text(const char *d, uint64_t n, std::vector<SeqIndex> &idx, uint64_t *scanned) {
+  idx.clear();
+  if (scanned) *scanned = 0;
+  if (n == 0) return NGIA_OK;
+  const uint64_t parts = std::max<uint64_t>(1, std::min<uint64_t>(worker_count() * 4, n >> 16));
+  std::vector<std::vector<uint64_t>> found(parts);
+  host_parallel_for(parts, 1, [&](uint64_t b, uint64_t e) {
+    for (uint64_t k = b; k < e; ++k) {
+      const uint64_t lo = n * k / parts, hi = n * (k + 1) / parts;
+      std::vector<uint64_t> &f = found[k];
+      if (lo == 0) f.push_back(0);
+      // starts i in [lo, hi), i > 0: a newline at i - 1 in [lo - 1, hi - 1)
+      uint64_t p = lo > 0 ? lo - 1 : 0;
+      const uint64_t stop = hi > 0 ? hi - 1 : 0;
+      while (p < stop) {
+        const void *q = memchr(d + p, '\n', stop - p);
+        if (!q) break;
+        const uint64_t at = (uint64_t)(static_cast<const char *>(q) - d);
+        if (at + 1 < n && d[at + 1] == '>') f.push_back(at + 1);
+        p = at + 1;
+      }
+    }
   });
-  if (scanned) *scanned = whole;
+  std::vector<uint64_t> starts;
+  size_t total = 0;
+  for (auto &f : found) total += f.size();
+  starts.reserve(total);
+  for (auto &f : found) starts.insert(starts.end(), f.begin(), f.end());
+  found.clear();
+  const uint64_t R = starts.size();
+  std::vector<SeqIndex> all(R);
+  host_parallel_for(R, 256, [&](uint64_t b, uint64_t e) {
+    for (uint64_t r = b; r < e; ++r) {
+      const uint64_t s = starts[r], end = r + 1 < R ? starts[r + 1] : n;
+      const void *nl = memchr(d + s, '\n', end - s);
+      const uint64_t ne = nl ? (uint64_t)(static_cast<const char *>(nl) - d) : end;
+      SeqIndex x;
+      x.fasta_offset = s;
+      x.name_len = (uint32_t)(ne - s);
+      uint64_t rl = 0, rec = (ne - s) + 1;
+      uint64_t pos = ne < end ? ne + 1 : end;
+      while (pos < end) {  // the read's lines
+        const void *q = memchr(d + pos, '\n', end - pos);
+        const uint64_t qe = q ? (uint64_t)(static_cast<const char *>(q) - d) : end;
+        rl += qe - pos;
+        rec += (qe - pos) + 1;
+        pos = qe < end ? qe + 1 : end;
+      }
+      x.read_len = rl > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)rl;
+      x.record_bytes = rec;
+      all[r] = x;
+    }
+  });
+  if (scanned) *scanned = R;
+  // stable, length descending: key 0xFFFE - len over the kept reads
+  std::vector<uint32_t> count(0x10000, 0u);
+  uint64_t kept = 0;
+  for (const SeqIndex &x : all)
+    if (x.read_len < 0xFFFF) {
+      ++count[0xFFFEu - x.read_len + 1];
+      ++kept;
+    }
+  for (size_t k = 1; k < count.size(); ++k) count[k] += count[k - 1];
+  idx.resize(kept);
+  for (const SeqIndex &x : all)
+    if (x.read_len < 0xFFFF) idx[count[0xFFFEu - x.read_len]++] = x;
   return NGIA_OK;
 }
 
-int write_packed_without_sigs(const std::string &fasta, const std::string &out,
-                              const std::vector<SeqIndex> &idx, PackedDb &db) {
-  MappedFile in;
-  if (!in.open(fasta)) return NGIA_ERR_IO;
+int make_index(const std::string &path, std::vector<SeqIndex> &idx, uint64_t *scanned) {
+  InFile f;
+  if (!f.open(path)) return NGIA_ERR_IO;
+  return make_index_text(f.data, f.size, idx, scanned);
+}
+
+int makedb_prepare(const std::string &fasta, const std::string &out, Makedb &m) {
+  if (!m.in.open(fasta)) return NGIA_ERR_IO;
+  std::string why;
+  NGIA_TRY_HOST(check_fasta_text(m.in.data, m.in.size, why));
+  std::vector<SeqIndex> idx;
+  NGIA_TRY_HOST(make_index_text(m.in.data, m.in.size, idx, &m.scanned));
+  if (idx.empty()) return NGIA_ERR_FORMAT;
+  if (idx.size() >= 0x7FFFFFFFull) return NGIA_ERR_ARG;
   const uint32_t n = (uint32_t)idx.size();
-  db = PackedDb();
-  db.n = n;
-  db.name_lens.resize(n);
-  db.lens.resize(n);
-  db.pack_off.resize(n);
-  db.fasta_off.resize(n);
-  db.offsets.resize(n);
-  uint64_t words = 0;
+  m.n = n;
+  m.name_lens.resize(n);
+  m.lens.resize(n);
+  m.offsets.resize(n);
+  m.text_starts.resize(n);
+  std::vector<uint64_t> frel(n);  // each record's FASTA-area offset
+  uint64_t words = 0, fbytes = 0;
   for (uint32_t i = 0; i < n; ++i) {
-    db.name_lens[i] = idx[i].name_len;
-    db.lens[i] = idx[i].read_len;
-    db.offsets[i] = words;
+    m.name_lens[i] = idx[i].name_len;
+    m.lens[i] = idx[i].read_len;
+    m.offsets[i] = words;
     words += 1 + (uint64_t)((idx[i].read_len + 31u) / 32u) * 4u;
-  }
-  const uint64_t pack0 = packed_area_offset(n);
-  for (uint32_t i = 0; i < n; ++i) db.pack_off[i] = pack0 + db.offsets[i] * 4;
-  const uint64_t fasta0 = pack0 + words * 4;
-  std::vector<uint64_t> frel(n);
-  uint64_t fbytes = 0;
-  for (uint32_t i = 0; i < n; ++i) {
     frel[i] = fbytes;
-    db.fasta_off[i] = fasta0 + fbytes;
+    m.text_starts[i] = fbytes + idx[i].name_len + 1;
     fbytes += (uint64_t)idx[i].name_len + idx[i].read_len + 2;
   }
-  db.packed.assign(words, 0u);
-  std::vector<char> farea(fbytes);
-  const char *src = in.data;
-  parallel_for(n, [&](size_t b, size_t e) {
-    for (size_t i = b; i < e; ++i) {
+  m.words = words;
+  m.pack0 = packed_area_offset(n);
+  m.fasta0 = m.pack0 + words * 4;
+  m.size = m.fasta0 + fbytes;
+  NGIA_TRY_HOST(m.file.create(out, m.size));
+  char *o = m.file.data;
+  // header (src/makedb.hpp:179-197): n, name lengths, read lengths, packed and
+  // FASTA offsets; the signature area and the planes come from the device
+  std::memcpy(o, &n, 4);
+  std::memcpy(o + 4, m.name_lens.data(), 4ull * n);
+  std::memcpy(o + 4 + 4ull * n, m.lens.data(), 4ull * n);
+  host_parallel_for(n, 4096, [&](uint64_t b, uint64_t e) {
+    for (uint64_t i = b; i < e; ++i) {
+      const uint64_t po = m.pack0 + m.offsets[i] * 4, fo = m.fasta0 + frel[i];
+      std::memcpy(o + 4 + 8ull * n + 8 * i, &po, 8);
+      std::memcpy(o + 4 + 16ull * n + 8 * i, &fo, 8);
+    }
+  });
+  // cleaned FASTA records "name\nread\n" in index order (the read on one line)
+  const char *src = m.in.data;
+  host_parallel_for(n, 64, [&](uint64_t b, uint64_t e) {
+    for (uint64_t i = b; i < e; ++i) {
       const SeqIndex &s = idx[i];
       const char *rec = src + s.fasta_offset;
-      char *fo = farea.data() + frel[i];
+      char *fo = o + m.fasta0 + frel[i];
       std::memcpy(fo, rec, s.name_len);
       fo[s.name_len] = '\n';
       char *ro = fo + s.name_len + 1;
-      uint32_t *pk = db.packed.data() + db.offsets[i];
-      pk[0] = s.read_len;
-      uint32_t p = 0;
       const char *q = rec + s.name_len + 1;
       const char *qe = rec + s.record_bytes;
-      for (; q < qe; ++q) {
-        const char ch = *q;
-        if (ch == '\n') continue;
-        ro[p] = ch;
-        const uint32_t code = residue_code((unsigned char)ch);
-        uint32_t *blk = pk + 1 + (p >> 5) * 4;
-        const uint32_t bit = 1u << (p & 31u);
-        if (code & 1u) blk[0] |= bit;
-        if (code & 2u) blk[1] |= bit;
-        if (code & 4u) blk[2] |= bit;
-        if (code & 8u) blk[3] |= bit;
-        ++p;
+      if (qe > src + m.in.size) qe = src + m.in.size;
+      while (q < qe) {
+        const void *nl = memchr(q, '\n', (size_t)(qe - q));
+        const char *le = nl ? static_cast<const char *>(nl) : qe;
+        std::memcpy(ro, q, (size_t)(le - q));
+        ro += le - q;
+        q = le + 1;
       }
-      ro[p] = '\n';
+      *ro = '\n';
     }
   });
-  FILE *f = fopen(out.c_str(), "wb");
-  if (!f) return NGIA_ERR_IO;
-  std::vector<char> big(1 << 22);
-  setvbuf(f, big.data(), _IOFBF, big.size());
-  bool ok = fwrite(&n, 4, 1, f) == 1;
-  ok = ok && fwrite(db.name_lens.data(), 4, n, f) == n;
-  ok = ok && fwrite(db.lens.data(), 4, n, f) == n;
-  ok = ok && fwrite(db.pack_off.data(), 8, n, f) == n;
-  ok = ok && fwrite(db.fasta_off.data(), 8, n, f) == n;
-  std::vector<uint32_t> zeros((size_t)NGIA_BANDS * n, 0u);
-  ok = ok && fwrite(zeros.data(), 4, zeros.size(), f) == zeros.size();
-  ok = ok && fwrite(db.packed.data(), 4, db.packed.size(), f) == db.packed.size();
-  ok = ok && fwrite(farea.data(), 1, farea.size(), f) == farea.size();
-  ok = (fflush(f) == 0) && ok;
-  ok = (fclose(f) == 0) && ok;
-  if (!ok) return NGIA_ERR_IO;
-  // size check of packData (src/makedb.hpp:271-284)
-  struct stat st;
-  if (stat(out.c_str(), &st) != 0) return NGIA_ERR_IO;
-  if ((uint64_t)st.st_size != fasta0 + fbytes) return NGIA_ERR_IO;
   return NGIA_OK;
 }
 
-int write_rep_rows(const std::string &out, uint32_t n, const std::vector<uint32_t> &rep) {
-  FILE *f = fopen(out.c_str(), "r+b");
-  if (!f) return NGIA_ERR_IO;
-  bool ok = write_at(f, sig_area_offset(n), rep.data(), rep.size() * 4);
-  ok = (fflush(f) == 0) && ok;
-  ok = (fclose(f) == 0) && ok;
-  return ok ? NGIA_OK : NGIA_ERR_IO;
+int makedb_finish(Makedb &m) {
+  NGIA_TRY_HOST(m.file.close_file());
+  m.in.close_file();
+  return NGIA_OK;
 }
 
-int read_packed(const std::string &path, uint32_t rep_bands, PackedDb &db) {
-  MappedFile f;
-  if (!f.open(path)) return NGIA_ERR_IO;
-  db = PackedDb();
+static int check_packed_header(const InFile &f, uint32_t &n, uint64_t &words) {
   if (f.size < 4) return NGIA_ERR_FORMAT;
-  uint32_t n = 0;
   std::memcpy(&n, f.data, 4);
   if (n == 0) return NGIA_ERR_FORMAT;
   const uint64_t pack0 = packed_area_offset(n);
   if (f.size < pack0) return NGIA_ERR_FORMAT;
+  uint64_t p0, fasta0;
+  std::memcpy(&p0, f.data + 4 + 8ull * n, 8);
+  std::memcpy(&fasta0, f.data + 4 + 16ull * n, 8);
+  if (p0 != pack0) return NGIA_ERR_FORMAT;
+  if (fasta0 < pack0 || fasta0 > f.size || ((fasta0 - pack0) & 3u)) return NGIA_ERR_FORMAT;
+  words = (fasta0 - pack0) / 4;
+  return NGIA_OK;
+}
+
+// Record offsets (file bytes -> packed-area words), each record inside the
+// area; rep rows below n.  All host threads.
+static int check_records(const InFile &f, uint32_t n, uint64_t words, const uint32_t *lens,
+                         uint32_t rep_bands, std::vector<uint64_t> &offsets) {
+  const uint64_t pack0 = packed_area_offset(n), fasta0 = pack0 + 4 * words;
+  offsets.resize(n);
+  std::atomic<int> bad(0);
+  host_parallel_for(n, 4096, [&](uint64_t b, uint64_t e) {
+    bool wrong = false;
+    for (uint64_t i = b; i < e; ++i) {
+      uint64_t o;
+      std::memcpy(&o, f.data + 4 + 8ull * n + 8 * i, 8);
+      wrong |= o < pack0 || o >= fasta0 || ((o - pack0) & 3u);
+      const uint64_t w = (o - pack0) / 4;
+      offsets[i] = w;
+      wrong |= w + 1 + (uint64_t)((lens[i] + 31u) / 32u) * 4u > words;
+    }
+    if (wrong) bad.store(1);
+  });
+  if (rep_bands) {
+    const uint32_t *rep = reinterpret_cast<const uint32_t *>(f.data + sig_area_offset(n));
+    host_parallel_for((uint64_t)rep_bands * n, 1 << 16, [&](uint64_t b, uint64_t e) {
+      uint32_t mx = 0;
+      for (uint64_t k = b; k < e; ++k) mx = std::max(mx, rep[k]);
+      if (mx >= n) bad.store(1);
+    });
+  }
+  return bad.load() ? NGIA_ERR_FORMAT : NGIA_OK;
+}
+
+int open_packed(const std::string &path, uint32_t rep_bands, PackedView &v) {
+  if (!v.f.open(path)) return NGIA_ERR_IO;
+  NGIA_TRY_HOST(check_packed_header(v.f, v.n, v.words));
+  const uint32_t n = v.n;
+  const char *d = v.f.data;
+  v.name_lens = reinterpret_cast<const uint32_t *>(d + 4);
+  v.lens = reinterpret_cast<const uint32_t *>(d + 4 + 4ull * n);
+  v.rep = reinterpret_cast<const uint32_t *>(d + sig_area_offset(n));
+  v.packed = reinterpret_cast<const uint32_t *>(d + packed_area_offset(n));
+  return check_records(v.f, n, v.words, v.lens, rep_bands, v.offsets);
+}
+
+int read_packed(const std::string &path, uint32_t rep_bands, PackedDb &db) {
+  PackedView v;
+  NGIA_TRY_HOST(open_packed(path, rep_bands, v));
+  const uint32_t n = v.n;
+  db = PackedDb();
   db.n = n;
-  db.name_lens.resize(n);
-  db.lens.resize(n);
+  db.name_lens.assign(v.name_lens, v.name_lens + n);
+  db.lens.assign(v.lens, v.lens + n);
   db.pack_off.resize(n);
   db.fasta_off.resize(n);
-  const char *p = f.data + 4;
-  std::memcpy(db.name_lens.data(), p, 4ull * n);
-  p += 4ull * n;
-  std::memcpy(db.lens.data(), p, 4ull * n);
-  p += 4ull * n;
-  std::memcpy(db.pack_off.data(), p, 8ull * n);
-  p += 8ull * n;
-  std::memcpy(db.fasta_off.data(), p, 8ull * n);
-  if (db.pack_off[0] != pack0) return NGIA_ERR_FORMAT;
-  const uint64_t fasta0 = db.fasta_off[0];
-  if (fasta0 < pack0 || fasta0 > f.size || ((fasta0 - pack0) & 3u)) return NGIA_ERR_FORMAT;
-  const uint64_t words = (fasta0 - pack0) / 4;
-  db.offsets.resize(n);
-  for (uint32_t i = 0; i < n; ++i) {
-    const uint64_t o = db.pack_off[i];
-    if (o < pack0 || o >= fasta0 || ((o - pack0) & 3u)) return NGIA_ERR_FORMAT;
-    db.offsets[i] = (o - pack0) / 4;
-    const uint64_t need = 1 + (uint64_t)((db.lens[i] + 31u) / 32u) * 4u;
-    if (db.offsets[i] + need > words) return NGIA_ERR_FORMAT;
-  }
-  db.packed.resize(words);
-  std::memcpy(db.packed.data(), f.data + pack0, words * 4);
-  if (rep_bands) {
-    db.rep.resize((size_t)rep_bands * n);
-    std::memcpy(db.rep.data(), f.data + sig_area_offset(n), 4ull * rep_bands * n);
-    for (uint32_t v : db.rep)
-      if (v >= n) return NGIA_ERR_FORMAT;
-  }
+  std::memcpy(db.pack_off.data(), v.f.data + 4 + 8ull * n, 8ull * n);
+  std::memcpy(db.fasta_off.data(), v.f.data + 4 + 16ull * n, 8ull * n);
+  db.offsets = std::move(v.offsets);
+  db.packed.assign(v.packed, v.packed + v.words);
+  if (rep_bands) db.rep.assign(v.rep, v.rep + (size_t)rep_bands * n);
   return NGIA_OK;
 }
 
@@ -302,49 +396,37 @@ int ngia_makedb(const char *fasta_path, const char *packed_path, uint32_t *n_out
   using namespace ngia;
   if (!fasta_path || !packed_path) return NGIA_ERR_ARG;
   if (n_out) *n_out = 0;
-  std::string why;
-  NGIA_TRY_HOST(check_fasta(fasta_path, why));
-  std::vector<SeqIndex> idx;
-  uint64_t scanned = 0;
-  NGIA_TRY_HOST(make_index(fasta_path, idx, &scanned));
-  if (idx.empty()) return NGIA_ERR_FORMAT;
-  if (idx.size() >= 0x7FFFFFFFull) return NGIA_ERR_ARG;
-  PackedDb db;
-  NGIA_TRY_HOST(write_packed_without_sigs(fasta_path, packed_path, idx, db));
-  idx.clear();
-  idx.shrink_to_fit();
+  Makedb m;
+  NGIA_TRY_HOST(makedb_prepare(fasta_path, packed_path, m));
   ngia_ctx *ctx = nullptr;
   NGIA_TRY_HOST(ngia_ctx_create(&ctx, nullptr));
-  int st = ngia_ctx_load(ctx, db.packed.data(), db.packed.size(), db.offsets.data(),
-                         db.lens.data(), db.n, nullptr, NGIA_BANDS);
-  if (st == NGIA_OK) st = ngia_ctx_sketch_bucket(ctx, NGIA_BANDS);
-  std::vector<uint32_t> rep;
-  if (st == NGIA_OK) {
-    rep.resize((size_t)NGIA_BANDS * db.n);
-    st = ngia_ctx_rep_rows(ctx, rep.data(), NGIA_BANDS);
-  }
+  const int st = makedb_device(ctx, m);
   ngia_ctx_destroy(ctx);
   if (st != NGIA_OK) return st;
-  NGIA_TRY_HOST(write_rep_rows(packed_path, db.n, rep));
-  if (n_out) *n_out = db.n;
+  NGIA_TRY_HOST(makedb_finish(m));
+  // size check of packData (src/makedb.hpp:271-284)
+  struct stat sb;
+  if (stat(packed_path, &sb) != 0 || (uint64_t)sb.st_size != m.size) return NGIA_ERR_IO;
+  if (n_out) *n_out = m.n;
   return NGIA_OK;
 }
 
+// SaveResult::save (src/saveResult.hpp:31-83): clusters in ascending id, the
+// representative (smallest index) as its name line and read line, every other
+// member as "  " + its name line, in index order.  The line lengths are
+// measured and the output laid out first, then all threads fill the mapped
+// result file.
 int ngia_save_result(const uint32_t *h_cluster, uint32_t n, const char *packed_path,
                      const char *result_path) {
   using namespace ngia;
   if (!h_cluster || !packed_path || !result_path || n == 0) return NGIA_ERR_ARG;
-  MappedFile f;
+  InFile f;
   if (!f.open(packed_path) || f.size < 4) return NGIA_ERR_IO;
   uint32_t fn = 0;
   std::memcpy(&fn, f.data, 4);
   if (fn != n || f.size < packed_area_offset(n)) return NGIA_ERR_FORMAT;
-  std::vector<uint32_t> name_lens(n), lens(n);
   std::vector<uint64_t> fasta_off(n);
-  std::memcpy(name_lens.data(), f.data + 4, 4ull * n);
-  std::memcpy(lens.data(), f.data + 4 + 4ull * n, 4ull * n);
   std::memcpy(fasta_off.data(), f.data + 4 + 16ull * n, 8ull * n);
-  // clusters in ascending id order, members in ascending index order
   uint32_t max_id = 0;
   for (uint32_t i = 0; i < n; ++i) max_id = std::max(max_id, h_cluster[i]);
   std::vector<uint32_t> start((size_t)max_id + 2, 0);
@@ -352,42 +434,56 @@ int ngia_save_result(const uint32_t *h_cluster, uint32_t n, const char *packed_p
   for (size_t c = 0; c <= max_id; ++c) start[c + 1] += start[c];
   std::vector<uint32_t> members(n), cur(start.begin(), start.end() - 1);
   for (uint32_t i = 0; i < n; ++i) members[cur[h_cluster[i]]++] = i;
-  FILE *out = fopen(result_path, "wb");
-  if (!out) return NGIA_ERR_IO;
-  std::vector<char> big(1 << 22);
-  setvbuf(out, big.data(), _IOFBF, big.size());
-  bool ok = true;
-  auto line_at = [&](uint64_t off, const char **s, size_t *len) {
-    // one line of the FASTA area, without its newline
-    if (off >= f.size) {
-      *s = f.data + f.size;
-      *len = 0;
-      return;
-    }
+  // one line of the FASTA area, without its newline
+  auto line_len = [&](uint64_t off) -> uint64_t {
+    if (off >= f.size) return 0;
     const void *nl = memchr(f.data + off, '\n', f.size - off);
-    const size_t e = nl ? (size_t)(static_cast<const char *>(nl) - f.data) : f.size;
-    *s = f.data + off;
-    *len = e - off;
+    return (nl ? (uint64_t)(static_cast<const char *>(nl) - f.data) : f.size) - off;
   };
-  for (size_t c = 0; c <= max_id && ok; ++c) {
-    const uint32_t b = start[c], e = start[c + 1];
-    if (b == e) continue;
-    const uint32_t r = members[b];
-    const char *s;
-    size_t len;
-    line_at(fasta_off[r], &s, &len);
-    ok = ok && fwrite(s, 1, len, out) == len && fputc('\n', out) != EOF;
-    const uint64_t seq_off = fasta_off[r] + len + 1;
-    line_at(seq_off, &s, &len);
-    ok = ok && fwrite(s, 1, len, out) == len && fputc('\n', out) != EOF;
-    for (uint32_t k = b + 1; k < e && ok; ++k) {
-      line_at(fasta_off[members[k]], &s, &len);
-      ok = fputs("  ", out) != EOF && fwrite(s, 1, len, out) == len && fputc('\n', out) != EOF;
+  std::vector<uint64_t> name_len(n), seq_len(n, 0);
+  host_parallel_for(n, 1024, [&](uint64_t b, uint64_t e) {
+    for (uint64_t i = b; i < e; ++i) name_len[i] = line_len(fasta_off[i]);
+  });
+  const uint64_t nclu = (uint64_t)max_id + 1;
+  std::vector<uint64_t> at(nclu + 1, 0);  // output offset of each cluster
+  host_parallel_for(nclu, 1024, [&](uint64_t b, uint64_t e) {
+    for (uint64_t c = b; c < e; ++c) {
+      const uint32_t lo = start[c], hi = start[c + 1];
+      if (lo == hi) continue;
+      const uint32_t r = members[lo];
+      seq_len[r] = line_len(fasta_off[r] + name_len[r] + 1);
+      uint64_t bytes = name_len[r] + 1 + seq_len[r] + 1;
+      for (uint32_t k = lo + 1; k < hi; ++k) bytes += 2 + name_len[members[k]] + 1;
+      at[c + 1] = bytes;
     }
-  }
-  ok = (fflush(out) == 0) && ok;
-  ok = (fclose(out) == 0) && ok;
-  return ok ? NGIA_OK : NGIA_ERR_IO;
+  });
+  for (uint64_t c = 0; c < nclu; ++c) at[c + 1] += at[c];
+  OutFile out;
+  NGIA_TRY_HOST(out.create(result_path, at[nclu]));
+  host_parallel_for(nclu, 1024, [&](uint64_t b, uint64_t e) {
+    for (uint64_t c = b; c < e; ++c) {
+      const uint32_t lo = start[c], hi = start[c + 1];
+      if (lo == hi) continue;
+      char *o = out.data + at[c];
+      const uint32_t r = members[lo];
+      if (name_len[r]) std::memcpy(o, f.data + fasta_off[r], name_len[r]);
+      o += name_len[r];
+      *o++ = '\n';
+      const uint64_t so = fasta_off[r] + name_len[r] + 1;
+      if (seq_len[r]) std::memcpy(o, f.data + so, seq_len[r]);
+      o += seq_len[r];
+      *o++ = '\n';
+      for (uint32_t k = lo + 1; k < hi; ++k) {
+        const uint32_t i = members[k];
+        *o++ = ' ';
+        *o++ = ' ';
+        if (name_len[i]) std::memcpy(o, f.data + fasta_off[i], name_len[i]);
+        o += name_len[i];
+        *o++ = '\n';
+      }
+    }
+  });
+  return out.close_file();
 }
 
 }  // extern "C"

@@ -109,7 +109,6 @@ collect_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict__ le
 // writes nothing.
 constexpr unsigned long long kStAgg = 1ull << 62, kStIncl = 2ull << 62;
 constexpr unsigned long long kStValue = (1ull << 62) - 1;
-constexpr uint32_t kLookbackSpins = 1u << 22;
 
 __global__ void __launch_bounds__(kPairThreads)
 collect_scan_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict__ lens,
@@ -117,7 +116,7 @@ collect_scan_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict
                     unsigned long long *__restrict__ status,
                     unsigned long long *__restrict__ cand_total,
                     uint64_t *__restrict__ unique_total, unsigned int *__restrict__ error,
-                    uint2 *__restrict__ pairs) {
+                    uint2 *__restrict__ pairs, uint32_t spin_limit) {
   __shared__ uint32_t tile[kBands * kTargetsPerBlock];
   __shared__ uint32_t vals[kPairThreads / 32][32];
   __shared__ uint32_t toff[kTargetsPerBlock];
@@ -128,6 +127,10 @@ collect_scan_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict
   __syncthreads();
   const uint32_t blk = blk_sh, i0 = blk * kTargetsPerBlock;
   const uint32_t nblocks = ceil_div(n, kTargetsPerBlock);
+  if (blk >= nblocks) {  // more tickets than blocks: only a check of the wait does this
+    if (threadIdx.x == 0) atomicOr(error, 1u);
+    return;
+  }
   for (uint32_t e = threadIdx.x; e < bands * kTargetsPerBlock; e += kPairThreads) {
     const uint32_t b = e / kTargetsPerBlock, c = e % kTargetsPerBlock;
     tile[e] = (i0 + c < n) ? rep[(size_t)b * n + i0 + c] : 0u;
@@ -171,7 +174,7 @@ collect_scan_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict
         for (int j = (int)blk - 1; j >= 0;) {
           const unsigned long long s = *(volatile unsigned long long *)(status + j);
           if ((s >> 62) == 0) {
-            if (++spins > kLookbackSpins) {  // a predecessor never published
+            if (++spins > spin_limit) {  // a predecessor never published
               atomicOr(error, 1u);
               ok = 0;
               break;
@@ -210,14 +213,14 @@ collect_scan_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict
 int collect_scan(const uint32_t *rep, const uint32_t *lens, uint32_t n, uint32_t bands,
                  uint32_t identity, unsigned int *ticket, unsigned long long *status,
                  unsigned long long *cand_total, uint64_t *unique_total, unsigned int *error,
-                 uint2 *pairs, cudaStream_t s) {
+                 uint2 *pairs, cudaStream_t s, uint32_t spin_limit) {
   if (n == 0) return NGIA_OK;
   const uint32_t nblocks = ceil_div(n, kTargetsPerBlock);
   NGIA_CUDA(cudaMemsetAsync(status, 0, (size_t)nblocks * 8, s));
   collect_scan_kernel<<<nblocks, kPairThreads, 0, s>>>(rep, lens, n, bands,
                                                        identity_threshold(identity), ticket,
                                                        status, cand_total, unique_total, error,
-                                                       pairs);
+                                                       pairs, spin_limit);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }
@@ -330,6 +333,79 @@ int classify(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t 
   }
   class_bounds_kernel<<<1, 32, 0, s>>>(class_count, bounds);
   NGIA_LAUNCHED();
+  return NGIA_OK;
+}
+
+// ---- shares of the pairs by band cells (a graph build split over devices) ----------
+// Band blocks of every pair (the reference's visited 32x32 blocks; 0 for a
+// pair failing the length filter).
+__global__ void __launch_bounds__(256)
+pair_blocks_kernel(const uint32_t *__restrict__ lens, const uint2 *__restrict__ pairs,
+                   uint32_t count, float t, int fma_mode, uint32_t *__restrict__ blocks) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < count;
+       p += gridDim.x * blockDim.x) {
+    const uint2 pr = pairs[p];
+    const uint64_t b = band_blocks(make_band(__ldg(lens + pr.x), __ldg(lens + pr.y), t, fma_mode));
+    blocks[p] = b < kFull ? (uint32_t)b : kFull;
+  }
+}
+
+// cut[k] for k = part, part + 1: the first pair whose exclusive prefix of
+// blocks reaches total * k / parts (0 and count at the ends).
+__global__ void part_cut_kernel(const uint64_t *__restrict__ prefix, uint32_t count,
+                                const uint64_t *__restrict__ total, uint32_t part, uint32_t parts,
+                                uint32_t *__restrict__ cut) {
+  const uint32_t k = part + threadIdx.x;
+  if (threadIdx.x > 1) return;
+  uint32_t c;
+  if (k == 0) {
+    c = 0;
+  } else if (k >= parts) {
+    c = count;
+  } else {
+    const uint64_t target = *total / parts * k + (*total % parts) * k / parts;
+    uint32_t lo = 0, hi = count;  // first index with prefix >= target
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if (prefix[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    c = lo;
+  }
+  cut[threadIdx.x] = c;
+}
+
+size_t share_scratch_bytes(uint32_t count) {
+  const size_t c = count ? count : 1;
+  return c * 4 + c * 8 + scan_scratch_bytes(count) + 64;
+}
+
+int share_range(const uint32_t *lens, const uint2 *pairs, uint32_t count, uint32_t identity,
+                uint32_t part, uint32_t parts, void *scratch, uint32_t h_cut[2],
+                cudaStream_t s) {
+  if (parts <= 1 || count == 0) {
+    h_cut[0] = 0;
+    h_cut[1] = count;
+    return NGIA_OK;
+  }
+  char *w = static_cast<char *>(scratch);
+  const size_t c = count;
+  uint32_t *blocks = reinterpret_cast<uint32_t *>(w);
+  uint64_t *prefix = reinterpret_cast<uint64_t *>(w + ((c * 4 + 15) & ~(size_t)15));
+  uint64_t *total = prefix + c;
+  uint32_t *cut = reinterpret_cast<uint32_t *>(total + 1);
+  void *scan_tmp = cut + 4;
+  int dev = 0, sms = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t want = ceil_div(count, 256u), cap = (uint32_t)sms * 8u;
+  pair_blocks_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
+      lens, pairs, count, identity_threshold(identity), round_mode(), blocks);
+  NGIA_LAUNCHED();
+  NGIA_TRY(exclusive_scan_u64(blocks, prefix, count, total, scan_tmp, s));
+  part_cut_kernel<<<1, 32, 0, s>>>(prefix, count, total, part, parts, cut);
+  NGIA_LAUNCHED();
+  NGIA_CUDA(cudaMemcpyAsync(h_cut, cut, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  NGIA_CUDA(cudaStreamSynchronize(s));
   return NGIA_OK;
 }
 

@@ -150,6 +150,7 @@ struct Slot {
 
 struct Server {
   ngia_server_config cfg{};
+  int device = 0;             // the device current at create; every buffer lives there
   uint32_t n = 0;             // database records
   uint64_t db_words = 0;
   Alphabet ab{16, 0};
@@ -203,8 +204,8 @@ static int run_request(Server *s, Slot *sl, Request *r) {
                             cudaMemcpyHostToDevice, st));
   NGIA_CUDA(cudaMemcpyAsync(offs, sl->h_offs, (size_t)q * 8, cudaMemcpyHostToDevice, st));
   NGIA_CUDA(cudaMemcpyAsync(lens, sl->h_lens, (size_t)q * 4, cudaMemcpyHostToDevice, st));
-  NGIA_TRY(launch_nibbles(packed, offs, q, s->nib.as<uint32_t>(), sl->presence.as<uint32_t>(),
-                          st));
+  NGIA_TRY(launch_nibbles(packed, offs, lens, q, sl->word_base + s->cfg.max_words,
+                          s->nib.as<uint32_t>(), sl->presence.as<uint32_t>(), st));
   if (s->recode_map)
     NGIA_TRY(launch_dense_layouts(packed, offs, q, s->recode_map, s->dense.as<uint32_t>(),
                                   s->dplanes.as<uint32_t>(), st));
@@ -248,30 +249,67 @@ static int run_request(Server *s, Slot *sl, Request *r) {
   return NGIA_OK;
 }
 
-static Slot *free_slot(Server *s) {
-  for (auto &sl : s->slots)
-    if (!sl->req) return sl.get();
+// A free slot for a request: slots below small_slots take only small
+// requests (a small one takes those first).
+static Slot *free_slot(Server *s, bool small) {
+  const uint32_t reserved = s->cfg.small_queries ? s->cfg.small_slots : 0u;
+  if (small)
+    for (uint32_t k = 0; k < reserved && k < s->slots.size(); ++k)
+      if (!s->slots[k]->req) return s->slots[k].get();
+  for (size_t k = reserved; k < s->slots.size(); ++k)
+    if (!s->slots[k]->req) return s->slots[k].get();
   return nullptr;
 }
 
+// The request to admit next and its slot: the first small request queued
+// (when small requests go first) if a slot takes it, else the front of the
+// queue; each within the HBM budget.
+static bool next_admission(Server *s, std::deque<Request *>::iterator *which, Slot **slot) {
+  auto fits = [&](const Request *r) {
+    return s->inflight == 0 || s->inflight + r->bytes <= s->cfg.hbm_budget;
+  };
+  if (s->cfg.small_queries) {
+    for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+      if ((*it)->q > s->cfg.small_queries) continue;
+      Slot *sl = free_slot(s, true);
+      if (sl && fits(*it)) {
+        *which = it;
+        *slot = sl;
+        return true;
+      }
+      break;
+    }
+  }
+  const Request *front = s->queue.front();
+  Slot *sl = free_slot(s, s->cfg.small_queries && front->q <= s->cfg.small_queries);
+  if (sl && fits(front)) {
+    *which = s->queue.begin();
+    *slot = sl;
+    return true;
+  }
+  return false;
+}
+
 static void dispatch_loop(Server *s) {
+  // a new thread starts on device 0: make the server's device current before
+  // any copy or launch on its streams
+  const cudaError_t dev_err = cudaSetDevice(s->device);
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
+    std::deque<Request *>::iterator which;
+    Slot *sl = nullptr;
     s->cv.wait(lk, [&] {
       if (s->queue.empty()) return s->stop;
-      const Request *r = s->queue.front();
-      return free_slot(s) != nullptr &&
-             (s->inflight == 0 || s->inflight + r->bytes <= s->cfg.hbm_budget);
+      return next_admission(s, &which, &sl);
     });
     if (s->queue.empty()) break;  // stopping, nothing left to admit
-    Request *r = s->queue.front();
-    s->queue.pop_front();
-    Slot *sl = free_slot(s);
+    Request *r = *which;
+    s->queue.erase(which);
     sl->req = r;
     s->inflight += r->bytes;
     r->t_admit = Clock::now();
     lk.unlock();
-    const int rc = run_request(s, sl, r);
+    const int rc = dev_err == cudaSuccess ? run_request(s, sl, r) : cuda_fail(dev_err);
     lk.lock();
     if (rc != NGIA_OK) {  // nothing more was enqueued after the failing call
       lk.unlock();
@@ -309,6 +347,7 @@ int ngia_server_create(ngia_server **out, ngia_ctx *db, const uint32_t *h_cluste
   if (cfg->identity < 1 || cfg->identity > 99 || cfg->slots < 1 || cfg->slots > 16 ||
       cfg->max_queries < 1 || cfg->max_words < 1)
     return NGIA_ERR_ARG;
+  if (cfg->small_queries && cfg->small_slots >= cfg->slots && !cfg->plain) return NGIA_ERR_ARG;
   ngia_server *s = new (std::nothrow) ngia_server();
   if (!s) return NGIA_ERR_NOMEM;
   const int rc = server_init(s, db, h_cluster, cfg);
@@ -324,9 +363,14 @@ int ngia_server_create(ngia_server **out, ngia_ctx *db, const uint32_t *h_cluste
 static int server_init(ngia_server *s, ngia_ctx *db, const uint32_t *h_cluster,
                        const ngia_server_config *cfg) {
   using namespace ngia;
+  NGIA_CUDA(cudaGetDevice(&s->device));
   if (!db->sigs_valid) NGIA_TRY(ctx_sketch_bucket(db, 1, nullptr));
   s->cfg = *cfg;
-  if (s->cfg.plain) s->cfg.slots = 1;
+  if (s->cfg.plain) {  // one slot, arrival order
+    s->cfg.slots = 1;
+    s->cfg.small_queries = s->cfg.small_slots = 0;
+  }
+  if (!s->cfg.small_queries) s->cfg.small_slots = 0;
   const uint32_t n = db->n, S = s->cfg.slots, Q = s->cfg.max_queries;
   const uint64_t W = s->cfg.max_words;
   s->n = n;
@@ -466,6 +510,11 @@ int ngia_server_wait(ngia_server *s, uint64_t ticket, uint32_t *h_cluster,
 
 void ngia_server_destroy(ngia_server *s) {
   if (!s) return;
+  // free on the server's device, whatever device the calling thread has current
+  int caller_dev = -1;
+  if (cudaGetDevice(&caller_dev) != cudaSuccess) caller_dev = -1;
+  const bool switched = caller_dev >= 0 && caller_dev != s->device &&
+                        cudaSetDevice(s->device) == cudaSuccess;
   {
     std::lock_guard<std::mutex> lock(s->mu);
     s->stop = true;
@@ -496,6 +545,7 @@ void ngia_server_destroy(ngia_server *s) {
                           &s->keys,   &s->vals, &s->cluster};
   for (ngia::DevBuf *b : bufs) b->release();
   delete s;
+  if (switched) cudaSetDevice(caller_dev);
 }
 
 }  // extern "C"

@@ -6,9 +6,9 @@
 //   1. histogram: per (segment, tile of 4096) digit counts;
 //   2. scan: per segment, exclusive scan of the counts in digit-major order,
 //      giving every (digit, tile) its first output slot;
-//   3. scatter: each tile ranks its elements stably (match_any within a warp,
-//      per-warp digit counts across warps, a running count across rounds) and
-//      writes them to their slots.
+//   3. scatter: each tile ranks its elements stably (equal digits within a
+//      warp found by eight ballots, per-warp digit counts across warps, a
+//      running count across rounds) and writes them to their slots.
 // Stability makes the passes compose into a sort by (key, input order); with
 // values = input index that is exactly a sort by (key, index).
 #include "kernels.cuh"
@@ -176,8 +176,15 @@ rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__
     const uint32_t key = valid ? kin[so + i] : 0u;
     const uint32_t val = valid ? (vin ? vin[so + i] : i) : 0u;
     const uint32_t d = (key >> shift) & 255u;
-    const uint32_t tag = valid ? d : 0x100u + lane;  // invalid lanes match nobody
-    const uint32_t peers = __match_any_sync(kFull, tag);
+    // lanes holding the same digit: one ballot per digit bit, each lane keeping
+    // the lanes that agree with it (a constant eight ballots, whatever the
+    // number of distinct digits in the warp; invalid lanes match nobody)
+    uint32_t peers = __ballot_sync(kFull, valid);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const uint32_t m = __ballot_sync(kFull, (d >> b) & 1u);
+      peers &= ((d >> b) & 1u) ? m : ~m;
+    }
     const uint32_t rank = __popc(peers & lt_mask);
     if (valid && rank == 0) wc[warp][d] = __popc(peers);
     __syncthreads();

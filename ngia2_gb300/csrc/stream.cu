@@ -279,7 +279,8 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
       NGIA_TRY(launch_dense_layouts(rp, roffs + at, c.count, map, rn,
                                     S.region_dplanes.as<uint32_t>(), s));
     else
-      NGIA_TRY(launch_nibbles(rp, roffs + at, c.count, rn, presence, s));
+      NGIA_TRY(launch_nibbles(rp, roffs + at, rlens + at, c.count, base + chunk_words, rn,
+                              presence, s));
     return NGIA_OK;
   };
 
@@ -303,6 +304,7 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
     NGIA_CUDA(cudaStreamSynchronize(s));
     for (uint32_t v : pk) present |= v;
   }
+  if (present & kBadRecord) return NGIA_ERR_FORMAT;  // a length word not the read length
   const double ms_sketch = since_ms(t0);
   const uint64_t bytes_sketch = S.stager.bytes;
 

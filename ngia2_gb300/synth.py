@@ -252,17 +252,20 @@ def packed_proteins(n_seqs, n_families, seed=5):
     return packed, offs, lens
 
 
-def serving_set(n_db=2_000_000, n_queries=300_000, n_families=100_000, novel=0.1, seed=4):
+def serving_set(n_db=2_000_000, n_queries=300_000, n_families=100_000, novel=0.1, seed=4,
+                subs=(0.05, 0.35), indels=(0.02, 3.0)):
     """The serving workload: sequences of the small-protein generator (log-normal
-    roots, median 300, sigma 0.5, 50-1500; 5-35 % substitutions, 2 % indels of
-    mean 3) from n_families families, split at random into a database of n_db
-    (index order: length descending) and held-out queries; a share `novel`
-    of the queries are unrelated sequences (new clusters).  Returns
-    (database SeqSet, queries SeqSet in random order)."""
+    roots, median 300, sigma 0.5, 50-1500; by default 5-35 % substitutions, 2 %
+    indels of mean 3) from n_families families, split at random into a
+    database of n_db (index order: length descending) and held-out queries; a
+    share `novel` of the queries are unrelated sequences (new clusters).
+    subs=(0, 0.04), indels=(0.005, 2) gives close relatives, most of which
+    reach identity 90 against their family.  Returns (database SeqSet,
+    queries SeqSet in random order)."""
     n_rel = int(round(n_queries * (1 - novel)))
     fam = families_parallel(n_db + n_rel, n_families, AMINO, AMINO_FREQ,
-                            _lognormal_roots(300, 0.5, 50, 1500), 0.05, 0.35, 0.02, 3.0, seed,
-                            prefix=b"srv")
+                            _lognormal_roots(300, 0.5, 50, 1500), subs[0], subs[1], indels[0],
+                            indels[1], seed, prefix=b"srv")
     rng = np.random.default_rng(seed + 1)
     perm = rng.permutation(len(fam))
     db_ids, q_ids = perm[:n_db], perm[n_db:]

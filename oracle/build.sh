@@ -4,8 +4,9 @@
 #   oracle/_ref/liboracle.so     the C restatement (ngia_oracle.c)
 #   oracle/_ref/src/             reference sources, staged from the reference
 #                                checkout when it is present (NGIA_REFERENCE_DIR,
-#                                default /root/reference); on machines without
-#                                the checkout the staged copy is used as is
+#                                default: a directory named "reference" beside
+#                                the repository's own directory); on machines
+#                                without the checkout the staged copy is used
 #   oracle/_ref/cpu{,_fma}/      the staged headers with the cuda_stub.h shim
 #   oracle/_ref/ngia2_cpu{,_fma} the reference CLI built as a host program
 #   oracle/_ref/libngia_ref{,_fma}.so  ref_harness.cpp over the shimmed headers
@@ -21,7 +22,7 @@
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
-REF="${NGIA_REFERENCE_DIR:-/root/reference}"
+REF="${NGIA_REFERENCE_DIR:-$HERE/../../reference}"
 NO_GPU=0
 [ "${1:-}" = "--no-gpu" ] && NO_GPU=1
 mkdir -p "$OUT"

@@ -55,6 +55,7 @@ def consuming(out: str, tag: str):
 
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--kind", choices=["dna", "protein"], default="dna")
     ap.add_argument("--n-seqs", type=int, default=200_000)
     ap.add_argument("--families", type=int, default=0)
     ap.add_argument("--identity", type=int, default=95)
@@ -70,10 +71,13 @@ def main():
         raise SystemExit("reference GPU build missing: run oracle/build.sh")
     fam = a.families or max(1, a.n_seqs // 10)
     d = Path(tempfile.mkdtemp(prefix="ngia_refgpu_"))
-    s = synth.dna_families(a.n_seqs, fam, 2)
+    if a.kind == "dna":
+        s = synth.dna_families(a.n_seqs, fam, 2)
+    else:
+        s = synth.protein_families(a.n_seqs, fam, 1)
     fa = d / "w.fa"
     s.write_fasta(fa)
-    res = {"workload": f"{a.n_seqs} DNA sequences, {fam} families, identity {a.identity}, "
+    res = {"workload": f"{a.n_seqs} {a.kind} sequences, {fam} families, identity {a.identity}, "
                        f"{a.bands} bands", "gpu": "same GPU, one process at a time"}
     t, out = run([ref, "-m", "makedb", "-f", fa, "-p", d / "ref.packed"])
     res["ref_makedb_s"] = t

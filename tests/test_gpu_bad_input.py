@@ -1,0 +1,103 @@
+"""Caller-built databases that do not hold together are refused, and the
+candidate collection's bounded wait gives up with an error the host reads:
+  * a record offset or read length that puts a record past the end of the
+    packed region -> NGIA_ERR_ARG from the host check, before any copy or
+    launch (ngia_ctx_load, ngia_ctx_run_host, ngia_stream_graph);
+  * a record whose length word is not its read length -> NGIA_ERR_FORMAT
+    from the first layout kernel, which skips such records;
+  * the look-back of the one-pass candidate collection with a predecessor
+    that never publishes -> NGIA_ERR_CUDA after a short poll limit.
+After each, the same context loads the good database and builds the same
+graph as a fresh one."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import ngia2_gb300 as ng
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def prot(golden):
+    return golden["prot"]["db"]
+
+
+def edges_of(ctx, db, identity=50):
+    ctx.load(db["packed"], db["offsets"], db["lens"])
+    ctx.sketch_bucket(64)
+    e, _ = ctx.graph(identity)
+    return e
+
+
+def raw_load(ctx, packed, offs, lens):
+    packed = np.ascontiguousarray(packed, np.uint32)
+    offs = np.ascontiguousarray(offs, np.uint64)
+    lens = np.ascontiguousarray(lens, np.uint32)
+    return ng.lib().ngia_ctx_load(ctx._h, packed.ctypes.data, packed.size, offs.ctypes.data,
+                                  lens.ctypes.data, lens.size, None, 64)
+
+
+def test_records_outside_the_region_are_refused(cuda, prot):
+    with ng.Context() as fresh:
+        want = edges_of(fresh, prot)
+    with ng.Context() as ctx:
+        launches = ng.kernel_launches()
+        offs = prot["offsets"].astype(np.uint64).copy()
+        offs[7] = prot["packed"].size  # past the end
+        assert raw_load(ctx, prot["packed"], offs, prot["lens"]) == ng.ERR_ARG
+        lens = prot["lens"].copy()
+        lens[-1] = 40_000  # the last record would run past the region
+        assert raw_load(ctx, prot["packed"], prot["offsets"], lens) == ng.ERR_ARG
+        lens = prot["lens"].copy()
+        lens[3] = 0x10000  # longer than the format allows
+        assert raw_load(ctx, prot["packed"], prot["offsets"], lens) == ng.ERR_ARG
+        assert ng.kernel_launches() == launches, "a launch before the host check"
+        got = edges_of(ctx, prot)
+    assert np.array_equal(got, want)
+
+
+def test_length_word_not_the_read_length_is_refused(cuda, prot):
+    with ng.Context() as fresh:
+        want = edges_of(fresh, prot)
+    with ng.Context() as ctx:
+        packed = prot["packed"].copy()
+        i = 11
+        o = int(prot["offsets"][i])
+        packed[o] = int(prot["lens"][i]) + 4000  # the kernel would read past the record
+        assert raw_load(ctx, packed, prot["offsets"], prot["lens"]) == ng.ERR_FORMAT
+        got = edges_of(ctx, prot)
+    assert np.array_equal(got, want)
+
+
+def test_run_host_and_streaming_refuse_records_outside(cuda, prot):
+    offs = prot["offsets"].astype(np.uint64).copy()
+    offs[5] = prot["packed"].size + 100
+    packed = np.ascontiguousarray(prot["packed"], np.uint32)
+    lens = np.ascontiguousarray(prot["lens"], np.uint32)
+    edges = np.zeros(16, ng.EDGE_DTYPE)
+    m = C.c_uint64()
+    with ng.Context() as ctx:
+        rc = ng.lib().ngia_ctx_run_host(ctx._h, packed.ctypes.data, packed.size,
+                                        offs.ctypes.data, lens.ctypes.data, lens.size, 50, 64,
+                                        edges.ctypes.data, len(edges), C.byref(m), None)
+        assert rc == ng.ERR_ARG
+    rc = ng.lib().ngia_stream_graph(packed.ctypes.data, packed.size, offs.ctypes.data,
+                                    lens.ctypes.data, lens.size, 50, 3, 1 << 20,
+                                    edges.ctypes.data, len(edges), C.byref(m), None)
+    assert rc == ng.ERR_ARG
+
+
+def test_lookback_wait_gives_up_and_context_stays_usable(cuda, prot):
+    with ng.Context() as fresh:
+        want = edges_of(fresh, prot)
+    with ng.Context() as ctx:
+        ctx.load(prot["packed"], prot["offsets"], prot["lens"])
+        ctx.sketch_bucket(64)
+        rc = ng.lib().ngia_ctx_test_lookback_timeout(ctx._h, 50, 64, 4096)
+        assert rc == ng.ERR_CUDA
+        e, _ = ctx.graph(50)
+    assert np.array_equal(e, want)

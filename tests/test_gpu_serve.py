@@ -144,3 +144,40 @@ def test_submit_checks_its_records(served):
         bad[1] = len(p) + 5
         with pytest.raises(ng.NgiaError):
             srv.submit(p, bad, l)
+
+
+def test_small_requests_first_same_results(served):
+    """Small requests admitted ahead of large ones, on slots reserved for
+    them: every request still gets the rule's answer, whatever the order."""
+    ctx, cluster, qr, want = served
+    sizes = [150, 3, 1, 140, 8, 2, 100, 5]  # 409 of the 460 queries
+    reqs = slice_requests(qr, sizes)
+    with ng.Server(ctx, cluster, IDENTITY, slots=3, small_queries=16, small_slots=1) as srv:
+        tickets = [srv.submit(p, o, l) for p, o, l, _ in reqs]
+        for t, (_, _, l, k) in zip(tickets, reqs):
+            res, st = srv.wait(t, len(l))
+            assert np.array_equal(res, want[k:k + len(l)])
+    with pytest.raises(ng.NgiaError):  # every slot reserved: large requests never run
+        ng.Server(ctx, cluster, IDENTITY, slots=2, small_queries=16, small_slots=2)
+
+
+def test_server_follows_its_device(served):
+    """A server created while device 1 is current runs there (its dispatcher
+    thread makes that device current)."""
+    import torch
+    if torch.cuda.device_count() < 2:
+        pytest.skip("one GPU")
+    ctx0, cluster, qr, want = served
+    torch.cuda.set_device(1)
+    try:
+        dbr, _ = database()
+        with ng.Context() as ctx:
+            ctx.load(*dbr)
+            ctx.sketch_bucket(64)
+            reqs = slice_requests(qr, [50])
+            with ng.Server(ctx, cluster, IDENTITY, slots=2) as srv:
+                p, o, l, k = reqs[0]
+                res, _ = srv.wait(srv.submit(p, o, l), len(l))
+        assert np.array_equal(res, want[k:k + len(l)])
+    finally:
+        torch.cuda.set_device(0)

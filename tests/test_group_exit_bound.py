@@ -28,6 +28,9 @@ import pytest
 
 FULL = (1 << 32) - 1
 SHAPES = [(16, 1), (16, 2), (16, 4), (32, 4), (32, 8), (32, 16)]  # (G, K) of the group classes
+# the widest classes as they run, one block of four warps per pair
+# (align_group_cta.cuh): (32, 8) as (128, 2), (32, 16) as (128, 4)
+CTA_SHAPES = [(128, 2), (128, 4)]
 
 
 def band(lr: int, lt: int, t: float):
@@ -141,6 +144,12 @@ def replay(rep, tar, t, G, K):
             got = [above[(l + o) % G] for l in range(G)]
             above = [above[l] + (got[l] if rank[l] + o < G else 0) for l in range(G)]
             o <<= 1
+        # the block-wide kernel's form: suffix sums in lane order, rotated by
+        # the lowest lane (align_group_cta.cuh)
+        suf = list(np.cumsum(live[::-1])[::-1])
+        total, sl = sum(live), suf[low[0]]
+        rotated = [suf[l] + total - sl if l >= low[0] else suf[l] - sl for l in range(G)]
+        assert rotated == above
         if not qhi1:
             out.append(None)
             continue
@@ -223,7 +232,7 @@ def test_group_row_aware_bound_never_below_final_lcs(seed):
         if len(tar) == 0 or np.float32(len(tar)) < np.float32(len(rep)) * np.float32(t):
             continue  # the length filter: never aligned
         ls, rs, nr, nc = band(len(rep), len(tar), t)
-        shapes = [(G, K) for G, K in SHAPES
+        shapes = [(G, K) for G, K in SHAPES + CTA_SHAPES
                   if (nr + K - 1) // K <= G or ls + rs <= (G - 1) * K + G]
         if not shapes:
             continue
@@ -240,3 +249,26 @@ def test_group_row_aware_bound_never_below_final_lcs(seed):
             steps += 1
         pairs += 1
     assert pairs > 0 and steps > 0 and tighter > 0
+
+
+@pytest.mark.parametrize("G,K,t", [(128, 2, 0.9), (128, 4, 0.7)])
+def test_block_wide_group_wraps_its_ring(G, K, t):
+    """A pair long enough that its slices wrap the block's ring of 128 lanes
+    (slice q + 128 on the lane of slice q): one live slice per lane, the
+    lanes' bound equal to the row-order bound and never below the final LCS."""
+    rng = np.random.default_rng(G + K)
+    a = rng.integers(1, 5, size=9000 if K == 2 else 17500)
+    b = mutate(rng, a, 0.02, 0.004)
+    rep, tar = (a, b) if len(a) >= len(b) else (b, a)
+    ls, rs, nr, nc = band(len(rep), len(tar), t)
+    assert (nr + K - 1) // K > G, "no wrap"
+    assert ls + rs <= (G - 1) * K + G
+    final, out = replay(rep, tar, t, G, K)
+    steps = 0
+    for step in out:
+        if step is None:
+            continue
+        ub, direct, _, _ = step
+        assert ub == direct and ub >= final
+        steps += 1
+    assert steps > 0
