@@ -971,10 +971,13 @@ def run_stream(args) -> dict:
     k = min(n, 1000)  # warm-up on the first records
     k_words = int(offs[k - 1]) + 1 + 4 * ((int(lens[k - 1]) + 31) // 32)
     budget = args.stream_chunk_bytes
+    import torch
+    clk = ClockSampler(torch.cuda.current_device())
     for identity in STREAM_IDENTITIES:
         ng.stream_graph(packed[:k_words], offs[:k], lens[:k], identity, STREAM_BANDS, budget)
-        edges, st = ng.stream_graph(packed, offs, lens, identity, STREAM_BANDS, budget,
-                                    cap=n * STREAM_BANDS)
+        with clk:
+            edges, st = ng.stream_graph(packed, offs, lens, identity, STREAM_BANDS, budget,
+                                        cap=n * STREAM_BANDS)
         gbs = lambda b, ms: b / (ms * 1e-3) / 1e9 if ms > 0 else None  # noqa: E731
         run = {"value": n / (st["ms_total"] * 1e-3), "unit": "seqs/s", "edges": int(len(edges)),
                "chunks": st["chunks"], "chunk_loads": st["chunk_loads"],
@@ -983,7 +986,8 @@ def run_stream(args) -> dict:
                "h2d_gbs": {"sketch": gbs(st["bytes_h2d_sketch"], st["ms_sketch"]),
                            "align": gbs(st["bytes_h2d_align"], st["ms_align"])},
                "h2d_bytes": {"sketch": st["bytes_h2d_sketch"], "align": st["bytes_h2d_align"]},
-               "unique_pairs": st["unique_pairs"], "computed_cells": st["computed_cells"]}
+               "unique_pairs": st["unique_pairs"], "computed_cells": st["computed_cells"],
+               "clocks": clk.summary()}
         if args.stream_check:
             with ng.Context() as ctx:
                 ctx.load(packed, offs, lens)

@@ -492,7 +492,14 @@ static int launch_group_cta_k(const RoundArgs &a, int cls, unsigned int *cursor,
 // A class of (32 lanes, K words) on one block of kCtaWarps warps per pair
 // (32 * kCtaWarps lanes, K / kCtaWarps words): the same rows per ring turn and
 // a wider span, so the class's binning holds (align_group_cta.cuh).
-constexpr int kCtaWarps = 4;
+// Measured on 2,000,000 heavy-tailed protein pairs (autotuned round): one warp
+// per pair 9.28 ms, blocks of two warps 9.69 ms, of four 10.46 ms -- the
+// shorter chains do not pay for the extra issue slots and barriers, so the
+// block-wide form is off by default (NGIA_CTA_WARPS=2 or 4 at build time).
+#ifndef NGIA_CTA_WARPS
+#define NGIA_CTA_WARPS 0  // 0: the classes run on one warp per pair (align_group.cuh)
+#endif
+constexpr int kCtaWarps = NGIA_CTA_WARPS > 0 ? NGIA_CTA_WARPS : 1;
 template <int K>
 static int launch_group_cta(const RoundArgs &a, int KC, int cls, unsigned int *cursor,
                             cudaStream_t s) {
@@ -570,8 +577,11 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
 #undef NGIA_GROUP_CASE
     case 15:
       static_assert(group_shape(15).G == 32 && group_shape(16).G == 32, "block-wide classes");
-      return launch_group_cta<group_shape(15).K>(a, ab.K, cls, cursor, s);
-    case 16: return launch_group_cta<group_shape(16).K>(a, ab.K, cls, cursor, s);
+      return NGIA_CTA_WARPS ? launch_group_cta<group_shape(15).K>(a, ab.K, cls, cursor, s)
+                            : launch_group<32, group_shape(15).K>(a, ab.K, cls, cursor, s);
+    case 16:
+      return NGIA_CTA_WARPS ? launch_group_cta<group_shape(16).K>(a, ab.K, cls, cursor, s)
+                            : launch_group<32, group_shape(16).K>(a, ab.K, cls, cursor, s);
     case kGeneralClass: {
       uint32_t grid = 0;
       NGIA_TRY(persistent_grid(align_general_kernel, 128, 0, kFull, &grid));

@@ -153,29 +153,42 @@ static uint32_t scan_chunks(uint32_t ntiles) {
   return len > kScanChunk ? ceil_div(len, kScanChunk) : 0u;
 }
 
+// The tile's keys (and values) are loaded into registers first, all in
+// flight at once, then ranked and written in rounds of one key per thread;
+// the per-warp digit counts are double-buffered by round, so a round takes
+// two barriers.
+constexpr uint32_t kRounds = kTile / kSortThreads;
+
 __global__ void __launch_bounds__(kSortThreads)
 rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                   uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                   uint32_t seg_len, int shift, uint32_t ntiles,
                   const uint32_t *__restrict__ offsets) {
   __shared__ uint32_t base[256];
-  __shared__ uint32_t wc[kSortWarps][256];
+  __shared__ uint32_t wc[2][kSortWarps][256];
   const uint32_t seg = blockIdx.y, tile = blockIdx.x;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const size_t so = (size_t)seg * seg_len;
+  uint32_t keys[kRounds], vals[kRounds];
+#pragma unroll
+  for (uint32_t r = 0; r < kRounds; ++r) {
+    const uint32_t i = tile * kTile + r * kSortThreads + threadIdx.x;
+    const bool valid = i < seg_len;
+    keys[r] = valid ? kin[so + i] : 0u;
+    vals[r] = valid ? (vin ? vin[so + i] : i) : 0u;
+  }
   base[threadIdx.x] = offsets[((size_t)seg * 256 + threadIdx.x) * ntiles + tile];
 #pragma unroll
-  for (uint32_t w = 0; w < kSortWarps; ++w) wc[w][threadIdx.x] = 0;
+  for (uint32_t w = 0; w < kSortWarps; ++w) wc[0][w][threadIdx.x] = wc[1][w][threadIdx.x] = 0;
   __syncthreads();
-  const size_t so = (size_t)seg * seg_len;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  for (uint32_t r = 0; r < kTile / kSortThreads; ++r) {
+#pragma unroll
+  for (uint32_t r = 0; r < kRounds; ++r) {
     const uint32_t first = tile * kTile + r * kSortThreads;
     if (first >= seg_len) break;  // block-uniform
-    const uint32_t i = first + threadIdx.x;
-    const bool valid = i < seg_len;
-    const uint32_t key = valid ? kin[so + i] : 0u;
-    const uint32_t val = valid ? (vin ? vin[so + i] : i) : 0u;
-    const uint32_t d = (key >> shift) & 255u;
+    uint32_t(&c)[kSortWarps][256] = wc[r & 1u];
+    const bool valid = first + threadIdx.x < seg_len;
+    const uint32_t d = (keys[r] >> shift) & 255u;
     // lanes holding the same digit: one ballot per digit bit, each lane keeping
     // the lanes that agree with it (a constant eight ballots, whatever the
     // number of distinct digits in the warp; invalid lanes match nobody)
@@ -186,23 +199,23 @@ rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__
       peers &= ((d >> b) & 1u) ? m : ~m;
     }
     const uint32_t rank = __popc(peers & lt_mask);
-    if (valid && rank == 0) wc[warp][d] = __popc(peers);
+    if (valid && rank == 0) c[warp][d] = __popc(peers);
     __syncthreads();
     if (valid) {
       uint32_t pos = base[d] + rank;
-      for (uint32_t w = 0; w < warp; ++w) pos += wc[w][d];
-      kout[so + pos] = key;
-      vout[so + pos] = val;
+      for (uint32_t w = 0; w < warp; ++w) pos += c[w][d];
+      kout[so + pos] = keys[r];
+      vout[so + pos] = vals[r];
     }
     __syncthreads();
+    // this round's counts move into the bases; the other buffer is the next round's
     uint32_t tot = 0;
 #pragma unroll
     for (uint32_t w = 0; w < kSortWarps; ++w) {
-      tot += wc[w][threadIdx.x];
-      wc[w][threadIdx.x] = 0;
+      tot += c[w][threadIdx.x];
+      c[w][threadIdx.x] = 0;
     }
     base[threadIdx.x] += tot;
-    __syncthreads();
   }
 }
 
