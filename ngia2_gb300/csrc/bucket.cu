@@ -11,9 +11,10 @@
 //      many as keep the runs of equal low bits (buckets) at about four
 //      entries on average -- two passes up to 2^18 sequences, three up to
 //      2^26, else all four; each bucket holds its entries in index order;
-//   2. resolve (rep_resolve_kernel): one thread per sorted entry scans back
-//      through its bucket to the nearest entry with the same signature, which
-//      is its predecessor in index order; none: the entry is its own rep.
+//   2. resolve (rep_resolve_kernel): each sorted entry scans back through its
+//      bucket to the nearest entry with the same signature, which is its
+//      predecessor in index order (none: the entry is its own rep), over tiles
+//      staged in shared memory.
 // Two or three sort passes instead of four, and the chain written by the
 // resolve pass itself.  Equal signatures always share a bucket, so a scan
 // only passes entries of other signatures whose low bits collide -- a few on
@@ -30,26 +31,61 @@ static int partition_passes(uint32_t n) {
 }
 
 // sk, sv: each band's (signature, index) pairs ordered stably by the
-// signature's low bits (low_mask).
-__global__ void __launch_bounds__(256)
+// signature's low bits (low_mask).  A block takes tiles of kResolveTile
+// sorted entries: the tile is loaded into shared memory first (every load in
+// flight at once), then each entry scans back within the tile; only an entry
+// whose bucket began before the tile continues in global memory.  (A plain
+// one-entry-per-thread scan waited on each load in turn: 27 cycles of
+// long-scoreboard stall per instruction.)
+constexpr uint32_t kResolveTile = 4096;
+constexpr uint32_t kResolveThreads = 256;
+constexpr uint32_t kResolvePer = kResolveTile / kResolveThreads;
+
+__global__ void __launch_bounds__(kResolveThreads)
 rep_resolve_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__ sv,
                    uint32_t n, uint32_t bands, uint32_t low_mask, uint32_t *__restrict__ rep) {
-  const size_t total = (size_t)n * bands;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const size_t band = e / n;
-    const size_t first = band * n;  // the band's first entry
-    const uint32_t sig = sk[e], bkt = sig & low_mask;
-    uint32_t r = sv[e];
-    for (size_t q = e; q-- > first;) {
-      const uint32_t s = __ldg(sk + q);
-      if ((s & low_mask) != bkt) break;  // the bucket's start
-      if (s == sig) {
-        r = __ldg(sv + q);
-        break;
-      }
+  __shared__ uint32_t tk[kResolveTile], tv[kResolveTile];
+  const uint64_t total = (uint64_t)n * bands;
+  const bool narrow = total <= 0xFFFFFFFFull;  // 32-bit division suffices
+  for (uint64_t t0 = (uint64_t)blockIdx.x * kResolveTile; t0 < total;
+       t0 += (uint64_t)gridDim.x * kResolveTile) {
+    const uint32_t cnt = total - t0 < kResolveTile ? (uint32_t)(total - t0) : kResolveTile;
+    uint32_t a[kResolvePer], b[kResolvePer];
+#pragma unroll
+    for (uint32_t j = 0; j < kResolvePer; ++j) {
+      const uint32_t k = threadIdx.x + j * kResolveThreads;
+      a[j] = k < cnt ? sk[t0 + k] : 0u;
+      b[j] = k < cnt ? sv[t0 + k] : 0u;
     }
-    rep[first + sv[e]] = r;
+#pragma unroll
+    for (uint32_t j = 0; j < kResolvePer; ++j) {
+      const uint32_t k = threadIdx.x + j * kResolveThreads;
+      tk[k] = a[j];
+      tv[k] = b[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (uint32_t j = 0; j < kResolvePer; ++j) {
+      const uint32_t k = threadIdx.x + j * kResolveThreads;
+      if (k >= cnt) break;
+      const uint64_t e = t0 + k;
+      const uint64_t band = narrow ? (uint64_t)((uint32_t)e / n) : e / n;
+      const uint64_t first = band * n;  // the band's first entry
+      const uint32_t sig = a[j], bkt = sig & low_mask;
+      uint32_t r = b[j];
+      for (uint64_t q = e; q > first;) {
+        --q;
+        const bool in_tile = q >= t0;
+        const uint32_t s = in_tile ? tk[q - t0] : __ldg(sk + q);
+        if ((s & low_mask) != bkt) break;  // the bucket's start
+        if (s == sig) {
+          r = in_tile ? tv[q - t0] : __ldg(sv + q);
+          break;
+        }
+      }
+      rep[first + b[j]] = r;
+    }
+    __syncthreads();
   }
 }
 
@@ -70,10 +106,10 @@ int bucket(const uint32_t *sigs, uint32_t n, uint32_t bands, uint32_t *rep,
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const size_t want = ceil_div<size_t>(total, 256);
-  const size_t cap = (size_t)sms * 8;
-  rep_resolve_kernel<<<(uint32_t)(want < cap ? want : cap), 256, 0, s>>>(sk, sv, n, bands,
-                                                                         low_mask, rep);
+  const size_t want = ceil_div<size_t>(total, kResolveTile);
+  const size_t cap = (size_t)sms * 4;  // resident blocks: 64 registers x 256 threads
+  rep_resolve_kernel<<<(uint32_t)(want < cap ? want : cap), kResolveThreads, 0, s>>>(
+      sk, sv, n, bands, low_mask, rep);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

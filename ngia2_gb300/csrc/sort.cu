@@ -6,9 +6,9 @@
 //   1. histogram: per (segment, tile of 4096) digit counts;
 //   2. scan: per segment, exclusive scan of the counts in digit-major order,
 //      giving every (digit, tile) its first output slot;
-//   3. scatter: each tile ranks its elements stably (equal digits within a
-//      warp found by eight ballots, per-warp digit counts across warps, a
-//      running count across rounds) and writes them to their slots.
+//   3. scatter: each warp of a tile ranks its contiguous sub-tile stably
+//      (equal digits within a round found by eight ballots, warp-private
+//      running slots per digit) and writes the keys to their slots.
 // Stability makes the passes compose into a sort by (key, input order); with
 // values = input index that is exactly a sort by (key, index).
 #include "kernels.cuh"
@@ -153,71 +153,109 @@ static uint32_t scan_chunks(uint32_t ntiles) {
   return len > kScanChunk ? ceil_div(len, kScanChunk) : 0u;
 }
 
-// The tile's keys (and values) are loaded into registers first, all in
-// flight at once, then ranked and written in rounds of one key per thread;
-// the per-warp digit counts are double-buffered by round, so a round takes
-// two barriers.
-constexpr uint32_t kRounds = kTile / kSortThreads;
+// The tile's keys and values are staged in shared memory (coalesced loads,
+// all in flight at once); then each warp takes a contiguous sub-tile of
+// kTile / kSortWarps keys:
+//   1. the warp counts its sub-tile's digits (warp-private counts);
+//   2. per digit, the block turns the counts into each warp's first slot
+//      (the tile's offset from the scan, plus the counts of the warps before);
+//   3. each warp writes its keys in order, ranking equal digits within a round
+//      of 32 by ballots and advancing its own slots -- no block barrier
+//      between rounds, three per tile.
+// Stable: warps hold consecutive sub-tiles, rounds and lanes go in key order.
+constexpr uint32_t kWarpKeys = kTile / kSortWarps;
+constexpr uint32_t kRounds = kWarpKeys / 32;
+constexpr uint32_t kLoads = kTile / kSortThreads;
+
+// lanes holding the same digit as this one: one ballot per digit bit (a
+// constant eight ballots, whatever the number of distinct digits in the
+// warp); lanes outside `valid` match nobody
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d, uint32_t valid) {
+  uint32_t peers = valid;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const uint32_t m = __ballot_sync(kFull, (d >> b) & 1u);
+    peers &= ((d >> b) & 1u) ? m : ~m;
+  }
+  return peers;
+}
 
 __global__ void __launch_bounds__(kSortThreads)
 rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                   uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                   uint32_t seg_len, int shift, uint32_t ntiles,
                   const uint32_t *__restrict__ offsets) {
-  __shared__ uint32_t base[256];
-  __shared__ uint32_t wc[2][kSortWarps][256];
+  extern __shared__ uint32_t rs_smem[];
+  uint32_t *tk = rs_smem, *tv = rs_smem + kTile;
+  uint32_t(*slot)[256] = reinterpret_cast<uint32_t(*)[256]>(rs_smem + 2 * kTile);
   const uint32_t seg = blockIdx.y, tile = blockIdx.x;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const size_t so = (size_t)seg * seg_len;
-  uint32_t keys[kRounds], vals[kRounds];
+  const uint32_t t0 = tile * kTile;
+  {
+    uint32_t a[kLoads], b[kLoads];
 #pragma unroll
-  for (uint32_t r = 0; r < kRounds; ++r) {
-    const uint32_t i = tile * kTile + r * kSortThreads + threadIdx.x;
-    const bool valid = i < seg_len;
-    keys[r] = valid ? kin[so + i] : 0u;
-    vals[r] = valid ? (vin ? vin[so + i] : i) : 0u;
+    for (uint32_t j = 0; j < kLoads; ++j) {
+      const uint32_t i = t0 + j * kSortThreads + threadIdx.x;
+      a[j] = i < seg_len ? kin[so + i] : 0u;
+      b[j] = i < seg_len ? (vin ? vin[so + i] : i) : 0u;
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < kLoads; ++j) {
+      tk[j * kSortThreads + threadIdx.x] = a[j];
+      tv[j * kSortThreads + threadIdx.x] = b[j];
+    }
   }
-  base[threadIdx.x] = offsets[((size_t)seg * 256 + threadIdx.x) * ntiles + tile];
 #pragma unroll
-  for (uint32_t w = 0; w < kSortWarps; ++w) wc[0][w][threadIdx.x] = wc[1][w][threadIdx.x] = 0;
+  for (uint32_t w = 0; w < kSortWarps; ++w) slot[w][threadIdx.x] = 0;
   __syncthreads();
   const uint32_t lt_mask = (1u << lane) - 1u;
-#pragma unroll
+  const uint32_t w0 = warp * kWarpKeys;  // the warp's first key in the tile
+  // 1. the warp's digit counts
+#pragma unroll 2
   for (uint32_t r = 0; r < kRounds; ++r) {
-    const uint32_t first = tile * kTile + r * kSortThreads;
-    if (first >= seg_len) break;  // block-uniform
-    uint32_t(&c)[kSortWarps][256] = wc[r & 1u];
-    const bool valid = first + threadIdx.x < seg_len;
-    const uint32_t d = (keys[r] >> shift) & 255u;
-    // lanes holding the same digit: one ballot per digit bit, each lane keeping
-    // the lanes that agree with it (a constant eight ballots, whatever the
-    // number of distinct digits in the warp; invalid lanes match nobody)
-    uint32_t peers = __ballot_sync(kFull, valid);
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const uint32_t m = __ballot_sync(kFull, (d >> b) & 1u);
-      peers &= ((d >> b) & 1u) ? m : ~m;
-    }
-    const uint32_t rank = __popc(peers & lt_mask);
-    if (valid && rank == 0) c[warp][d] = __popc(peers);
-    __syncthreads();
-    if (valid) {
-      uint32_t pos = base[d] + rank;
-      for (uint32_t w = 0; w < warp; ++w) pos += c[w][d];
-      kout[so + pos] = keys[r];
-      vout[so + pos] = vals[r];
-    }
-    __syncthreads();
-    // this round's counts move into the bases; the other buffer is the next round's
-    uint32_t tot = 0;
+    const uint32_t k = w0 + 32 * r + lane;
+    const uint32_t valid = __ballot_sync(kFull, t0 + k < seg_len);
+    if (!valid) break;  // warp-uniform: the tile's end
+    const uint32_t d = (tk[k] >> shift) & 255u;
+    const uint32_t peers = digit_peers(d, valid);
+    if ((valid >> lane & 1u) && (peers & lt_mask) == 0) slot[warp][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // 2. each warp's first slot per digit (thread t: digit t)
+  {
+    uint32_t run = offsets[((size_t)seg * 256 + threadIdx.x) * ntiles + tile];
 #pragma unroll
     for (uint32_t w = 0; w < kSortWarps; ++w) {
-      tot += c[w][threadIdx.x];
-      c[w][threadIdx.x] = 0;
+      const uint32_t c = slot[w][threadIdx.x];
+      slot[w][threadIdx.x] = run;
+      run += c;
     }
-    base[threadIdx.x] += tot;
+  }
+  __syncthreads();
+  // 3. the warp's keys in order
+#pragma unroll 2
+  for (uint32_t r = 0; r < kRounds; ++r) {
+    const uint32_t k = w0 + 32 * r + lane;
+    const uint32_t valid = __ballot_sync(kFull, t0 + k < seg_len);
+    if (!valid) break;
+    const uint32_t key = tk[k];
+    const uint32_t d = (key >> shift) & 255u;
+    const uint32_t peers = digit_peers(d, valid);
+    const bool mine = valid >> lane & 1u;
+    if (mine) {
+      const uint32_t pos = slot[warp][d] + __popc(peers & lt_mask);
+      kout[so + pos] = key;
+      vout[so + pos] = tv[k];
+    }
+    __syncwarp();
+    if (mine && (peers & lt_mask) == 0) slot[warp][d] += __popc(peers);
+    __syncwarp();
   }
 }
+
+constexpr size_t kScatterSmem = (2 * kTile + kSortWarps * 256) * sizeof(uint32_t);
 
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs) {
   const size_t ntiles = ceil_div<size_t>(seg_len, kTile);
@@ -268,8 +306,8 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
                                                              sums);
       NGIA_LAUNCHED();
     }
-    rs_scatter_kernel<<<grid, kSortThreads, 0, s>>>(sk, sv, dk, dv, seg_len, shift,
-                                                    ntiles, counts);
+    rs_scatter_kernel<<<grid, kSortThreads, kScatterSmem, s>>>(sk, sv, dk, dv, seg_len, shift,
+                                                               ntiles, counts);
     NGIA_LAUNCHED();
     sk = dk;
     sv = dv;
