@@ -11,10 +11,11 @@
 //      many as keep the runs of equal low bits (buckets) at about four
 //      entries on average -- two passes up to 2^18 sequences, three up to
 //      2^26, else all four; each bucket holds its entries in index order;
-//   2. resolve (rep_resolve_kernel): each sorted entry scans back through its
-//      bucket to the nearest entry with the same signature, which is its
-//      predecessor in index order (none: the entry is its own rep), over tiles
-//      staged in shared memory.
+//   2. resolve (rep_resolve_kernel, rep_resolve_far_kernel): each sorted entry
+//      scans back through its bucket to the nearest entry with the same
+//      signature, which is its predecessor in index order (none: the entry is
+//      its own rep) -- within a tile staged in shared memory for the first
+//      steps, one warp per entry 32 entries a step beyond.
 // Two or three sort passes instead of four, and the chain written by the
 // resolve pass itself.  Equal signatures always share a bucket, so a scan
 // only passes entries of other signatures whose low bits collide -- a few on
@@ -25,25 +26,36 @@
 
 namespace ngia {
 
-// Partition passes: buckets of n / 2^(8P) <= 4 entries on average.
+// Partition passes: buckets of n / 2^(8P) <= 4 entries on average.  A build
+// may fix the count (1..4; 4 = the full sort, buckets of equal signatures).
+#ifndef NGIA_BUCKET_PASSES
+#define NGIA_BUCKET_PASSES 0
+#endif
 static int partition_passes(uint32_t n) {
+  if (NGIA_BUCKET_PASSES >= 1 && NGIA_BUCKET_PASSES <= 4) return NGIA_BUCKET_PASSES;
   return n <= (1u << 10) ? 1 : n <= (1u << 18) ? 2 : n <= (1u << 26) ? 3 : 4;
 }
 
 // sk, sv: each band's (signature, index) pairs ordered stably by the
 // signature's low bits (low_mask).  A block takes tiles of kResolveTile
-// sorted entries: the tile is loaded into shared memory first (every load in
-// flight at once), then each entry scans back within the tile; only an entry
-// whose bucket began before the tile continues in global memory.  (A plain
-// one-entry-per-thread scan waited on each load in turn: 27 cycles of
-// long-scoreboard stall per instruction.)
+// sorted entries staged in shared memory (every load in flight at once); each
+// entry scans back within its tile for at most kResolveSteps entries.  An
+// entry whose scan would go further -- its bucket began before the tile, or
+// a long run of another signature with the same low bits lies between it and
+// its predecessor -- is listed in `slow` and resolved by
+// rep_resolve_far_kernel, one warp per entry and 32 entries per step.  (A
+// scan of one thread per entry down to its answer lasted as long as the
+// longest one: on the 200k DNA set a few entries scan back over ~2,000
+// entries of another signature in global memory, and the kernel took 450 us.)
 constexpr uint32_t kResolveTile = 4096;
 constexpr uint32_t kResolveThreads = 256;
 constexpr uint32_t kResolvePer = kResolveTile / kResolveThreads;
+constexpr uint32_t kResolveSteps = 64;
 
 __global__ void __launch_bounds__(kResolveThreads)
 rep_resolve_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__ sv,
-                   uint32_t n, uint32_t bands, uint32_t low_mask, uint32_t *__restrict__ rep) {
+                   uint32_t n, uint32_t bands, uint32_t low_mask, uint32_t *__restrict__ rep,
+                   uint64_t *__restrict__ slow, unsigned int *__restrict__ slow_count) {
   __shared__ uint32_t tk[kResolveTile], tv[kResolveTile];
   const uint64_t total = (uint64_t)n * bands;
   const bool narrow = total <= 0xFFFFFFFFull;  // 32-bit division suffices
@@ -72,20 +84,63 @@ rep_resolve_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__
       const uint64_t band = narrow ? (uint64_t)((uint32_t)e / n) : e / n;
       const uint64_t first = band * n;  // the band's first entry
       const uint32_t sig = a[j], bkt = sig & low_mask;
+      // within the tile and the band, at most kResolveSteps entries back
+      const uint64_t lo_tile = first > t0 ? first : t0;
+      const uint32_t room = (uint32_t)(e - lo_tile);
+      const uint32_t reach = room < kResolveSteps ? room : kResolveSteps;
       uint32_t r = b[j];
-      for (uint64_t q = e; q > first;) {
-        --q;
-        const bool in_tile = q >= t0;
-        const uint32_t s = in_tile ? tk[q - t0] : __ldg(sk + q);
-        if ((s & low_mask) != bkt) break;  // the bucket's start
+      bool settled = false;
+      for (uint32_t d = 1; d <= reach; ++d) {
+        const uint32_t s = tk[k - d];
+        if ((s & low_mask) != bkt) {  // the bucket's start: no predecessor
+          settled = true;
+          break;
+        }
         if (s == sig) {
-          r = in_tile ? tv[q - t0] : __ldg(sv + q);
+          r = tv[k - d];
+          settled = true;
           break;
         }
       }
-      rep[first + b[j]] = r;
+      // back at the band's first entry without a match: no predecessor
+      if (!settled && reach == room && lo_tile == first) settled = true;
+      if (settled) rep[first + b[j]] = r;
+      else slow[atomicAdd(slow_count, 1u)] = e;
     }
     __syncthreads();
+  }
+}
+
+// The listed entries: one warp per entry, lane l testing entry e - 1 - 32s - l
+// at step s; the nearest lane holding the signature gives the predecessor
+// unless a nearer lane is outside the bucket (or the band starts first).
+__global__ void __launch_bounds__(256)
+rep_resolve_far_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__ sv,
+                       uint32_t n, uint32_t low_mask, const uint64_t *__restrict__ slow,
+                       const unsigned int *__restrict__ slow_count, uint32_t *__restrict__ rep) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t count = *slow_count;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += warps) {
+    const uint64_t e = slow[w];
+    const uint64_t first = e / n * n;
+    const uint32_t sig = sk[e], bkt = sig & low_mask, self = sv[e];
+    uint32_t r = self;
+    for (uint64_t base = e; base > first;) {  // warp-uniform
+      const uint64_t q = base - 1u - lane;     // base - 32 .. base - 1
+      const bool in = base >= first + 1u + lane;
+      const uint32_t s = in ? __ldg(sk + q) : 0u;
+      const uint32_t hit = __ballot_sync(kFull, in && s == sig);
+      const uint32_t out = __ballot_sync(kFull, !in || (s & low_mask) != bkt);
+      const uint32_t stop = hit | out;
+      if (stop) {
+        const uint32_t l = __ffs(stop) - 1u;  // the nearest
+        if ((hit >> l) & 1u) r = __shfl_sync(kFull, in ? __ldg(sv + q) : 0u, l);
+        break;
+      }
+      base = base >= first + 32u ? base - 32u : first;
+    }
+    if (lane == 0) rep[first + self] = r;
   }
 }
 
@@ -106,10 +161,18 @@ int bucket(const uint32_t *sigs, uint32_t n, uint32_t bands, uint32_t *rep,
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // after the sort its temporary keys hold the list of far entries, and the
+  // first word of its digit counts their number
+  // (8 * total bytes into the scratch: 8-byte aligned)
+  uint64_t *slow = static_cast<uint64_t *>(sort_scratch);
+  unsigned int *slow_count = reinterpret_cast<unsigned int *>(slow + total);
+  NGIA_CUDA(cudaMemsetAsync(slow_count, 0, sizeof(unsigned int), s));
   const size_t want = ceil_div<size_t>(total, kResolveTile);
   const size_t cap = (size_t)sms * 4;  // resident blocks: 64 registers x 256 threads
   rep_resolve_kernel<<<(uint32_t)(want < cap ? want : cap), kResolveThreads, 0, s>>>(
-      sk, sv, n, bands, low_mask, rep);
+      sk, sv, n, bands, low_mask, rep, slow, slow_count);
+  NGIA_LAUNCHED();
+  rep_resolve_far_kernel<<<sms * 4, 256, 0, s>>>(sk, sv, n, low_mask, slow, slow_count, rep);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

@@ -65,3 +65,79 @@ def test_resolve_replay_low_bits_collide():
     sig = ((rng.integers(0, 200, n).astype(np.uint32) << 16) | 0x5A5A).astype(np.uint32)
     got = resolve_replay(sig, 2)
     assert np.array_equal(got, oracle.bucket_band(sig).astype(np.int64))
+
+
+def two_phase_replay(sk, sv, n, bands, low_mask, tile, steps):
+    """bucket.cu's resolve as it runs: tiles of `tile` sorted entries, each
+    entry scanning back at most `steps` entries inside its tile and band; the
+    rest listed and resolved by the warp-per-entry pass in chunks of 32."""
+    total = n * bands
+    rep = np.full(total, -1, np.int64)
+    slow = []
+    for t0 in range(0, total, tile):
+        for e in range(t0, min(t0 + tile, total)):
+            first = e // n * n
+            lo = max(first, t0)
+            room = e - lo
+            reach = min(room, steps)
+            sig, bkt, r, settled = sk[e], sk[e] & low_mask, sv[e], False
+            for d in range(1, reach + 1):
+                s = sk[e - d]
+                if (s & low_mask) != bkt:
+                    settled = True
+                    break
+                if s == sig:
+                    r, settled = sv[e - d], True
+                    break
+            if not settled and reach == room and lo == first:
+                settled = True
+            if settled:
+                rep[first + sv[e]] = r
+            else:
+                slow.append(e)
+    for e in slow:  # one warp per entry
+        first = e // n * n
+        sig, bkt, r = sk[e], sk[e] & low_mask, sv[e]
+        base = e
+        while base > first:
+            lanes = [base - 1 - l for l in range(32)]
+            stop = None
+            for l, q in enumerate(lanes):
+                if q < first or (sk[q] & low_mask) != bkt:
+                    stop = (l, False)
+                    break
+                if sk[q] == sig:
+                    stop = (l, True)
+                    break
+            if stop is not None:
+                if stop[1]:
+                    r = sv[lanes[stop[0]]]
+                break
+            base = base - 32 if base >= first + 32 else first
+        rep[first + sv[e]] = r
+    return rep, len(slow)
+
+
+@pytest.mark.parametrize("tile,steps", [(64, 4), (100, 1), (4096, 64)])
+def test_two_phase_resolve_equals_reference_grouping(tile, steps):
+    """Three bands of family signatures with a long run of one signature whose
+    low 16 bits collide with another's (a far predecessor), band boundaries
+    inside tiles."""
+    rng = np.random.default_rng(tile + steps)
+    n, bands = 3000, 3
+    rows = []
+    for b in range(bands):
+        sig = family_sigs(rng, n, 300, 0.7)
+        sig[500:2500:7] = 0x12345A5A                  # a long run of one signature ...
+        sig[[499, 2600, 2900]] = 0x77775A5A           # ... and one with the same low bits
+        rows.append(sig)
+    sk_parts, sv_parts = [], []
+    for sig in rows:
+        order = np.argsort(sig & 0xFFFF, kind="stable")
+        sk_parts.append(sig[order].astype(np.int64))
+        sv_parts.append(order.astype(np.int64))
+    sk, sv = np.concatenate(sk_parts), np.concatenate(sv_parts)
+    rep, far = two_phase_replay(sk, sv, n, bands, 0xFFFF, tile, steps)
+    assert far > 0
+    for b, sig in enumerate(rows):
+        assert np.array_equal(rep[b * n:(b + 1) * n], oracle.bucket_band(sig).astype(np.int64))
