@@ -111,9 +111,13 @@ rep_resolve_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__
   }
 }
 
-// The listed entries: one warp per entry, lane l testing entry e - 1 - 32s - l
-// at step s; the nearest lane holding the signature gives the predecessor
-// unless a nearer lane is outside the bucket (or the band starts first).
+// The listed entries: one warp per entry, lane l testing entries
+// base - 1 - 32j - l for j < kFarChunks at each step (all loads in flight
+// together, base moving down kFarChunks * 32 a step); the nearest lane holding
+// the signature gives the predecessor unless a nearer one is outside the
+// bucket (or the band starts first).
+constexpr uint32_t kFarChunks = 4;
+
 __global__ void __launch_bounds__(256)
 rep_resolve_far_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__ sv,
                        uint32_t n, uint32_t low_mask, const uint64_t *__restrict__ slow,
@@ -126,19 +130,28 @@ rep_resolve_far_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restri
     const uint64_t first = e / n * n;
     const uint32_t sig = sk[e], bkt = sig & low_mask, self = sv[e];
     uint32_t r = self;
-    for (uint64_t base = e; base > first;) {  // warp-uniform
-      const uint64_t q = base - 1u - lane;     // base - 32 .. base - 1
-      const bool in = base >= first + 1u + lane;
-      const uint32_t s = in ? __ldg(sk + q) : 0u;
-      const uint32_t hit = __ballot_sync(kFull, in && s == sig);
-      const uint32_t out = __ballot_sync(kFull, !in || (s & low_mask) != bkt);
-      const uint32_t stop = hit | out;
-      if (stop) {
-        const uint32_t l = __ffs(stop) - 1u;  // the nearest
-        if ((hit >> l) & 1u) r = __shfl_sync(kFull, in ? __ldg(sv + q) : 0u, l);
-        break;
+    bool done = false;
+    for (uint64_t base = e; base > first && !done;) {  // warp-uniform
+      uint32_t v[kFarChunks];
+      bool in[kFarChunks];
+#pragma unroll
+      for (uint32_t j = 0; j < kFarChunks; ++j) {
+        in[j] = base >= first + 1u + lane + 32u * j;
+        v[j] = in[j] ? __ldg(sk + (base - 1u - lane - 32u * j)) : 0u;
       }
-      base = base >= first + 32u ? base - 32u : first;
+#pragma unroll
+      for (uint32_t j = 0; j < kFarChunks; ++j) {
+        if (done) break;
+        const uint32_t hit = __ballot_sync(kFull, in[j] && v[j] == sig);
+        const uint32_t out = __ballot_sync(kFull, !in[j] || (v[j] & low_mask) != bkt);
+        const uint32_t stop = hit | out;
+        if (stop) {
+          const uint32_t l = __ffs(stop) - 1u;  // the nearest
+          if ((hit >> l) & 1u) r = __ldg(sv + (base - 1u - l - 32u * j));
+          done = true;
+        }
+      }
+      base = base >= first + 32u * kFarChunks ? base - 32u * kFarChunks : first;
     }
     if (lane == 0) rep[first + self] = r;
   }

@@ -70,7 +70,8 @@ def test_resolve_replay_low_bits_collide():
 def two_phase_replay(sk, sv, n, bands, low_mask, tile, steps):
     """bucket.cu's resolve as it runs: tiles of `tile` sorted entries, each
     entry scanning back at most `steps` entries inside its tile and band; the
-    rest listed and resolved by the warp-per-entry pass in chunks of 32."""
+    rest listed and resolved by the warp-per-entry pass, which tests four
+    chunks of 32 entries a step and takes the nearest stop."""
     total = n * bands
     rep = np.full(total, -1, np.int64)
     slow = []
@@ -95,25 +96,23 @@ def two_phase_replay(sk, sv, n, bands, low_mask, tile, steps):
                 rep[first + sv[e]] = r
             else:
                 slow.append(e)
-    for e in slow:  # one warp per entry
+    for e in slow:  # one warp per entry, four chunks of 32 lanes a step
         first = e // n * n
         sig, bkt, r = sk[e], sk[e] & low_mask, sv[e]
-        base = e
-        while base > first:
-            lanes = [base - 1 - l for l in range(32)]
-            stop = None
-            for l, q in enumerate(lanes):
-                if q < first or (sk[q] & low_mask) != bkt:
-                    stop = (l, False)
+        base, done = e, False
+        while base > first and not done:
+            for j in range(4):
+                for l in range(32):
+                    q = base - 1 - 32 * j - l
+                    if q < first or (sk[q] & low_mask) != bkt:
+                        done = True
+                        break
+                    if sk[q] == sig:
+                        r, done = sv[q], True
+                        break
+                if done:
                     break
-                if sk[q] == sig:
-                    stop = (l, True)
-                    break
-            if stop is not None:
-                if stop[1]:
-                    r = sv[lanes[stop[0]]]
-                break
-            base = base - 32 if base >= first + 32 else first
+            base = base - 128 if base >= first + 128 else first
         rep[first + sv[e]] = r
     return rep, len(slow)
 
