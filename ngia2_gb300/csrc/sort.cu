@@ -153,109 +153,149 @@ static uint32_t scan_chunks(uint32_t ntiles) {
   return len > kScanChunk ? ceil_div(len, kScanChunk) : 0u;
 }
 
-// The tile's keys and values are staged in shared memory (coalesced loads,
-// all in flight at once); then each warp takes a contiguous sub-tile of
-// kTile / kSortWarps keys:
-//   1. the warp counts its sub-tile's digits (warp-private counts);
-//   2. per digit, the block turns the counts into each warp's first slot
-//      (the tile's offset from the scan, plus the counts of the warps before);
-//   3. each warp writes its keys in order, ranking equal digits within a round
-//      of 32 by ballots and advancing its own slots -- no block barrier
-//      between rounds, three per tile.
+// Scatter of one tile of kTile keys and values.  Each warp takes a contiguous
+// sub-tile of kWarpKeys, held in registers (lane l: keys 32r + l):
+//   1. rank: per round of 32 keys, each lane sets its bit in a warp-private
+//      mask of its digit (a shared-memory atomic OR), reads the mask back --
+//      the lanes sharing its digit -- and takes its slot among them after the
+//      warp's running count of that digit, which the lowest of them advances;
+//      three mask buffers in rotation, so one warp barrier per round;
+//   2. the block turns the warp counts into tile-local slots per (warp, digit)
+//      and the scanned offsets into each digit's global first slot;
+//   3. keys and values go to their tile-local slots in shared memory (the
+//      tile sorted by digit), then out in that order: consecutive threads
+//      write consecutive slots of a digit's run, so stores coalesce.
 // Stable: warps hold consecutive sub-tiles, rounds and lanes go in key order.
 constexpr uint32_t kWarpKeys = kTile / kSortWarps;
 constexpr uint32_t kRounds = kWarpKeys / 32;
-constexpr uint32_t kLoads = kTile / kSortThreads;
+constexpr uint32_t kMaskBufs = 3;
+// shared memory, in u32: sorted keys and values (the rank masks live in their
+// space until the tile is placed), per-warp digit counts / slots, per-digit
+// global first slots (less the tile-local one), the block scan's warp totals
+constexpr uint32_t kSmSorted = 2 * kTile;
+constexpr uint32_t kSmCount = kSmSorted;
+constexpr uint32_t kSmGlobal = kSmCount + kSortWarps * 256;
+constexpr uint32_t kSmWarpSum = kSmGlobal + 256;
+constexpr uint32_t kSmWords = kSmWarpSum + kSortWarps;
+static_assert(kMaskBufs * kSortWarps * 256 <= kSmSorted, "masks fit the sorted tile's space");
+static_assert(kSortThreads == 256, "one thread per digit in the block scan");
 
-// lanes holding the same digit as this one: one ballot per digit bit (a
-// constant eight ballots, whatever the number of distinct digits in the
-// warp); lanes outside `valid` match nobody
-__device__ __forceinline__ uint32_t digit_peers(uint32_t d, uint32_t valid) {
-  uint32_t peers = valid;
-#pragma unroll
-  for (int b = 0; b < 8; ++b) {
-    const uint32_t m = __ballot_sync(kFull, (d >> b) & 1u);
-    peers &= ((d >> b) & 1u) ? m : ~m;
-  }
-  return peers;
-}
-
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, 4)
 rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                   uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                   uint32_t seg_len, int shift, uint32_t ntiles,
                   const uint32_t *__restrict__ offsets) {
   extern __shared__ uint32_t rs_smem[];
-  uint32_t *tk = rs_smem, *tv = rs_smem + kTile;
-  uint32_t(*slot)[256] = reinterpret_cast<uint32_t(*)[256]>(rs_smem + 2 * kTile);
+  uint32_t *sk = rs_smem, *sv = rs_smem + kTile;
+  uint32_t *mask = rs_smem;  // [kMaskBufs][kSortWarps][256], inside the sorted space
+  uint32_t(*count)[256] = reinterpret_cast<uint32_t(*)[256]>(rs_smem + kSmCount);
+  uint32_t *global = rs_smem + kSmGlobal;
+  uint32_t *wsum = rs_smem + kSmWarpSum;
   const uint32_t seg = blockIdx.y, tile = blockIdx.x;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const size_t so = (size_t)seg * seg_len;
   const uint32_t t0 = tile * kTile;
-  {
-    uint32_t a[kLoads], b[kLoads];
+  const uint32_t cnt = seg_len - t0 < kTile ? seg_len - t0 : kTile;  // keys in this tile
+  const uint32_t w0 = warp * kWarpKeys;                              // the warp's first key
+  // keys in registers through the rank; values are read again when placed
+  // (from L2: the block read them moments before), which keeps the registers
+  // to keys and ranks
+  const size_t my = so + t0 + w0 + lane;  // the lane's first key; round r adds 32r
+  const uint32_t mine = cnt > w0 + lane ? cnt - w0 - lane : 0u;  // round r valid: 32r < mine
+  uint32_t key[kRounds], rank[kRounds];
 #pragma unroll
-    for (uint32_t j = 0; j < kLoads; ++j) {
-      const uint32_t i = t0 + j * kSortThreads + threadIdx.x;
-      a[j] = i < seg_len ? kin[so + i] : 0u;
-      b[j] = i < seg_len ? (vin ? vin[so + i] : i) : 0u;
-    }
+  for (uint32_t r = 0; r < kRounds; ++r) key[r] = 32 * r < mine ? kin[my + 32 * r] : 0u;
+  if (vin && lane < kRounds && w0 + 32 * lane < cnt)  // the warp's value lines into L2
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(vin + so + t0 + w0 + 32 * lane));
+  for (uint32_t i = threadIdx.x; i < kMaskBufs * kSortWarps * 256; i += kSortThreads) mask[i] = 0;
 #pragma unroll
-    for (uint32_t j = 0; j < kLoads; ++j) {
-      tk[j * kSortThreads + threadIdx.x] = a[j];
-      tv[j * kSortThreads + threadIdx.x] = b[j];
-    }
-  }
-#pragma unroll
-  for (uint32_t w = 0; w < kSortWarps; ++w) slot[w][threadIdx.x] = 0;
+  for (uint32_t w = 0; w < kSortWarps; ++w) count[w][threadIdx.x] = 0;
   __syncthreads();
-  const uint32_t lt_mask = (1u << lane) - 1u;
-  const uint32_t w0 = warp * kWarpKeys;  // the warp's first key in the tile
-  // 1. the warp's digit counts
-#pragma unroll 2
+
+  // 1. rank within the warp
+  const uint32_t bit = 1u << lane, lt_mask = bit - 1u;
+  uint32_t *wmask = mask + warp * 256;
+  uint32_t *wcount = count[warp];
+  uint32_t clear = kFull;  // the entry this lane led last round (cleared one round later)
+#pragma unroll
   for (uint32_t r = 0; r < kRounds; ++r) {
-    const uint32_t k = w0 + 32 * r + lane;
-    const uint32_t valid = __ballot_sync(kFull, t0 + k < seg_len);
-    if (!valid) break;  // warp-uniform: the tile's end
-    const uint32_t d = (tk[k] >> shift) & 255u;
-    const uint32_t peers = digit_peers(d, valid);
-    if ((valid >> lane & 1u) && (peers & lt_mask) == 0) slot[warp][d] += __popc(peers);
+    const bool valid = 32 * r < mine;
+    const uint32_t d = (key[r] >> shift) & 255u;
+    uint32_t *m = wmask + (r % kMaskBufs) * (kSortWarps * 256);
+    if (valid) atomicOr(m + d, bit);
     __syncwarp();
+    const uint32_t peers = valid ? m[d] : 0u;
+    const uint32_t leader = peers ? __ffs(peers) - 1u : lane;
+    const uint32_t seen = valid && leader == lane ? wcount[d] : 0u;  // the leaders read
+    const uint32_t base = __shfl_sync(kFull, seen, leader);
+    // last round's masks: every lane has read them (the barrier above)
+    if (clear != kFull) wmask[clear] = 0u;
+    clear = kFull;
+    if (valid && (peers & lt_mask) == 0) {
+      wcount[d] = base + __popc(peers);
+      clear = (r % kMaskBufs) * (kSortWarps * 256) + d;
+    }
+    rank[r] = base + __popc(peers & lt_mask);
   }
   __syncthreads();
-  // 2. each warp's first slot per digit (thread t: digit t)
+
+  // 2. tile-local slots per (warp, digit) and each digit's global first slot
   {
-    uint32_t run = offsets[((size_t)seg * 256 + threadIdx.x) * ntiles + tile];
+    const uint32_t t = threadIdx.x;  // digit t
+    uint32_t tot = 0;
 #pragma unroll
     for (uint32_t w = 0; w < kSortWarps; ++w) {
-      const uint32_t c = slot[w][threadIdx.x];
-      slot[w][threadIdx.x] = run;
-      run += c;
+      const uint32_t c = count[w][t];
+      count[w][t] = tot;
+      tot += c;
     }
+    uint32_t x = tot;  // inclusive scan over digits
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kSortWarps; ++w) before += w < warp ? wsum[w] : 0u;
+    const uint32_t first = before + x - tot;  // tile-local first slot of digit t
+#pragma unroll
+    for (uint32_t w = 0; w < kSortWarps; ++w) count[w][t] += first;
+    global[t] = offsets[((size_t)seg * 256 + t) * ntiles + tile] - first;
   }
   __syncthreads();
-  // 3. the warp's keys in order
-#pragma unroll 2
+
+  // 3. the tile sorted by digit in shared memory, then written out in order
+#pragma unroll
   for (uint32_t r = 0; r < kRounds; ++r) {
-    const uint32_t k = w0 + 32 * r + lane;
-    const uint32_t valid = __ballot_sync(kFull, t0 + k < seg_len);
-    if (!valid) break;
-    const uint32_t key = tk[k];
-    const uint32_t d = (key >> shift) & 255u;
-    const uint32_t peers = digit_peers(d, valid);
-    const bool mine = valid >> lane & 1u;
-    if (mine) {
-      const uint32_t pos = slot[warp][d] + __popc(peers & lt_mask);
-      kout[so + pos] = key;
-      vout[so + pos] = tv[k];
+    if (32 * r < mine) {
+      rank[r] += wcount[(key[r] >> shift) & 255u];  // now the key's slot
+      sk[rank[r]] = key[r];
     }
-    __syncwarp();
-    if (mine && (peers & lt_mask) == 0) slot[warp][d] += __popc(peers);
-    __syncwarp();
+  }
+  if (vin) {
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; ++r)
+      if (32 * r < mine) sv[rank[r]] = vin[my + 32 * r];
+  } else {
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; ++r)
+      if (32 * r < mine) sv[rank[r]] = t0 + w0 + lane + 32 * r;
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < cnt; i += kSortThreads) {
+    const uint32_t k = sk[i];
+    const uint32_t pos = global[(k >> shift) & 255u] + i;  // mod 2^32: the digit's slot
+    if (pos < seg_len) {
+      kout[so + pos] = k;
+      vout[so + pos] = sv[i];
+    }
   }
 }
 
-constexpr size_t kScatterSmem = (2 * kTile + kSortWarps * 256) * sizeof(uint32_t);
+constexpr size_t kScatterSmem = kSmWords * sizeof(uint32_t);
 
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs) {
   const size_t ntiles = ceil_div<size_t>(seg_len, kTile);
