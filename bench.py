@@ -886,7 +886,7 @@ def run_pairs(args) -> dict:
     t0 = time.time()
     plan = default_plan
     if not args.no_autotune:
-        plan, _ = ctx.autotune(d_pairs.data_ptr(), sample, PAIRS_IDENTITY, 2)
+        plan, _ = ctx.autotune(d_pairs.data_ptr(), sample, PAIRS_IDENTITY, 3)
     tune_s = time.time() - t0
     for _ in range(warm):
         batched()

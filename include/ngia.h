@@ -222,7 +222,7 @@ int ngia_ctx_edges(ngia_ctx *ctx, ngia_edge *h_edges, uint64_t cap);
  * :192-253; 0 for pairs failing the length filter), computed by the
  * length-binned persistent kernels: pairs are binned by band width, each bin
  * is queued longest first and taken by a persistent grid -- one pair per lane
- * for narrow bands, one pair per group of 16 or 32 lanes for wide ones.
+ * for narrow bands, one pair per group of 8, 16 or 32 lanes for wide ones.
  * d_pairs: count (rep, tar) u32 index pairs on the device, every index below
  * the loaded record count (not checked); d_scores: count u32 out.  The
  * context's own pair scratch is not touched.  Synchronises. */
@@ -233,12 +233,12 @@ int ngia_ctx_align_pairs(ngia_ctx *ctx, const uint32_t *d_pairs, uint32_t count,
  * classes: one pair per lane with a window of W = 4, 5, ..., 12, 14, 16 words for
  * pairs whose window ls + min(rs, nr) (in 32-residue blocks) is at most
  * stream_max; otherwise the first group class -- G lanes per pair with K
- * words per lane: (16,1) (16,2) (16,4) (32,4) (32,8) (32,16) -- whose
+ * words per lane: (8,3) (8,4) (16,4) (16,6) (32,4) (32,6) (32,8) (32,16) -- whose
  * group_limit admits the band (ls + rs <= group_limit, or a rep of at most G
  * slices); otherwise one pair per thread.  group_limit 0 leaves a class
  * unused; a limit above (G-1)K + G is refused.  Scores never depend on the
  * plan. */
-#define NGIA_GROUP_CLASSES 6
+#define NGIA_GROUP_CLASSES 8
 typedef struct ngia_plan {
   uint32_t stream_max; /* 4..16 */
   uint32_t group_limit[NGIA_GROUP_CLASSES];

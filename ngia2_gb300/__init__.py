@@ -56,7 +56,12 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-GROUP_SHAPES = [(16, 1), (16, 2), (16, 4), (32, 4), (32, 8), (32, 16)]  # (lanes, words)
+GROUP_SHAPES = [(8, 3), (8, 4), (16, 4), (16, 6), (32, 4), (32, 6), (32, 8), (32, 16)]  # (lanes, words)
+# class numbers of the batched aligner (align.cuh): 11 one-pair-per-lane
+# windows, the group classes, the general kernel, then the length-filter skip
+FIRST_GROUP_CLASS = 11
+GENERAL_CLASS = FIRST_GROUP_CLASS + len(GROUP_SHAPES)
+SKIP_CLASS = GENERAL_CLASS + 1
 
 
 class Plan(C.Structure):

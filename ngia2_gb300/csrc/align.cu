@@ -570,18 +570,24 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
 #undef NGIA_STREAM_CASE
 #define NGIA_GROUP_CASE(C) \
   case C: return launch_group<group_shape(C).G, group_shape(C).K>(a, ab.K, cls, cursor, s);
-    NGIA_GROUP_CASE(11)
-    NGIA_GROUP_CASE(12)
-    NGIA_GROUP_CASE(13)
-    NGIA_GROUP_CASE(14)
+    NGIA_GROUP_CASE(kFirstGroupClass)
+    NGIA_GROUP_CASE(kFirstGroupClass + 1)
+    NGIA_GROUP_CASE(kFirstGroupClass + 2)
+    NGIA_GROUP_CASE(kFirstGroupClass + 3)
+    NGIA_GROUP_CASE(kFirstGroupClass + 4)
+    NGIA_GROUP_CASE(kFirstGroupClass + 5)
 #undef NGIA_GROUP_CASE
-    case 15:
-      static_assert(group_shape(15).G == 32 && group_shape(16).G == 32, "block-wide classes");
-      return NGIA_CTA_WARPS ? launch_group_cta<group_shape(15).K>(a, ab.K, cls, cursor, s)
-                            : launch_group<32, group_shape(15).K>(a, ab.K, cls, cursor, s);
-    case 16:
-      return NGIA_CTA_WARPS ? launch_group_cta<group_shape(16).K>(a, ab.K, cls, cursor, s)
-                            : launch_group<32, group_shape(16).K>(a, ab.K, cls, cursor, s);
+    case kFirstGroupClass + 6:
+      static_assert(group_shape(kFirstGroupClass + 6).G == 32 &&
+                        group_shape(kFirstGroupClass + 7).G == 32 && kNumGroupClasses == 8,
+                    "block-wide classes: the two widest");
+      return NGIA_CTA_WARPS
+                 ? launch_group_cta<group_shape(kFirstGroupClass + 6).K>(a, ab.K, cls, cursor, s)
+                 : launch_group<32, group_shape(kFirstGroupClass + 6).K>(a, ab.K, cls, cursor, s);
+    case kFirstGroupClass + 7:
+      return NGIA_CTA_WARPS
+                 ? launch_group_cta<group_shape(kFirstGroupClass + 7).K>(a, ab.K, cls, cursor, s)
+                 : launch_group<32, group_shape(kFirstGroupClass + 7).K>(a, ab.K, cls, cursor, s);
     case kGeneralClass: {
       uint32_t grid = 0;
       NGIA_TRY(persistent_grid(align_general_kernel, 128, 0, kFull, &grid));

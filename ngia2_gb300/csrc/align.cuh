@@ -259,26 +259,34 @@ __device__ inline uint32_t lcs_general(const uint32_t *__restrict__ rep,
 //          per lane, W = 4, 5, ..., 12, 14, 16 words by stream_width (every
 //          width up to 12: a window word above the band costs as much as a
 //          live one, and bands of equal ls + rs - 1 are common)
-//   11..16 group kernel (align_group.cuh), one pair per group of G lanes with
-//          K words per lane: (16,1) (16,2) (16,4) (32,4) (32,8) (32,16)
-//   17     general kernel, one pair per thread (any width)
-//   18     pairs failing the length filter (score 0, not launched)
+//   11..18 group kernel (align_group.cuh), one pair per group of G lanes with
+//          K words per lane: (8,3) (8,4) (16,4) (16,6) (32,4) (32,6) (32,8)
+//          (32,16).  A column step costs a lane 3 ops per word plus a fixed
+//          ~6 (carry pop and push, code, table row), and a band of span S
+//          keeps about S / (K + 1) of the G lanes live, so the ladder takes
+//          each span to the shape with the fewest issue slots per cell: eight
+//          lanes of three or four words for the 17-36-word bands of medium
+//          proteins rather than sixteen lanes of one or two
+//   19     general kernel, one pair per thread (any width)
+//   20     pairs failing the length filter (score 0, not launched)
 constexpr int kNumLdsClasses = 11;
 constexpr int kFirstGroupClass = 11;
-constexpr int kNumGroupClasses = 6;
-constexpr int kGeneralClass = 17;
-constexpr int kSkipClass = 18;
-constexpr int kNumClasses = 19;
+constexpr int kNumGroupClasses = 8;
+constexpr int kGeneralClass = kFirstGroupClass + kNumGroupClasses;
+constexpr int kSkipClass = kGeneralClass + 1;
+constexpr int kNumClasses = kSkipClass + 1;
 
 struct GroupShape {
   int G, K;
 };
 __host__ __device__ constexpr GroupShape group_shape(int c) {
-  return c == kFirstGroupClass ? GroupShape{16, 1}
-       : c == kFirstGroupClass + 1 ? GroupShape{16, 2}
+  return c == kFirstGroupClass ? GroupShape{8, 3}
+       : c == kFirstGroupClass + 1 ? GroupShape{8, 4}
        : c == kFirstGroupClass + 2 ? GroupShape{16, 4}
-       : c == kFirstGroupClass + 3 ? GroupShape{32, 4}
-       : c == kFirstGroupClass + 4 ? GroupShape{32, 8}
+       : c == kFirstGroupClass + 3 ? GroupShape{16, 6}
+       : c == kFirstGroupClass + 4 ? GroupShape{32, 4}
+       : c == kFirstGroupClass + 5 ? GroupShape{32, 6}
+       : c == kFirstGroupClass + 6 ? GroupShape{32, 8}
                                    : GroupShape{32, 16};
 }
 

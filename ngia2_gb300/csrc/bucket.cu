@@ -180,8 +180,10 @@ int bucket(const uint32_t *sigs, uint32_t n, uint32_t bands, uint32_t *rep,
   uint64_t *slow = static_cast<uint64_t *>(sort_scratch);
   unsigned int *slow_count = reinterpret_cast<unsigned int *>(slow + total);
   NGIA_CUDA(cudaMemsetAsync(slow_count, 0, sizeof(unsigned int), s));
+  // one tile per block (up to 2^31 - 1 blocks), so that the blocks resident
+  // on an SM overlap one another's loads, scans and stores
   const size_t want = ceil_div<size_t>(total, kResolveTile);
-  const size_t cap = (size_t)sms * 4;  // resident blocks: 64 registers x 256 threads
+  const size_t cap = 0x7FFFFFFF;
   rep_resolve_kernel<<<(uint32_t)(want < cap ? want : cap), kResolveThreads, 0, s>>>(
       sk, sv, n, bands, low_mask, rep, slow, slow_count);
   NGIA_LAUNCHED();

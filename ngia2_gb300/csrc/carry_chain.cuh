@@ -182,6 +182,17 @@ __device__ __forceinline__ void add_chain2_pp(uint32_t *s, const uint32_t *a, co
       : "r"(a[0]), "r"(a[1]), "r"(b[0]), "r"(b[1]));
 }
 
+__device__ __forceinline__ void add_chain3_pp(uint32_t *s, const uint32_t *a, const uint32_t *b,
+                                              uint32_t &cin, uint32_t &cout) {
+  asm("add.cc.u32 %3, %3, %3;\n\t"
+      "addc.cc.u32 %0, %5, %8;\n\t"
+      "addc.cc.u32 %1, %6, %9;\n\t"
+      "addc.cc.u32 %2, %7, %10;\n\t"
+      "addc.u32 %4, %4, %4;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "+r"(cin), "+r"(cout)
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(b[0]), "r"(b[1]), "r"(b[2]));
+}
+
 __device__ __forceinline__ void add_chain4_pp(uint32_t *s, const uint32_t *a, const uint32_t *b,
                                               uint32_t &cin, uint32_t &cout) {
   asm("add.cc.u32 %4, %4, %4;\n\t"
@@ -192,6 +203,21 @@ __device__ __forceinline__ void add_chain4_pp(uint32_t *s, const uint32_t *a, co
       "addc.u32 %5, %5, %5;\n\t"
       : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "+r"(cin), "+r"(cout)
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]));
+}
+
+__device__ __forceinline__ void add_chain6_pp(uint32_t *s, const uint32_t *a, const uint32_t *b,
+                                              uint32_t &cin, uint32_t &cout) {
+  asm("add.cc.u32 %6, %6, %6;\n\t"
+      "addc.cc.u32 %0, %8, %14;\n\t"
+      "addc.cc.u32 %1, %9, %15;\n\t"
+      "addc.cc.u32 %2, %10, %16;\n\t"
+      "addc.cc.u32 %3, %11, %17;\n\t"
+      "addc.cc.u32 %4, %12, %18;\n\t"
+      "addc.cc.u32 %5, %13, %19;\n\t"
+      "addc.u32 %7, %7, %7;\n\t"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "+r"(cin), "+r"(cout)
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]),
+        "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]));
 }
 
 __device__ __forceinline__ void add_chain8_pp(uint32_t *s, const uint32_t *a, const uint32_t *b,
@@ -250,10 +276,12 @@ __device__ __forceinline__ void add_words_pp(uint32_t *s, const uint32_t *a, con
                                              uint32_t &cin, uint32_t &cout) {
   if constexpr (K == 1) add_chain1_pp(s, a, b, cin, cout);
   else if constexpr (K == 2) add_chain2_pp(s, a, b, cin, cout);
+  else if constexpr (K == 3) add_chain3_pp(s, a, b, cin, cout);
   else if constexpr (K == 4) add_chain4_pp(s, a, b, cin, cout);
+  else if constexpr (K == 6) add_chain6_pp(s, a, b, cin, cout);
   else if constexpr (K == 8) add_chain8_pp(s, a, b, cin, cout);
   else {
-    static_assert(K == 16, "carry-word chains of 1, 2, 4, 8 or 16 words");
+    static_assert(K == 16, "carry-word chains of 1, 2, 3, 4, 6, 8 or 16 words");
     uint32_t c;
     add_chain8_pc(s, a, b, cin, c);
     add_chain8_cp(s + 8, a + 8, b + 8, c, cout);

@@ -686,8 +686,9 @@ int ngia_ctx_autotune(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count, uint
   if (identity < 1 || identity > 99 || count == 0) return NGIA_ERR_ARG;
   if (reps < 1) reps = 1;
   NGIA_TRY(c->scores.reserve((size_t)count * 4));
-  const bool graphs = c->round.use_graphs;
-  c->round.use_graphs = false;
+  // timed the way the round runs (replayed as a graph when graphs are on; a
+  // plan change recaptures, so the first of the reps carries the capture and
+  // the best of them is kept)
   const uint2 *pairs = reinterpret_cast<const uint2 *>(d_pairs);
   auto time_plan = [&](const ngia_plan &p, double *ms) -> int {
     NGIA_TRY(ngia_ctx_set_plan(c, &p));
@@ -731,7 +732,6 @@ int ngia_ctx_autotune(ngia_ctx *c, const uint32_t *d_pairs, uint32_t count, uint
       }
     }
   }
-  c->round.use_graphs = graphs;
   if (rc != NGIA_OK) return rc;
   NGIA_TRY(ngia_ctx_set_plan(c, &cur));
   if (best) *best = cur;

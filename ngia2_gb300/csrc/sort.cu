@@ -148,9 +148,12 @@ chunk_apply_kernel(uint32_t *__restrict__ data, uint32_t len, uint32_t nchunks,
   }
 }
 
+// Counts up to kScanOneBlock per segment are scanned by one block per segment
+// (16 per thread: one launch instead of three); longer ones in chunks.
+constexpr uint32_t kScanOneBlock = 16384;
 static uint32_t scan_chunks(uint32_t ntiles) {
   const uint32_t len = 256 * ntiles;
-  return len > kScanChunk ? ceil_div(len, kScanChunk) : 0u;
+  return len > kScanOneBlock ? ceil_div(len, kScanChunk) : 0u;
 }
 
 // Scatter of one tile of kTile keys and values.  Each warp takes a contiguous

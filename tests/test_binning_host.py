@@ -127,4 +127,6 @@ def test_every_pair_lands_in_a_class_that_holds_it(tmp_path, built):
     for lr, lt, identity, cls in rows:
         assert width_class(lr, lt, identity) == cls, (lr, lt, identity, cls)
         seen.add(cls)
-    assert {0, 10, 17, 18} <= seen and set(range(11, 17)) & seen, sorted(seen)
+    import ngia2_gb300 as ng
+    assert {0, 10, ng.GENERAL_CLASS, ng.SKIP_CLASS} <= seen, sorted(seen)
+    assert set(range(ng.FIRST_GROUP_CLASS, ng.GENERAL_CLASS)) & seen, sorted(seen)

@@ -1,6 +1,6 @@
 """The batched aligner on caller-given pairs (ngia_ctx_align_pairs): every
-width class -- one pair per lane for narrow bands, groups of 16 and 32 lanes
-for wide ones, the general kernel beyond -- against the oracle, pair by pair,
+width class -- one pair per lane for narrow bands, groups of 8, 16 and 32
+lanes for wide ones, the general kernel beyond -- against the oracle, pair by pair,
 and against the drop-in one-thread-per-pair kernel."""
 from __future__ import annotations
 
@@ -18,16 +18,16 @@ def width_class(lr: int, lt: int, identity: int) -> int:
     """The class the library bins a pair into (align.cuh width_class)."""
     bb = oracle.band_bounds(lr, lt, identity, oracle.ROUND_FMA)
     if bb is None:
-        return 18
+        return ng.SKIP_CLASS
     lsft, rsft = bb
     ls, rs, nr = lsft // 32, (rsft + 31) // 32, (lr + 31) // 32
     ws = ls + min(rs, nr)
     if ws <= 16:
         return 0 if ws <= 4 else ws - 4 if ws <= 12 else 9 if ws <= 14 else 10
-    for c, (g, k) in enumerate(GROUP_SHAPES, start=11):
+    for c, (g, k) in enumerate(GROUP_SHAPES, start=ng.FIRST_GROUP_CLASS):
         if (nr + k - 1) // k <= g or ls + rs <= (g - 1) * k + g:
             return c
-    return 17
+    return ng.GENERAL_CLASS
 
 
 def mutate(rng, s: bytes, sub: float, indel: float) -> bytes:
@@ -95,7 +95,7 @@ def test_batched_pairs_match_oracle(cuda, built, identity):
     assert st["unique_pairs"] == len(pairs)
     assert (want > 0).any() and (want == 0).any()
     # the set reaches the group kernels at every identity
-    assert classes & set(range(11, 17)), sorted(classes)
+    assert classes & set(range(ng.FIRST_GROUP_CLASS, ng.GENERAL_CLASS)), sorted(classes)
 
 
 @pytest.mark.gpu
@@ -141,8 +141,8 @@ def test_every_group_class_is_covered(built):
         seqs, pairs = pair_set(identity, 900 + identity)
         lens = [len(s) for s in seqs]
         seen |= {width_class(lens[r], lens[t], identity) for r, t in pairs}
-    assert set(range(11, 17)) <= seen, sorted(seen)
-    assert {0, 17} <= seen, sorted(seen)
+    assert set(range(ng.FIRST_GROUP_CLASS, ng.GENERAL_CLASS)) <= seen, sorted(seen)
+    assert {0, ng.GENERAL_CLASS} <= seen, sorted(seen)
 
 
 @pytest.mark.gpu
@@ -161,8 +161,9 @@ def test_plans_change_binning_not_scores(cuda, built):
         limits = default["group_limit"]
         assert limits == [(g - 1) * k + g for g, k in ng.GROUP_SHAPES]
         for plan in ({"stream_max": 8, "group_limit": limits},
-                     {"stream_max": 4, "group_limit": [0, limits[1], 0, limits[3], 0, 0]},
-                     {"stream_max": 12, "group_limit": [0] * 6}):
+                     {"stream_max": 4, "group_limit": [0, limits[1], 0, limits[3], 0, 0,
+                                                      limits[6], 0]},
+                     {"stream_max": 12, "group_limit": [0] * len(limits)}):
             ctx.set_plan(plan)
             assert ctx.plan() == plan
             got, _ = ctx.align_pairs(pairs, 70)

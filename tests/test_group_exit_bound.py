@@ -27,7 +27,7 @@ import numpy as np
 import pytest
 
 FULL = (1 << 32) - 1
-SHAPES = [(16, 1), (16, 2), (16, 4), (32, 4), (32, 8), (32, 16)]  # (G, K) of the group classes
+SHAPES = [(8, 3), (8, 4), (16, 4), (16, 6), (32, 4), (32, 6), (32, 8), (32, 16)]  # (G, K) of the group classes
 # the widest classes as they run, one block of four warps per pair
 # (align_group_cta.cuh): (32, 8) as (128, 2), (32, 16) as (128, 4)
 CTA_SHAPES = [(128, 2), (128, 4)]
