@@ -576,7 +576,7 @@ def hbm_rooflines(stats, st, n, hbm) -> dict:
     out = {}
     for name, ms_key, algo, kernel in (
             ("bucket", "ms_bucket", 8 * BANDS * n,
-             "rs_hist/rs_scatter (segmented radix sort) + rep_chain_kernel"),
+             "rs_hist/rs_scatter (segmented radix partition) + rep_resolve_kernel / rep_resolve_far_kernel"),
             ("emit", "ms_emit", 12 * st["unique_pairs"] + 12 * st["edges"],
              "emit_sorted (run counts, ordered compaction, radix sort by rep)")):
         ms = statistics.mean(s[ms_key] for s in stats)
@@ -586,6 +586,15 @@ def hbm_rooflines(stats, st, n, hbm) -> dict:
                      "frac": achieved / (hbm * 1e9) if hbm else None,
                      "peak_source": "measured: MEASURED_PEAKS hbm_gbs", "ms": ms,
                      "algorithmic_bytes": algo, "traffic": None}
+    # the partition form's own bytes per sequence and band: per pass a digit
+    # count (4) and a scatter (read and write key and value, 16), then the
+    # resolve (read key and value, write the rep entry: 12)
+    passes = 1 if n <= 1 << 10 else 2 if n <= 1 << 18 else 3 if n <= 1 << 26 else 4
+    impl = (20 * passes + 12) * BANDS * n
+    b = out["bucket"]
+    b["partition_passes"] = passes
+    b["implementation_bytes"] = impl
+    b["implementation_frac"] = impl / (b["ms"] * 1e-3) / (hbm * 1e9) if hbm and b["ms"] else None
     return out
 
 

@@ -116,7 +116,7 @@ rep_resolve_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__
 // together, base moving down kFarChunks * 32 a step); the nearest lane holding
 // the signature gives the predecessor unless a nearer one is outside the
 // bucket (or the band starts first).
-constexpr uint32_t kFarChunks = 4;
+constexpr uint32_t kFarChunks = 16;
 
 __global__ void __launch_bounds__(256)
 rep_resolve_far_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__ sv,

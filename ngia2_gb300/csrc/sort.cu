@@ -11,6 +11,8 @@
 //      running slots per digit) and writes the keys to their slots.
 // Stability makes the passes compose into a sort by (key, input order); with
 // values = input index that is exactly a sort by (key, index).
+#include <mutex>
+
 #include "kernels.cuh"
 
 namespace ngia {
@@ -24,13 +26,17 @@ rs_hist_kernel(const uint32_t *__restrict__ keys, uint32_t seg_len, int shift,
                uint32_t ntiles, uint32_t *__restrict__ counts) {
   __shared__ uint32_t h[kSortWarps][256];
   const uint32_t seg = blockIdx.y, tile = blockIdx.x, warp = threadIdx.x >> 5;
+  const uint32_t *k = keys + (size_t)seg * seg_len + tile * kTile + threadIdx.x;
+  const uint32_t cnt = seg_len - tile * kTile < kTile ? seg_len - tile * kTile : kTile;
+  uint32_t v[kTile / kSortThreads];  // every load in flight before the counts
+#pragma unroll
+  for (uint32_t j = 0; j < kTile / kSortThreads; ++j)
+    v[j] = threadIdx.x + j * kSortThreads < cnt ? k[j * kSortThreads] : 0u;
   for (uint32_t d = threadIdx.x; d < kSortWarps * 256; d += kSortThreads) (&h[0][0])[d] = 0;
   __syncthreads();
-  const uint32_t *k = keys + (size_t)seg * seg_len;
-  const uint32_t beg = tile * kTile;
-  const uint32_t end = min(beg + kTile, seg_len);
-  for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads)
-    atomicAdd(&h[warp][(k[i] >> shift) & 255u], 1u);
+#pragma unroll
+  for (uint32_t j = 0; j < kTile / kSortThreads; ++j)
+    if (threadIdx.x + j * kSortThreads < cnt) atomicAdd(&h[warp][(v[j] >> shift) & 255u], 1u);
   __syncthreads();
   uint32_t c = 0;
 #pragma unroll
@@ -157,7 +163,9 @@ static uint32_t scan_chunks(uint32_t ntiles) {
 }
 
 // Scatter of one tile of kTile keys and values.  Each warp takes a contiguous
-// sub-tile of kWarpKeys, held in registers (lane l: keys 32r + l):
+// sub-tile of kWarpKeys, its keys held in registers (lane l: keys 32r + l)
+// and its values, when the pass has any, copied into shared memory by
+// cp.async while the keys are ranked:
 //   1. rank: per round of 32 keys, each lane sets its bit in a warp-private
 //      mask of its digit (a shared-memory atomic OR), reads the mask back --
 //      the lanes sharing its digit -- and takes its slot among them after the
@@ -172,25 +180,36 @@ static uint32_t scan_chunks(uint32_t ntiles) {
 constexpr uint32_t kWarpKeys = kTile / kSortWarps;
 constexpr uint32_t kRounds = kWarpKeys / 32;
 constexpr uint32_t kMaskBufs = 3;
-// shared memory, in u32: sorted keys and values (the rank masks live in their
-// space until the tile is placed), per-warp digit counts / slots, per-digit
-// global first slots (less the tile-local one), the block scan's warp totals
-constexpr uint32_t kSmSorted = 2 * kTile;
-constexpr uint32_t kSmCount = kSmSorted;
+constexpr uint32_t kMaskWords = kSortWarps * 256;  // one buffer
+// shared memory, in u32: the sorted keys, the sorted values (where the values
+// are staged until the keys are placed), a spare region, per-warp digit
+// counts / slots, per-digit global first slots (less the tile-local one), the
+// block scan's warp totals.  Mask buffers 0 and 1 sit in the sorted keys'
+// space and buffer 2 in the spare region, clear of the staged values.
+constexpr uint32_t kSmKeys = 0;
+constexpr uint32_t kSmVals = kTile;
+constexpr uint32_t kSmSpare = 2 * kTile;
+constexpr uint32_t kSmCount = kSmSpare + kMaskWords;
 constexpr uint32_t kSmGlobal = kSmCount + kSortWarps * 256;
 constexpr uint32_t kSmWarpSum = kSmGlobal + 256;
 constexpr uint32_t kSmWords = kSmWarpSum + kSortWarps;
-static_assert(kMaskBufs * kSortWarps * 256 <= kSmSorted, "masks fit the sorted tile's space");
+static_assert(2 * kMaskWords <= kTile, "mask buffers 0 and 1 fit the sorted keys' space");
 static_assert(kSortThreads == 256, "one thread per digit in the block scan");
 
+__device__ __forceinline__ void cp_async4(uint32_t *smem, const uint32_t *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem));
+}
+
+template <bool kValues>
 __global__ void __launch_bounds__(kSortThreads, 4)
 rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                   uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                   uint32_t seg_len, int shift, uint32_t ntiles,
                   const uint32_t *__restrict__ offsets) {
   extern __shared__ uint32_t rs_smem[];
-  uint32_t *sk = rs_smem, *sv = rs_smem + kTile;
-  uint32_t *mask = rs_smem;  // [kMaskBufs][kSortWarps][256], inside the sorted space
+  uint32_t *sk = rs_smem + kSmKeys, *sv = rs_smem + kSmVals;
   uint32_t(*count)[256] = reinterpret_cast<uint32_t(*)[256]>(rs_smem + kSmCount);
   uint32_t *global = rs_smem + kSmGlobal;
   uint32_t *wsum = rs_smem + kSmWarpSum;
@@ -200,31 +219,36 @@ rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__
   const uint32_t t0 = tile * kTile;
   const uint32_t cnt = seg_len - t0 < kTile ? seg_len - t0 : kTile;  // keys in this tile
   const uint32_t w0 = warp * kWarpKeys;                              // the warp's first key
-  // keys in registers through the rank; values are read again when placed
-  // (from L2: the block read them moments before), which keeps the registers
-  // to keys and ranks
   const size_t my = so + t0 + w0 + lane;  // the lane's first key; round r adds 32r
   const uint32_t mine = cnt > w0 + lane ? cnt - w0 - lane : 0u;  // round r valid: 32r < mine
   uint32_t key[kRounds], rank[kRounds];
 #pragma unroll
   for (uint32_t r = 0; r < kRounds; ++r) key[r] = 32 * r < mine ? kin[my + 32 * r] : 0u;
-  if (vin && lane < kRounds && w0 + 32 * lane < cnt)  // the warp's value lines into L2
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(vin + so + t0 + w0 + 32 * lane));
-  for (uint32_t i = threadIdx.x; i < kMaskBufs * kSortWarps * 256; i += kSortThreads) mask[i] = 0;
+  if constexpr (kValues) {  // the lane's values into the staging space, asynchronously
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; ++r)
+      if (32 * r < mine) cp_async4(sv + w0 + 32 * r + lane, vin + my + 32 * r);
+    asm volatile("cp.async.commit_group;\n" ::);
+  }
+  {
+    uint32_t *m0 = rs_smem + kSmKeys, *m2 = rs_smem + kSmSpare;
+    for (uint32_t i = threadIdx.x; i < 2 * kMaskWords; i += kSortThreads) m0[i] = 0;
+    for (uint32_t i = threadIdx.x; i < kMaskWords; i += kSortThreads) m2[i] = 0;
+  }
 #pragma unroll
   for (uint32_t w = 0; w < kSortWarps; ++w) count[w][threadIdx.x] = 0;
   __syncthreads();
 
   // 1. rank within the warp
   const uint32_t bit = 1u << lane, lt_mask = bit - 1u;
-  uint32_t *wmask = mask + warp * 256;
   uint32_t *wcount = count[warp];
-  uint32_t clear = kFull;  // the entry this lane led last round (cleared one round later)
+  uint32_t *clear = nullptr;  // the entry this lane led last round (cleared one round later)
 #pragma unroll
   for (uint32_t r = 0; r < kRounds; ++r) {
     const bool valid = 32 * r < mine;
     const uint32_t d = (key[r] >> shift) & 255u;
-    uint32_t *m = wmask + (r % kMaskBufs) * (kSortWarps * 256);
+    const uint32_t b = r % kMaskBufs;
+    uint32_t *m = rs_smem + (b < 2 ? kSmKeys + b * kMaskWords : kSmSpare) + warp * 256;
     if (valid) atomicOr(m + d, bit);
     __syncwarp();
     const uint32_t peers = valid ? m[d] : 0u;
@@ -232,11 +256,11 @@ rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__
     const uint32_t seen = valid && leader == lane ? wcount[d] : 0u;  // the leaders read
     const uint32_t base = __shfl_sync(kFull, seen, leader);
     // last round's masks: every lane has read them (the barrier above)
-    if (clear != kFull) wmask[clear] = 0u;
-    clear = kFull;
+    if (clear) *clear = 0u;
+    clear = nullptr;
     if (valid && (peers & lt_mask) == 0) {
       wcount[d] = base + __popc(peers);
-      clear = (r % kMaskBufs) * (kSortWarps * 256) + d;
+      clear = m + d;
     }
     rank[r] = base + __popc(peers & lt_mask);
   }
@@ -278,10 +302,15 @@ rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__
       sk[rank[r]] = key[r];
     }
   }
-  if (vin) {
+  if constexpr (kValues) {
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    uint32_t val[kRounds];  // the lane's own staged values, then their slots
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; ++r) val[r] = sv[w0 + 32 * r + lane];
+    __syncthreads();  // every staged value read before any is overwritten
 #pragma unroll
     for (uint32_t r = 0; r < kRounds; ++r)
-      if (32 * r < mine) sv[rank[r]] = vin[my + 32 * r];
+      if (32 * r < mine) sv[rank[r]] = val[r];
   } else {
 #pragma unroll
     for (uint32_t r = 0; r < kRounds; ++r)
@@ -299,6 +328,24 @@ rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__
 }
 
 constexpr size_t kScatterSmem = kSmWords * sizeof(uint32_t);
+
+// Above 48 KB of dynamic shared memory a kernel must opt in, once per device.
+static int scatter_smem_opt_in() {
+  static std::mutex mu;
+  static bool done[128] = {};
+  int dev = 0;
+  NGIA_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return NGIA_ERR_ARG;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!done[dev]) {
+    NGIA_CUDA(cudaFuncSetAttribute(rs_scatter_kernel<false>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem));
+    NGIA_CUDA(cudaFuncSetAttribute(rs_scatter_kernel<true>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem));
+    done[dev] = true;
+  }
+  return NGIA_OK;
+}
 
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs) {
   const size_t ntiles = ceil_div<size_t>(seg_len, kTile);
@@ -328,6 +375,7 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
     }
     return NGIA_ERR_ARG;  // identity values with zero passes: caller's job
   }
+  NGIA_TRY(scatter_smem_opt_in());
   const uint32_t *sk = keys_in, *sv = vals_in;
   for (int p = 0; p < passes; ++p) {
     // the last pass lands in keys_out / vals_out
@@ -349,8 +397,12 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
                                                              sums);
       NGIA_LAUNCHED();
     }
-    rs_scatter_kernel<<<grid, kSortThreads, kScatterSmem, s>>>(sk, sv, dk, dv, seg_len, shift,
-                                                               ntiles, counts);
+    if (sv)
+      rs_scatter_kernel<true><<<grid, kSortThreads, kScatterSmem, s>>>(sk, sv, dk, dv, seg_len,
+                                                                       shift, ntiles, counts);
+    else
+      rs_scatter_kernel<false><<<grid, kSortThreads, kScatterSmem, s>>>(sk, sv, dk, dv, seg_len,
+                                                                        shift, ntiles, counts);
     NGIA_LAUNCHED();
     sk = dk;
     sv = dv;

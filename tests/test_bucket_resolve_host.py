@@ -70,7 +70,7 @@ def test_resolve_replay_low_bits_collide():
 def two_phase_replay(sk, sv, n, bands, low_mask, tile, steps):
     """bucket.cu's resolve as it runs: tiles of `tile` sorted entries, each
     entry scanning back at most `steps` entries inside its tile and band; the
-    rest listed and resolved by the warp-per-entry pass, which tests four
+    rest listed and resolved by the warp-per-entry pass, which tests sixteen
     chunks of 32 entries a step and takes the nearest stop."""
     total = n * bands
     rep = np.full(total, -1, np.int64)
@@ -96,12 +96,12 @@ def two_phase_replay(sk, sv, n, bands, low_mask, tile, steps):
                 rep[first + sv[e]] = r
             else:
                 slow.append(e)
-    for e in slow:  # one warp per entry, four chunks of 32 lanes a step
+    for e in slow:  # one warp per entry, sixteen chunks of 32 lanes a step
         first = e // n * n
         sig, bkt, r = sk[e], sk[e] & low_mask, sv[e]
         base, done = e, False
         while base > first and not done:
-            for j in range(4):
+            for j in range(16):
                 for l in range(32):
                     q = base - 1 - 32 * j - l
                     if q < first or (sk[q] & low_mask) != bkt:
@@ -112,7 +112,7 @@ def two_phase_replay(sk, sv, n, bands, low_mask, tile, steps):
                         break
                 if done:
                     break
-            base = base - 128 if base >= first + 128 else first
+            base = base - 512 if base >= first + 512 else first
         rep[first + sv[e]] = r
     return rep, len(slow)
 
