@@ -15,7 +15,7 @@
 //      scans back through its bucket to the nearest entry with the same
 //      signature, which is its predecessor in index order (none: the entry is
 //      its own rep) -- within a tile staged in shared memory for the first
-//      steps, one warp per entry 32 entries a step beyond.
+//      steps, one warp per entry 512 entries a step beyond.
 // Two or three sort passes instead of four, and the chain written by the
 // resolve pass itself.  Equal signatures always share a bucket, so a scan
 // only passes entries of other signatures whose low bits collide -- a few on
@@ -43,7 +43,7 @@ static int partition_passes(uint32_t n) {
 // entry whose scan would go further -- its bucket began before the tile, or
 // a long run of another signature with the same low bits lies between it and
 // its predecessor -- is listed in `slow` and resolved by
-// rep_resolve_far_kernel, one warp per entry and 32 entries per step.  (A
+// rep_resolve_far_kernel, one warp per entry and 512 entries per step.  (A
 // scan of one thread per entry down to its answer lasted as long as the
 // longest one: on the 200k DNA set a few entries scan back over ~2,000
 // entries of another signature in global memory, and the kernel took 450 us.)
