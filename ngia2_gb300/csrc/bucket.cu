@@ -52,43 +52,48 @@ constexpr uint32_t kResolveThreads = 256;
 constexpr uint32_t kResolvePer = kResolveTile / kResolveThreads;
 constexpr uint32_t kResolveSteps = 64;
 
-__global__ void __launch_bounds__(kResolveThreads)
+__global__ void __launch_bounds__(kResolveThreads, 7)
 rep_resolve_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__ sv,
                    uint32_t n, uint32_t bands, uint32_t low_mask, uint32_t *__restrict__ rep,
                    uint64_t *__restrict__ slow, unsigned int *__restrict__ slow_count) {
   __shared__ uint32_t tk[kResolveTile], tv[kResolveTile];
   const uint64_t total = (uint64_t)n * bands;
-  const bool narrow = total <= 0xFFFFFFFFull;  // 32-bit division suffices
   for (uint64_t t0 = (uint64_t)blockIdx.x * kResolveTile; t0 < total;
        t0 += (uint64_t)gridDim.x * kResolveTile) {
     const uint32_t cnt = total - t0 < kResolveTile ? (uint32_t)(total - t0) : kResolveTile;
-    uint32_t a[kResolvePer], b[kResolvePer];
+    {
+      uint32_t a[kResolvePer], b[kResolvePer];  // every load in flight, then staged
 #pragma unroll
-    for (uint32_t j = 0; j < kResolvePer; ++j) {
-      const uint32_t k = threadIdx.x + j * kResolveThreads;
-      a[j] = k < cnt ? sk[t0 + k] : 0u;
-      b[j] = k < cnt ? sv[t0 + k] : 0u;
-    }
+      for (uint32_t j = 0; j < kResolvePer; ++j) {
+        const uint32_t k = threadIdx.x + j * kResolveThreads;
+        a[j] = k < cnt ? sk[t0 + k] : 0u;
+        b[j] = k < cnt ? sv[t0 + k] : 0u;
+      }
 #pragma unroll
-    for (uint32_t j = 0; j < kResolvePer; ++j) {
-      const uint32_t k = threadIdx.x + j * kResolveThreads;
-      tk[k] = a[j];
-      tv[k] = b[j];
+      for (uint32_t j = 0; j < kResolvePer; ++j) {
+        const uint32_t k = threadIdx.x + j * kResolveThreads;
+        tk[k] = a[j];
+        tv[k] = b[j];
+      }
     }
+    // the tile's bands: the one holding its first entry, and where the next
+    // begins (a tile shorter than a band meets at most one boundary)
+    const uint64_t band0 = t0 / n;
+    const uint64_t next0 = (band0 + 1) * n;
+    const bool one_cut = n >= kResolveTile;
     __syncthreads();
-#pragma unroll
+#pragma unroll 4
     for (uint32_t j = 0; j < kResolvePer; ++j) {
       const uint32_t k = threadIdx.x + j * kResolveThreads;
       if (k >= cnt) break;
       const uint64_t e = t0 + k;
-      const uint64_t band = narrow ? (uint64_t)((uint32_t)e / n) : e / n;
-      const uint64_t first = band * n;  // the band's first entry
-      const uint32_t sig = a[j], bkt = sig & low_mask;
+      const uint64_t first = one_cut ? (e < next0 ? next0 - n : next0) : e / n * n;
+      const uint32_t sig = tk[k], self = tv[k], bkt = sig & low_mask;
       // within the tile and the band, at most kResolveSteps entries back
       const uint64_t lo_tile = first > t0 ? first : t0;
       const uint32_t room = (uint32_t)(e - lo_tile);
       const uint32_t reach = room < kResolveSteps ? room : kResolveSteps;
-      uint32_t r = b[j];
+      uint32_t r = self;
       bool settled = false;
       for (uint32_t d = 1; d <= reach; ++d) {
         const uint32_t s = tk[k - d];
@@ -104,7 +109,7 @@ rep_resolve_kernel(const uint32_t *__restrict__ sk, const uint32_t *__restrict__
       }
       // back at the band's first entry without a match: no predecessor
       if (!settled && reach == room && lo_tile == first) settled = true;
-      if (settled) rep[first + b[j]] = r;
+      if (settled) rep[first + self] = r;
       else slow[atomicAdd(slow_count, 1u)] = e;
     }
     __syncthreads();

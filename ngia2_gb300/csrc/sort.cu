@@ -167,7 +167,8 @@ static uint32_t scan_chunks(uint32_t ntiles) {
 // and its values, when the pass has any, copied into shared memory by
 // cp.async while the keys are ranked:
 //   1. rank: per round of 32 keys, each lane sets its bit in a warp-private
-//      mask of its digit (a shared-memory atomic OR), reads the mask back --
+//      mask of its digit (a shared-memory atomic OR, one per run of equal
+//      digits in neighbouring lanes), reads the mask back --
 //      the lanes sharing its digit -- and takes its slot among them after the
 //      warp's running count of that digit, which the lowest of them advances;
 //      three mask buffers in rotation, so one warp barrier per round;
@@ -249,7 +250,19 @@ rs_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__
     const uint32_t d = (key[r] >> shift) & 255u;
     const uint32_t b = r % kMaskBufs;
     uint32_t *m = rs_smem + (b < 2 ? kSmKeys + b * kMaskWords : kSmSpare) + warp * 256;
-    if (valid) atomicOr(m + d, bit);
+    // a run of lanes with one digit (sorted input repeats keys) sets its bits
+    // with one atomic: same-address atomics of a warp serialise.  Valid lanes
+    // are a prefix of the warp.
+    const uint32_t dprev = __shfl_up_sync(kFull, d, 1);
+    const bool start = valid && (lane == 0 || dprev != d);
+    const uint32_t starts = __ballot_sync(kFull, start);
+    const uint32_t vmask = __ballot_sync(kFull, valid);
+    if (start) {
+      const uint32_t above = starts & ~((2u << lane) - 1u);  // later run starts
+      const uint32_t end = above ? (uint32_t)__ffs(above) - 1u : 32u;
+      const uint32_t upto = end == 32u ? kFull : (1u << end) - 1u;
+      atomicOr(m + d, upto & ~lt_mask & vmask);
+    }
     __syncwarp();
     const uint32_t peers = valid ? m[d] : 0u;
     const uint32_t leader = peers ? __ffs(peers) - 1u : lane;
