@@ -207,6 +207,9 @@ nibble_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ 
     }
     const uint32_t len = __ldg(packed + o);
     if (len != lens[i] || o + 1 + 4ull * ((len + 31) >> 5) > words) {
+      // flagged; an empty record in its place, so that a kernel reading the
+      // layout before the flag is seen stays inside the region
+      if (lane == 0) nib[o] = 0;
       mine |= kBadRecord;
       continue;
     }
@@ -305,13 +308,19 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
   bool wrong = false;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
+    // a record outside its piece or with the wrong length word is flagged and
+    // left empty in every layout (its offset lies in the region: the host
+    // checked it), so that the sketch, which reads these layouts before the
+    // flag is seen, stays inside the region
     if (o < w0 || o >= w1) {
+      if (lane == 0) nib[o] = dense_nib[o] = dplanes[o] = 0;
       wrong = true;
       continue;
     }
     const uint32_t len = __ldg(packed + o);
     const uint32_t blocks = (len + 31) >> 5;
     if (len != lens[i] || o + 1 + 4ull * blocks > w1) {
+      if (lane == 0) nib[o] = dense_nib[o] = dplanes[o] = 0;
       wrong = true;
       continue;
     }

@@ -36,7 +36,13 @@ DbView db_view(const ngia_ctx *c) {
                 c->lens.as<uint32_t>()};
 }
 
-int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_done) {
+void ctx_stage_stats(ngia_ctx *c, ngia_stats *st) {
+  st->ms_sketch = ev_ms(c->ev[8], c->ev[9]);
+  st->ms_bucket = ev_ms(c->ev[9], c->ev[10]);
+}
+
+int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_done,
+                      bool defer_stats) {
   if (c->n == 0) return NGIA_ERR_STATE;
   if (bands < 1 || bands > (uint32_t)kBands) return NGIA_ERR_ARG;
   cudaStream_t s = c->stream;
@@ -51,8 +57,8 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_d
     c->table_built = true;
     c->table_inv = c->ab.inv;
   }
-  if (!sketch_done) {  // (else ev[0], ev[1] bracket the pipelined load and sketch)
-    NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  if (!sketch_done) {  // (else ev[8], ev[9] bracket the pipelined load and sketch)
+    NGIA_CUDA(cudaEventRecord(c->ev[8], s));
     if (c->use_table && c->table_ok)
       NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
                                    c->offs.as<uint64_t>(), c->n, c->ab.inv, c->sketch_table.p,
@@ -61,17 +67,16 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_d
     else
       NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
                                      c->sigs.as<uint32_t>(), s));
-    NGIA_CUDA(cudaEventRecord(c->ev[1], s));
+    NGIA_CUDA(cudaEventRecord(c->ev[9], s));
   }
   NGIA_TRY(bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(),
                   c->sort_tmp.p, s));
-  NGIA_CUDA(cudaEventRecord(c->ev[2], s));
+  NGIA_CUDA(cudaEventRecord(c->ev[10], s));
   c->rep_bands = bands;
   c->sigs_valid = true;
-  if (st) {
-    NGIA_CUDA(cudaEventSynchronize(c->ev[2]));
-    st->ms_sketch = ev_ms(c->ev[0], c->ev[1]);
-    st->ms_bucket = ev_ms(c->ev[1], c->ev[2]);
+  if (st && !defer_stats) {
+    NGIA_CUDA(cudaEventSynchronize(c->ev[10]));
+    ctx_stage_stats(c, st);
   }
   return NGIA_OK;
 }
@@ -256,12 +261,17 @@ static int use_alphabet(ngia_ctx *c, const AlphaChoice &a, uint64_t words, uint3
 // copy); the device checks each record's length word as it lays it out.
 static bool records_inside(const uint64_t *h_offs, const uint32_t *h_lens, uint32_t n,
                            uint64_t words) {
-  bool bad = false;
+  // the longest read and the furthest record end, compared once (a max
+  // reduction the compiler vectorises; a record's end lies past its offset)
+  uint32_t max_len = 0;
+  uint64_t max_end = 0;
   for (uint32_t i = 0; i < n; ++i) {
-    const uint64_t end = h_offs[i] + 1 + 4ull * ((h_lens[i] + 31u) >> 5);
-    bad |= (h_lens[i] > NGIA_MAX_READ) | (end > words) | (h_offs[i] >= words);
+    const uint32_t len = h_lens[i];
+    const uint64_t end = h_offs[i] + 1 + 4ull * (((uint64_t)len + 31u) >> 5);
+    max_len = len > max_len ? len : max_len;
+    max_end = end > max_end ? end : max_end;
   }
-  return !bad;
+  return max_len <= NGIA_MAX_READ && max_end <= words;
 }
 
 int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64_t *h_offs,
@@ -362,21 +372,29 @@ int makedb_device(ngia_ctx *c, Makedb &m) {
 // signatures are computed while the next pieces are in flight.  The layouts
 // and the sketch need the database's code map, known only once every record
 // has been seen; the pipeline assumes the previous load's map (its sketch
-// tables are cached) and checks at the end that every residue's code is one of
-// the map's and every record lay inside its piece (offsets in order).  Runs
-// only when that map takes the table sketch.  *used = false: nothing usable
-// was done (the caller loads as usual); else the load is complete and
-// *sketched tells whether the signatures are in place.
+// tables are cached) and checks that every residue's code is one of the map's
+// and every record lay inside its piece (offsets in order); the check's
+// result lands in *c->h_flag (nonzero: the caller discards the step and loads
+// as usual) once the stream passes it.  Runs only when that map takes the
+// table sketch.  *used = false: nothing was done (the caller loads as usual);
+// else the load and the signatures are in place, subject to the check.
 int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
                     const uint64_t *h_offs, const uint32_t *h_lens, uint32_t n, bool *used,
                     bool *sketched) {
   *used = *sketched = false;
+  if (!c->h_flag) {  // pinned, so that the check's copy stays asynchronous
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return NGIA_OK;  // the plain load then
+    }
+    c->h_flag = static_cast<uint32_t *>(p);
+  }
   if (n < 4096 || !h_packed || !h_offs || !h_lens || !c->last_present || !c->use_table)
     return NGIA_OK;
   const AlphaChoice spec = choose_alphabet(c->last_present);
   if (!spec.dense || !spec.table_ok || !c->table_built || c->table_inv != spec.inv)
     return NGIA_OK;
-  if (!records_inside(h_offs, h_lens, n, words)) return NGIA_ERR_ARG;
   *used = true;
   cudaStream_t s = c->stream;
   NGIA_TRY(c->packed.reserve(words * 4));
@@ -414,16 +432,37 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
   }
   first[C] = n;
   uint32_t *packed = c->packed.as<uint32_t>();
+  // piece k's words: [bound(k), bound(k + 1)), inside the region whatever the
+  // offsets hold (they are checked below, while the copies run)
+  auto bound = [&](int k) -> uint64_t {
+    if (k <= 0) return 0;
+    if (k >= C) return words;
+    const uint64_t w = first[k] < n ? h_offs[first[k]] : words;
+    return w < words ? w : words;
+  };
   // the copies overwrite records that earlier work on the stream may still read
   NGIA_CUDA(cudaEventRecord(c->ev[5], s));
   NGIA_CUDA(cudaStreamWaitEvent(c->copy, c->ev[5], 0));
   for (int k = C - 1; k >= 0; --k) {
-    const uint64_t w0 = k == 0 ? 0 : (first[k] < n ? h_offs[first[k]] : words);
-    const uint64_t w1 = k + 1 == C ? words : (first[k + 1] < n ? h_offs[first[k + 1]] : words);
+    const uint64_t w0 = bound(k), w1 = bound(k + 1);
     if (w1 > w0)
       NGIA_CUDA(cudaMemcpyAsync(packed + w0, h_packed + w0, (w1 - w0) * 4,
                                 cudaMemcpyHostToDevice, c->copy));
     NGIA_CUDA(cudaEventRecord(c->chunk_ev[k], c->copy));
+  }
+  // the host check of every record, beside the copies: nothing reads a
+  // record on the device before it passes
+  if (!records_inside(h_offs, h_lens, n, words)) {
+    NGIA_CUDA(cudaStreamSynchronize(c->copy));  // the caller's buffers stay in use until then
+    NGIA_CUDA(cudaStreamSynchronize(s));
+    // the copies overwrote the resident records: no database until a load
+    c->n = 0;
+    c->packed_words = 0;
+    c->sigs_valid = false;
+    c->rep_bands = 0;
+    c->n_edges = 0;
+    *used = false;
+    return NGIA_ERR_ARG;
   }
   // each piece's layouts on their own stream right behind its copy, so they
   // can run while the main stream sketches the previous piece
@@ -432,8 +471,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
     const uint32_t r0 = first[k], cnt = first[k + 1] - first[k];
     NGIA_CUDA(cudaStreamWaitEvent(c->layout, c->chunk_ev[k], 0));
     if (cnt) {
-      const uint64_t w0 = k == 0 ? 0 : (first[k] < n ? h_offs[first[k]] : words);
-      const uint64_t w1 = k + 1 == C ? words : (first[k + 1] < n ? h_offs[first[k + 1]] : words);
+      const uint64_t w0 = bound(k), w1 = bound(k + 1);
       NGIA_TRY(launch_load_layouts(packed, offs + r0, c->lens.as<uint32_t>() + r0, cnt, w0, w1,
                                    spec.inv,
                                    c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
@@ -442,7 +480,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
     }
     NGIA_CUDA(cudaEventRecord(c->layout_ev[k], c->layout));
   }
-  NGIA_CUDA(cudaEventRecord(c->ev[0], s));
+  NGIA_CUDA(cudaEventRecord(c->ev[8], s));
   for (int k = C - 1; k >= 0; --k) {
     const uint32_t r0 = first[k], cnt = first[k + 1] - first[k];
     NGIA_CUDA(cudaStreamWaitEvent(s, c->layout_ev[k], 0));
@@ -453,15 +491,16 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
   }
   NGIA_CUDA(cudaEventRecord(c->ev[7], c->side));  // the short records' kernels
   NGIA_CUDA(cudaStreamWaitEvent(s, c->ev[7], 0));
-  NGIA_CUDA(cudaEventRecord(c->ev[1], s));
-  uint32_t bad = 0;  // a code outside the map, or a record outside its piece
-  NGIA_CUDA(cudaMemcpyAsync(&bad, c->presence.p, sizeof(bad), cudaMemcpyDeviceToHost, s));
-  NGIA_CUDA(cudaStreamSynchronize(s));
-  if (bad) {  // the plain load takes over from the start
-    *used = false;
-    return NGIA_OK;
-  }
-  // the codes present are among the map's: the same map serves them
+  NGIA_CUDA(cudaEventRecord(c->ev[9], s));
+  // a code outside the map, or a record outside its piece: copied to
+  // *h_flag and read by the caller after the step's next synchronisation,
+  // without a host round trip here.  Until then the step goes on as if the map serves (the
+  // layouts of such records hold in-range codes, so the work on them is
+  // wasted, never out of bounds); if the check fails, the caller starts over
+  // with the plain load.
+  *c->h_flag = 0;
+  NGIA_CUDA(cudaMemcpyAsync(c->h_flag, c->presence.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            s));
   *sketched = true;
   NGIA_TRY(use_alphabet(c, spec, words, n, false));
   c->n = n;
@@ -514,7 +553,7 @@ int ngia_ctx_create(ngia_ctx **out, void *stream) {
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     c->own_stream = (e == cudaSuccess);
   }
-  for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+  for (int k = 0; k < ngia_ctx::kEvents && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->layout, cudaStreamNonBlocking);
@@ -546,8 +585,10 @@ void ngia_ctx_destroy(ngia_ctx *c) {
                           &c->edges,    &c->scan_tmp, &c->jobs, &c->sketch_table};
   for (ngia::DevBuf *b : bufs) b->release();
   c->round.destroy();  // shares c->stream, which it leaves alone
-  for (int k = 0; k < 8; ++k)
+  for (int k = 0; k < ngia_ctx::kEvents; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  if (c->h_flag) cudaFreeHost(c->h_flag);
+  c->h_flag = nullptr;
   if (c->side) cudaStreamDestroy(c->side);
   if (c->copy) cudaStreamDestroy(c->copy);
   if (c->layout) cudaStreamDestroy(c->layout);
@@ -608,8 +649,12 @@ int ngia_ctx_group_align(ngia_ctx *c, uint32_t identity, uint32_t bands,
                          uint64_t *h_n_edges, ngia_stats *stats) {
   if (!c) return NGIA_ERR_ARG;
   if (stats) std::memset(stats, 0, sizeof(*stats));
-  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats));
-  return ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats);
+  // the stage timings are read after the graph build's synchronisation, so
+  // that no host round trip sits between the bucketing and the candidates
+  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats, false, true));
+  NGIA_TRY(ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats));
+  if (stats) ngia::ctx_stage_stats(c, stats);
+  return NGIA_OK;
 }
 
 int ngia_ctx_test_lookback_timeout(ngia_ctx *c, uint32_t identity, uint32_t bands,
@@ -814,10 +859,22 @@ int ngia_ctx_run_host(ngia_ctx *c, const uint32_t *h_packed, uint64_t packed_wor
   if (bands >= 1 && bands <= (uint32_t)ngia::kBands)
     NGIA_TRY(ngia::ctx_load_sketch(c, h_packed, packed_words, h_rec_offsets, h_lens, n, &piped,
                                    &sketched));
-  if (!piped)
-    NGIA_TRY(ngia::ctx_load(c, h_packed, packed_words, h_rec_offsets, h_lens, n, nullptr, bands));
-  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats, sketched));
-  if (stats) stats->load_pipelined = sketched ? 1u : 0u;
+  if (piped) {
+    // no synchronisation until the graph build needs its pair count; the
+    // pipelined load's check is read after the build
+    NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats, true, true));
+    NGIA_TRY(ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats));
+    if (*c->h_flag == 0) {  // the map served every record: the step stands
+      if (stats) {
+        ngia::ctx_stage_stats(c, stats);
+        stats->load_pipelined = 1u;
+      }
+      return ngia_ctx_edges(c, h_edges, cap);
+    }
+    if (stats) std::memset(stats, 0, sizeof(*stats));  // start over: the plain load
+  }
+  NGIA_TRY(ngia::ctx_load(c, h_packed, packed_words, h_rec_offsets, h_lens, n, nullptr, bands));
+  NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats, false));
   NGIA_TRY(ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats));
   return ngia_ctx_edges(c, h_edges, cap);
 }

@@ -7,7 +7,11 @@
 struct ngia_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  cudaEvent_t ev[8] = {};  // 0-3 stage timing, 5 copy ordering, 6-7 fork/join of `side`
+  // 0-3 graph-build stage timing, 5 copy ordering, 6-7 fork/join of `side`,
+  // 8-10 sketch and bucket timing
+  static constexpr int kEvents = 11;
+  cudaEvent_t ev[kEvents] = {};
+  uint32_t *h_flag = nullptr;  // pinned: a pipelined load's check, read after the step
   cudaStream_t side = nullptr;  // work that runs beside the main stream's (sketch)
   // pipelined loads (ngia_ctx_run_host): chunks of the records copied on `copy`
   // while the previous chunks are sketched on `stream`
@@ -46,7 +50,12 @@ struct ngia_ctx {
 namespace ngia {
 DbView db_view(const ngia_ctx *c);
 // sketch_done: the signatures are already in place (a pipelined load).
-int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_done = false);
+// defer_stats: no wait for the stage timings; a later synchronisation makes
+// them readable (ctx_stage_stats).
+int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_done = false,
+                      bool defer_stats = false);
+// ms_sketch and ms_bucket of the last ctx_sketch_bucket, once its work is done.
+void ctx_stage_stats(ngia_ctx *c, ngia_stats *st);
 int ctx_fast_cluster(ngia_ctx *c, uint32_t identity, uint32_t bands, uint32_t *h_cluster,
                      ngia_stats *st);
 // Load from residue text (makedb): record i's h_lens[i] residues start at byte

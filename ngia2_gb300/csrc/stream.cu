@@ -217,7 +217,6 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
     if (h_lens[i] > NGIA_MAX_READ || h_offs[i] + w > words) return NGIA_ERR_ARG;
     if (i > 0 && h_offs[i] < h_offs[i - 1] + 1 + 4ull * ((h_lens[i - 1] + 31) / 32))
       return NGIA_ERR_ARG;  // records in index order, not overlapping
-    if (h_packed[h_offs[i]] != h_lens[i]) return NGIA_ERR_FORMAT;
     if (chunks.empty() || h_offs[i] + w - chunks.back().word_first > chunk_words) {
       if (w > chunk_words) return NGIA_ERR_ARG;  // a record larger than a chunk
       chunks.push_back(Chunk{i, 0, h_offs[i], 0});

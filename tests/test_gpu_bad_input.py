@@ -4,7 +4,9 @@ candidate collection's bounded wait gives up with an error the host reads:
     packed region -> NGIA_ERR_ARG from the host check, before any copy or
     launch (ngia_ctx_load, ngia_ctx_run_host, ngia_stream_graph);
   * a record whose length word is not its read length -> NGIA_ERR_FORMAT
-    from the first layout kernel, which skips such records;
+    from the first layout kernel, which lays such records out empty (the
+    pieced upload of ngia_ctx_run_host and the streamed build sketch before
+    they read the flag);
   * the look-back of the one-pass candidate collection with a predecessor
     that never publishes -> NGIA_ERR_CUDA after a short poll limit.
 After each, the same context loads the good database and builds the same
@@ -101,3 +103,54 @@ def test_lookback_wait_gives_up_and_context_stays_usable(cuda, prot):
         assert rc == ng.ERR_CUDA
         e, _ = ctx.graph(50)
     assert np.array_equal(e, want)
+
+
+@pytest.fixture(scope="module")
+def dna5k(tmp_path_factory, cuda):
+    """5,000 DNA sequences: enough records for run_host's pieced upload, which
+    takes over once a load has fixed the four-code map."""
+    from ngia2_gb300 import synth
+    d = tmp_path_factory.mktemp("dna5k")
+    synth.dna_families(5_000, 500, 5).write_fasta(d / "in.fa")
+    ng.makedb(d / "in.fa", d / "db.packed")
+    return ng.read_packed(d / "db.packed")
+
+
+def run_host(ctx, db, packed=None, identity=95):
+    packed = db["packed"] if packed is None else packed
+    edges = np.zeros(len(db["lens"]) * 64, ng.EDGE_DTYPE)
+    m, st = ctx.run_host(np.ascontiguousarray(packed, np.uint32),
+                         np.ascontiguousarray(db["offsets"], np.uint64),
+                         np.ascontiguousarray(db["lens"], np.uint32), identity, 64, edges)
+    return edges[:m].copy(), st
+
+
+def test_pieced_upload_refuses_a_wrong_length_word(dna5k):
+    """The pieced upload lays out and sketches before it reads its check: a
+    record whose length word is not its read length is laid out empty, the
+    step is discarded, and the plain load refuses it; the context then builds
+    the same graph from the good database, through the pieced upload again."""
+    with ng.Context() as ctx:
+        want, st0 = run_host(ctx, dna5k)
+        bad = dna5k["packed"].copy()
+        i = len(dna5k["lens"]) - 3  # a short record: in the first piece uploaded
+        bad[int(dna5k["offsets"][i])] = int(dna5k["lens"][i]) + 5000
+        with pytest.raises(ng.NgiaError) as err:
+            run_host(ctx, dna5k, bad)
+        assert err.value.status == ng.ERR_FORMAT
+        got, st = run_host(ctx, dna5k)
+        assert st["load_pipelined"] == 1
+    assert np.array_equal(got, want)
+
+
+def test_streaming_refuses_a_wrong_length_word(dna5k):
+    packed = np.ascontiguousarray(dna5k["packed"], np.uint32).copy()
+    offs = np.ascontiguousarray(dna5k["offsets"], np.uint64)
+    lens = np.ascontiguousarray(dna5k["lens"], np.uint32)
+    packed[int(offs[100])] = int(lens[100]) + 7
+    edges = np.zeros(16, ng.EDGE_DTYPE)
+    m = C.c_uint64()
+    rc = ng.lib().ngia_stream_graph(packed.ctypes.data, packed.size, offs.ctypes.data,
+                                    lens.ctypes.data, lens.size, 90, 3, 1 << 20,
+                                    edges.ctypes.data, len(edges), C.byref(m), None)
+    assert rc == ng.ERR_FORMAT
