@@ -20,9 +20,11 @@ e2e     the same through ngia_ctx_run_host on pinned host buffers: H2D of the
         the reference code built as a host OpenMP program) on a bounded
         sample of the workload with all host cores.
 pairs   (one GPU) aligned cells/s of the batched aligner against the plain
-        one-thread-per-pair form launched once per group, on 2,000,000
-        heavy-tailed protein candidate pairs at identity 90, scores compared
-        bit for bit (--pairs N to resize, 0 to skip; --pairs-only).
+        one-thread-per-pair form launched once per group, and against the
+        reference's own kernel (BuildGraph::kernel_dynamic, built unmodified)
+        launched the same way, on 2,000,000 heavy-tailed protein candidate
+        pairs at identity 90, scores compared bit for bit (--pairs N to
+        resize, 0 to skip; --pairs-only; --no-plain skips both baselines).
 serving (one GPU) queries/s and p50/p99 request latency of the serving engine
         (a resident 2,000,000-protein database, Poisson-arriving requests of
         1-50,000 queries at identity 90, 8 slots) against the same requests
@@ -835,6 +837,36 @@ def make_pairs(n_pairs: int, workdir: Path):
     return db, pairs
 
 
+def run_reference_kernel(db, pairs, workdir: Path, want) -> dict:
+    """The reference's own alignment kernel (BuildGraph::kernel_dynamic, built
+    unmodified by oracle/build.sh) on the same pairs, one launch per group of
+    1/PAIRS_GROUPS of them with a synchronisation after each, as the reference
+    launches one kernel per band; kernel time from CUDA events in the
+    harness, scores compared with the batched round's."""
+    import numpy as np
+
+    import oracle
+    exe = oracle.ref_gpu_align()
+    if not exe.exists():
+        return {"ms": None, "error": "reference GPU build missing (oracle/build.sh)"}
+    jobs = np.zeros((len(pairs), 3), np.uint32)
+    jobs[:, :2] = pairs
+    files = {k: workdir / f"ref_{k}.bin" for k in ("packed", "offs", "jobs", "out")}
+    np.ascontiguousarray(db["packed"], np.uint32).tofile(files["packed"])
+    np.ascontiguousarray(db["offsets"], np.uint64).tofile(files["offs"])
+    jobs.tofile(files["jobs"])
+    r = subprocess.run([str(exe), str(files["packed"]), str(files["offs"]), str(files["jobs"]),
+                        str(PAIRS_IDENTITY), str(files["out"]), str(PAIRS_GROUPS)],
+                       capture_output=True, text=True, timeout=1200)
+    if r.returncode != 0:
+        return {"ms": None, "error": (r.stdout + r.stderr)[-300:]}
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    scores = np.fromfile(files["out"], np.uint32).reshape(-1, 3)[:, 2]
+    return {"kernel": "BuildGraph::kernel_dynamic (src/buildGraph.hpp:192-253), built "
+                      "unmodified, one thread per pair", "ms": out["kernel_ms"],
+            "launches": out["groups"], "scores_identical": bool(np.array_equal(scores, want))}
+
+
 def run_pairs(args) -> dict:
     """Aligned cells/s of the batched aligner (width classes, persistent
     per-class launches) against the plain form (one thread per pair in job
@@ -912,6 +944,7 @@ def run_pairs(args) -> dict:
     torch.cuda.synchronize()
     got = d_scores.cpu().numpy().view(np.uint32)
     ref = d_jobs.cpu().numpy().view(np.uint32).reshape(-1, 3)[:, 2]
+    ref_kernel = None if args.no_plain else run_reference_kernel(db, pairs, workdir, got)
     cells = st["aligned_cells"]
     ms_b = statistics.mean(tb)
     ms_p = statistics.mean(tp) if tp else None
@@ -926,12 +959,16 @@ def run_pairs(args) -> dict:
         "metric": "aligned cells/s", "unit": "cells/s",
         "band_cells": cells, "computed_cells": st["computed_cells"],
         "batched": {"value": cells / (ms_b * 1e-3), "ms": ms_b, "steps": steps,
+                    "computed_cells_per_s": st["computed_cells"] / (ms_b * 1e-3),
                     "cuda_graph": True, "plan": plan, "autotune_s": tune_s,
                     "autotune_sample_pairs": sample,
                     "ms_default_plan": t_default, "default_plan": default_plan},
         "plain": {"value": cells / (ms_p * 1e-3) if ms_p else None, "ms": ms_p,
                   "launches": groups, "steps": len(tp)},
         "batched_over_plain": ms_p / ms_b if ms_p else None,
+        "reference_kernel": ref_kernel,
+        "batched_over_reference_kernel": (ref_kernel["ms"] / ms_b
+                                          if ref_kernel and ref_kernel.get("ms") else None),
         "roofline": {"bound": "int32_alu", "kernel": "batched round (all width classes)",
                      "achieved": ops / (ms_b * 1e-3) / 1e12, "peak": int_peak / 1e12,
                      "unit": "Tops/s (32-bit lane ops)",

@@ -405,8 +405,9 @@ int ngia_ctx_rep_rows(ngia_ctx *ctx, uint32_t *h_rep, uint32_t bands);
  * stats->load_pipelined tells which).  Pinned host buffers give the upload
  * the link's full bandwidth.  Records outside the region (see ngia_ctx_load)
  * are refused with NGIA_ERR_ARG; the pieced upload checks them on the host
- * while its first copies run, so after that refusal the context holds no
- * database until the next load.  Synchronises. */
+ * while the device already copies, lays out, sketches and buckets (kernels
+ * that bound every record by the region), so after that refusal the context
+ * holds no database until the next load.  Synchronises. */
 int ngia_ctx_run_host(ngia_ctx *ctx, const uint32_t *h_packed,
                       uint64_t packed_words, const uint64_t *h_rec_offsets,
                       const uint32_t *h_lens, uint32_t n, uint32_t identity,

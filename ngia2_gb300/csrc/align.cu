@@ -300,7 +300,7 @@ int launch_nibbles(const uint32_t *packed, const uint64_t *offs, const uint32_t 
 __global__ void __launch_bounds__(256)
 load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
                     const uint32_t *__restrict__ lens, uint32_t n, uint64_t w0, uint64_t w1,
-                    uint32_t codes, uint32_t ncodes,
+                    uint64_t words, uint32_t codes, uint32_t ncodes,
                     uint32_t *__restrict__ nib, uint32_t *__restrict__ dense_nib,
                     uint32_t *__restrict__ dplanes, uint32_t *__restrict__ bad) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -308,12 +308,11 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
   bool wrong = false;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
-    // a record outside its piece or with the wrong length word is flagged and
-    // left empty in every layout (its offset lies in the region: the host
-    // checked it), so that the sketch, which reads these layouts before the
-    // flag is seen, stays inside the region
+    // a record outside its piece or with the wrong length word is flagged and,
+    // when its offset lies in the region, left empty in every layout (the
+    // sketch also bounds every record it reads by the region)
     if (o < w0 || o >= w1) {
-      if (lane == 0) nib[o] = dense_nib[o] = dplanes[o] = 0;
+      if (lane == 0 && o < words) nib[o] = dense_nib[o] = dplanes[o] = 0;
       wrong = true;
       continue;
     }
@@ -372,8 +371,10 @@ static int map_bits(uint64_t map, uint32_t (&bits)[3]) {
 }
 
 int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint32_t *lens,
-                        uint32_t n, uint64_t w0, uint64_t w1, uint64_t inv, uint32_t *nib,
-                        uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad, cudaStream_t s) {
+                        uint32_t n, uint64_t w0, uint64_t w1, uint64_t words, uint64_t inv,
+                        uint32_t *nib, uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad,
+                        cudaStream_t s) {
+  if (w0 > w1 || w1 > words) return NGIA_ERR_ARG;
   if (n == 0) return NGIA_OK;
   uint32_t codes = 0, ncodes = 0;  // inv nibble d = residue code of aligner code d
   for (uint32_t d = 1; d < 8; ++d) {
@@ -386,7 +387,7 @@ int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
   load_layouts_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
-      packed, offs, lens, n, w0, w1, codes, ncodes, nib, dense_nib, dplanes, bad);
+      packed, offs, lens, n, w0, w1, words, codes, ncodes, nib, dense_nib, dplanes, bad);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

@@ -61,7 +61,8 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_d
     NGIA_CUDA(cudaEventRecord(c->ev[8], s));
     if (c->use_table && c->table_ok)
       NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
-                                   c->offs.as<uint64_t>(), c->n, c->ab.inv, c->sketch_table.p,
+                                   c->offs.as<uint64_t>(), c->n, c->packed_words, c->ab.inv,
+                                   c->sketch_table.p,
                                    c->sigs.as<uint32_t>(), c->n, s, c->side, c->ev[6],
                                    c->ev[7]));
     else
@@ -259,8 +260,8 @@ static int use_alphabet(ngia_ctx *c, const AlphaChoice &a, uint64_t words, uint3
 // Every record inside the region by its offset and read length, and no read
 // longer than the format allows (one pass over the two arrays, before any
 // copy); the device checks each record's length word as it lays it out.
-static bool records_inside(const uint64_t *h_offs, const uint32_t *h_lens, uint32_t n,
-                           uint64_t words) {
+bool records_inside(const uint64_t *h_offs, const uint32_t *h_lens, uint32_t n,
+                    uint64_t words) {
   // the longest read and the furthest record end, compared once (a max
   // reduction the compiler vectorises; a record's end lies past its offset)
   uint32_t max_len = 0;
@@ -433,7 +434,10 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
   first[C] = n;
   uint32_t *packed = c->packed.as<uint32_t>();
   // piece k's words: [bound(k), bound(k + 1)), inside the region whatever the
-  // offsets hold (they are checked below, while the copies run)
+  // offsets hold.  Nothing launched here trusts the offsets: the layout
+  // kernel checks every record against its piece and the sketch bounds every
+  // record by the region; the caller checks them on the host while this runs
+  // (ngia_ctx_run_host) and before anything that trusts them is launched.
   auto bound = [&](int k) -> uint64_t {
     if (k <= 0) return 0;
     if (k >= C) return words;
@@ -450,20 +454,6 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
                                 cudaMemcpyHostToDevice, c->copy));
     NGIA_CUDA(cudaEventRecord(c->chunk_ev[k], c->copy));
   }
-  // the host check of every record, beside the copies: nothing reads a
-  // record on the device before it passes
-  if (!records_inside(h_offs, h_lens, n, words)) {
-    NGIA_CUDA(cudaStreamSynchronize(c->copy));  // the caller's buffers stay in use until then
-    NGIA_CUDA(cudaStreamSynchronize(s));
-    // the copies overwrote the resident records: no database until a load
-    c->n = 0;
-    c->packed_words = 0;
-    c->sigs_valid = false;
-    c->rep_bands = 0;
-    c->n_edges = 0;
-    *used = false;
-    return NGIA_ERR_ARG;
-  }
   // each piece's layouts on their own stream right behind its copy, so they
   // can run while the main stream sketches the previous piece
   const uint64_t *offs = c->offs.as<uint64_t>();
@@ -473,7 +463,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
     if (cnt) {
       const uint64_t w0 = bound(k), w1 = bound(k + 1);
       NGIA_TRY(launch_load_layouts(packed, offs + r0, c->lens.as<uint32_t>() + r0, cnt, w0, w1,
-                                   spec.inv,
+                                   words, spec.inv,
                                    c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
                                    c->dplanes.as<uint32_t>(), c->presence.as<uint32_t>(),
                                    c->layout));
@@ -486,8 +476,8 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
     NGIA_CUDA(cudaStreamWaitEvent(s, c->layout_ev[k], 0));
     if (cnt == 0) continue;
     NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(), offs + r0,
-                                 cnt, spec.inv, c->sketch_table.p, c->sigs.as<uint32_t>() + r0,
-                                 n, s, c->side, c->ev[6], nullptr));
+                                 cnt, words, spec.inv, c->sketch_table.p,
+                                 c->sigs.as<uint32_t>() + r0, n, s, c->side, c->ev[6], nullptr));
   }
   NGIA_CUDA(cudaEventRecord(c->ev[7], c->side));  // the short records' kernels
   NGIA_CUDA(cudaStreamWaitEvent(s, c->ev[7], 0));
@@ -861,8 +851,22 @@ int ngia_ctx_run_host(ngia_ctx *c, const uint32_t *h_packed, uint64_t packed_wor
                                    &sketched));
   if (piped) {
     // no synchronisation until the graph build needs its pair count; the
-    // pipelined load's check is read after the build
+    // pieced load's code-map check is read after the build
     NGIA_TRY(ngia::ctx_sketch_bucket(c, bands, stats, true, true));
+    // the host check of every record, while the device sketches and buckets
+    // (nothing launched so far trusts the offsets; the candidates do)
+    if (!ngia::records_inside(h_rec_offsets, h_lens, n, packed_words)) {
+      cudaStreamSynchronize(c->copy);  // the caller's buffers stay in use until then
+      cudaStreamSynchronize(c->layout);
+      cudaStreamSynchronize(c->side);
+      NGIA_CUDA(cudaStreamSynchronize(c->stream));
+      c->n = 0;  // the copies overwrote the resident records: no database until a load
+      c->packed_words = 0;
+      c->sigs_valid = false;
+      c->rep_bands = 0;
+      c->n_edges = 0;
+      return NGIA_ERR_ARG;
+    }
     NGIA_TRY(ngia::ctx_build_graph(c, identity, bands, h_n_edges, stats));
     if (*c->h_flag == 0) {  // the map served every record: the step stands
       if (stats) {

@@ -22,11 +22,13 @@ int build_sketch_table(uint64_t inv, void *table, cudaStream_t s);
 // Records offs[0..n) (a run of a database's records), signatures at
 // sigs[band * stride + i].  The short records' kernel runs on `side` (forked
 // from s through `fork`, joined back through `join`; join = null: the caller
-// joins later) beside the rank walk on s.
+// joins later) beside the rank walk on s.  A record whose offset or length
+// word puts it past `words` (the layouts' size) is skipped, so the kernels
+// stay inside the layouts whatever the offsets hold.
 int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
-                        uint32_t n, uint64_t inv, const void *table, uint32_t *sigs,
-                        uint32_t stride, cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
-                        cudaEvent_t join);
+                        uint32_t n, uint64_t words, uint64_t inv, const void *table,
+                        uint32_t *sigs, uint32_t stride, cudaStream_t s, cudaStream_t side,
+                        cudaEvent_t fork, cudaEvent_t join);
 
 // sort.cu
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs);
@@ -75,8 +77,9 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
 // the map or a record is not inside words [w0, w1) (such a record is skipped).
 // (A record whose length word is not lens[i] sets *bad too.)
 int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint32_t *lens,
-                        uint32_t n, uint64_t w0, uint64_t w1, uint64_t inv, uint32_t *nib,
-                        uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad, cudaStream_t s);
+                        uint32_t n, uint64_t w0, uint64_t w1, uint64_t words, uint64_t inv,
+                        uint32_t *nib, uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad,
+                        cudaStream_t s);
 // presence |= the codes seen (cleared first unless accumulate); a record
 // outside the region's `words`, or whose length word is not lens[i], is
 // skipped and sets kBadRecord.

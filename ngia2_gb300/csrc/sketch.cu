@@ -259,7 +259,7 @@ __device__ __forceinline__ void for_each_index(const uint32_t *w, uint32_t pb, u
 // Records with at least kRankMinSpan signed positions: the rank walk.
 __global__ void __launch_bounds__(kRankWarps * 32)
 sketch_rank_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restrict__ offs,
-                   uint32_t n, uint64_t inv, const uint16_t *__restrict__ ranks,
+                   uint32_t n, uint64_t words, uint64_t inv, const uint16_t *__restrict__ ranks,
                    uint32_t *__restrict__ sigs, uint32_t stride) {
   __shared__ __align__(16) uint32_t bitsets[kRankWarps * kBitsetWords];
   const uint32_t lane = threadIdx.x & 31u;
@@ -271,8 +271,10 @@ sketch_rank_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restric
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
+    if (o >= words) continue;  // outside the layouts (flagged by their kernel)
     const uint32_t len = __ldg(dense + o);
     if (len < 7 + kRankMinSpan) continue;  // short: the row table kernel's
+    if (o + 1 + 4ull * ((len + 31u) >> 5) > words) continue;
     // mark the 8-mers: lane l takes code words l, l + 32, ... (coalesced), the
     // entry rolling over the word's 8 positions from the previous word's last
     const uint32_t *w = dense + o + 1;
@@ -336,15 +338,17 @@ sketch_rank_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restric
 // directly); dense: the same records in aligner codes 1..4.
 __global__ void __launch_bounds__(256)
 sketch_table_kernel(const uint32_t *__restrict__ nib, const uint32_t *__restrict__ dense,
-                    const uint64_t *__restrict__ offs, uint32_t n,
+                    const uint64_t *__restrict__ offs, uint32_t n, uint64_t words,
                     const uint4 *__restrict__ table, uint32_t *__restrict__ sigs,
                     uint32_t stride) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
+    if (o >= words) continue;  // outside the layouts (flagged by their kernel)
     const uint32_t len = __ldg(nib + o);
     if (len >= 7 + kRankMinSpan) continue;  // the rank walk's
+    if (o + 1 + 4ull * ((len + 31u) >> 5) > words) continue;
     uint32_t mn[kBands];
 #pragma unroll
     for (int k = 0; k < kBands; ++k) mn[k] = kFull;
@@ -437,9 +441,9 @@ static int rank_blocks_per_sm() {
 }
 
 int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
-                        uint32_t n, uint64_t inv, const void *table, uint32_t *sigs,
-                        uint32_t stride, cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
-                        cudaEvent_t join) {
+                        uint32_t n, uint64_t words, uint64_t inv, const void *table,
+                        uint32_t *sigs, uint32_t stride, cudaStream_t s, cudaStream_t side,
+                        cudaEvent_t fork, cudaEvent_t join) {
   if (n == 0) return NGIA_OK;
   int dev = 0, sms = 0;
   NGIA_CUDA(cudaGetDevice(&dev));
@@ -452,13 +456,13 @@ int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64
   NGIA_CUDA(cudaStreamWaitEvent(side, fork, 0));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms;
   sketch_table_kernel<<<want < cap ? want : cap, 256, 0, side>>>(
-      nib, dense, offs, n, reinterpret_cast<const uint4 *>(base), sigs, stride);
+      nib, dense, offs, n, words, reinterpret_cast<const uint4 *>(base), sigs, stride);
   NGIA_LAUNCHED();
   const uint32_t rank_want = ceil_div(n, kRankWarps);
   const uint32_t rank_cap = (uint32_t)(sms * rank_blocks_per_sm());
   sketch_rank_kernel<<<rank_want < rank_cap ? rank_want : rank_cap, kRankWarps * 32, 0, s>>>(
-      dense, offs, n, inv, reinterpret_cast<const uint16_t *>(base + kRowTableBytes), sigs,
-      stride);
+      dense, offs, n, words, inv, reinterpret_cast<const uint16_t *>(base + kRowTableBytes),
+      sigs, stride);
   NGIA_LAUNCHED();
   if (join) {
     NGIA_CUDA(cudaEventRecord(join, side));

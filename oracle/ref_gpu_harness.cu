@@ -6,11 +6,15 @@
  * on the same GPU, pair by pair.  Original work; it includes the reference
  * header, it does not reproduce it.
  *
- * usage: ref_gpu_align <packed.u32> <offsets.u64> <jobs.u32> <identity> <out.u32>
+ * usage: ref_gpu_align <packed.u32> <offsets.u64> <jobs.u32> <identity> <out.u32> [groups]
  *   packed.u32  : the packed-record region as little-endian u32 words
  *   offsets.u64 : word offset of each record in that region
  *   jobs.u32    : (rep, tar, 0) u32 triples
  *   out.u32     : the jobs array after the kernel (scores in every third word)
+ *   groups      : launches, one per consecutive group of count / groups jobs
+ *                 with a device synchronisation after each, as the reference
+ *                 launches one kernel per band (default 1)
+ * Prints {"count": N, "groups": G, "kernel_ms": T}: T spans every launch.
  */
 #include <cstdio>
 #include <cstdlib>
@@ -33,10 +37,12 @@ static std::vector<char> slurp(const char *path) {
 }
 
 int main(int argc, char **argv) {
-  if (argc != 6) {
-    std::fprintf(stderr, "usage: %s packed offsets jobs identity out\n", argv[0]);
+  if (argc != 6 && argc != 7) {
+    std::fprintf(stderr, "usage: %s packed offsets jobs identity out [groups]\n", argv[0]);
     return 2;
   }
+  const int groups_arg = argc == 7 ? std::atoi(argv[6]) : 1;
+  const uint32_t groups = groups_arg > 0 ? (uint32_t)groups_arg : 1u;
   std::vector<char> packed = slurp(argv[1]), offs = slurp(argv[2]),
                     jobs = slurp(argv[3]);
   const unsigned identity = (unsigned)std::atoi(argv[4]);
@@ -55,11 +61,17 @@ int main(int argc, char **argv) {
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   cudaEventRecord(a);
-  if (count)
-    BuildGraph::kernel_dynamic<<<(count + 63) / 64, 64>>>(d_reads, d_offs, d_jobs,
-                                                          count, threshold);
+  cudaError_t err = cudaSuccess;
+  for (uint32_t g = 0; g < groups && err == cudaSuccess; ++g) {
+    const uint32_t lo = (uint32_t)((uint64_t)count * g / groups);
+    const uint32_t hi = (uint32_t)((uint64_t)count * (g + 1) / groups);
+    if (hi > lo)
+      BuildGraph::kernel_dynamic<<<(hi - lo + 63) / 64, 64>>>(d_reads, d_offs, d_jobs + 3ull * lo,
+                                                              hi - lo, threshold);
+    err = cudaDeviceSynchronize();
+  }
   cudaEventRecord(b);
-  cudaError_t err = cudaDeviceSynchronize();
+  if (err == cudaSuccess) err = cudaDeviceSynchronize();
   if (err == cudaSuccess) err = cudaGetLastError();
   if (err != cudaSuccess) {
     std::fprintf(stderr, "kernel failed: %s\n", cudaGetErrorString(err));
@@ -72,7 +84,7 @@ int main(int argc, char **argv) {
   if (!f) return 6;
   if (count) std::fwrite(jobs.data(), 1, jobs.size(), f);
   std::fclose(f);
-  std::printf("{\"count\": %u, \"kernel_ms\": %.6f}\n", count, ms);
+  std::printf("{\"count\": %u, \"groups\": %u, \"kernel_ms\": %.6f}\n", count, groups, ms);
   cudaFree(d_reads);
   cudaFree(d_offs);
   cudaFree(d_jobs);

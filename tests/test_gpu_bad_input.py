@@ -154,3 +154,23 @@ def test_streaming_refuses_a_wrong_length_word(dna5k):
                                     lens.ctypes.data, lens.size, 90, 3, 1 << 20,
                                     edges.ctypes.data, len(edges), C.byref(m), None)
     assert rc == ng.ERR_FORMAT
+
+
+def test_pieced_upload_refuses_records_outside(dna5k):
+    """The pieced upload checks the records on the host while the device
+    already sketches them (kernels bounded by the region): an offset past the
+    region, or a length beyond the format, is refused after the fact, and the
+    context builds the same graph once the good database is loaded again."""
+    with ng.Context() as ctx:
+        want, _ = run_host(ctx, dna5k)
+        offs = dna5k["offsets"].astype(np.uint64).copy()
+        offs[7] = dna5k["packed"].size  # past the end
+        lens = dna5k["lens"].copy()
+        lens[3] = 0x10000  # longer than the format allows
+        for bad in (dict(dna5k, offsets=offs), dict(dna5k, lens=lens)):
+            with pytest.raises(ng.NgiaError) as err:
+                run_host(ctx, bad)
+            assert err.value.status == ng.ERR_ARG
+            got, st = run_host(ctx, dna5k)
+            assert st["load_pipelined"] == 1
+            assert np.array_equal(got, want)
