@@ -163,30 +163,47 @@ collect_scan_kernel(const uint32_t *__restrict__ rep, const uint32_t *__restrict
     }
     toff[lane] = x - v;
     const uint32_t agg = __shfl_sync(kFull, x, 31);
-    if (lane == 0) {
-      unsigned long long excl = 0;
-      uint32_t ok = 1;
-      if (blk == 0) {
-        atomicExch(status, kStIncl | agg);
-      } else {
-        atomicExch(status + blk, kStAgg | agg);
-        uint32_t spins = 0;
-        for (int j = (int)blk - 1; j >= 0;) {
-          const unsigned long long s = *(volatile unsigned long long *)(status + j);
-          if ((s >> 62) == 0) {
+    unsigned long long excl = 0;
+    uint32_t ok = 1;
+    if (blk == 0) {
+      if (lane == 0) atomicExch(status, kStIncl | agg);
+    } else {
+      if (lane == 0) atomicExch(status + blk, kStAgg | agg);
+      // warp-wide look-back: lane l reads the status of block j - l (lane 0
+      // the nearest), 32 predecessors a round, until one holds an inclusive
+      // prefix (before block 0: an inclusive 0)
+      for (int64_t j = (int64_t)blk - 1; ok;) {
+        const int64_t q = j - (int64_t)lane;
+        unsigned long long s = kStIncl;
+        if (q >= 0) {
+          uint32_t spins = 0;
+          for (;;) {
+            s = *(volatile unsigned long long *)(status + q);
+            if ((s >> 62) != 0) break;
             if (++spins > spin_limit) {  // a predecessor never published
-              atomicOr(error, 1u);
-              ok = 0;
+              s = 0;
               break;
             }
-            continue;
           }
-          excl += s & kStValue;
-          if ((s >> 62) == 2) break;
-          --j;
         }
-        if (ok) atomicExch(status + blk, kStIncl | (excl + agg));
+        if (__any_sync(kFull, s == 0)) {
+          if (lane == 0) atomicOr(error, 1u);
+          ok = 0;
+          break;
+        }
+        const uint32_t incl = __ballot_sync(kFull, (s >> 62) == 2);
+        // lanes up to the nearest inclusive one (all 32 when there is none)
+        const uint32_t upto = incl ? (uint32_t)__ffs(incl) - 1u : 31u;
+        unsigned long long val = lane <= upto ? (s & kStValue) : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(kFull, val, o);
+        excl += val;
+        if (incl) break;
+        j -= 32;
       }
+      if (ok && lane == 0) atomicExch(status + blk, kStIncl | (excl + agg));
+    }
+    if (lane == 0) {
       if (ok && blk + 1 == nblocks) *unique_total = excl + agg;
       excl_sh = excl;
       ok_sh = ok;
