@@ -290,19 +290,20 @@ int launch_nibbles(const uint32_t *packed, const uint64_t *offs, const uint32_t 
   return NGIA_OK;
 }
 
-// Every layout of a run of records in one pass over their planes, for loads
-// whose code map is assumed ahead (the pipelined load): nibbles, recoded
-// nibbles and code planes.  Only the map's own codes are looked at: a residue
+// The layouts a recoded database needs, for a run of records in one pass over
+// their planes, for loads whose code map is assumed ahead (the pipelined
+// load): recoded nibbles and code planes (the sketch reads residue codes from
+// the planes themselves).  Only the map's own codes are looked at: a residue
 // of another code (or a record outside words [w0, w1), which is then left
-// alone) sets *bad, and the load falls back.  Any subset of the map's codes
+// empty) sets *bad, and the load falls back.  Any subset of the map's codes
 // is served by the same map (it stays one-to-one on the codes present).
 // codes[k], k < ncodes: the residue codes of the map, aligner code k + 1.
 __global__ void __launch_bounds__(256)
 load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
                     const uint32_t *__restrict__ lens, uint32_t n, uint64_t w0, uint64_t w1,
                     uint64_t words, uint32_t codes, uint32_t ncodes,
-                    uint32_t *__restrict__ nib, uint32_t *__restrict__ dense_nib,
-                    uint32_t *__restrict__ dplanes, uint32_t *__restrict__ bad) {
+                    uint32_t *__restrict__ dense_nib, uint32_t *__restrict__ dplanes,
+                    uint32_t *__restrict__ bad) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   bool wrong = false;
@@ -312,19 +313,18 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
     // when its offset lies in the region, left empty in every layout (the
     // sketch also bounds every record it reads by the region)
     if (o < w0 || o >= w1) {
-      if (lane == 0 && o < words) nib[o] = dense_nib[o] = dplanes[o] = 0;
+      if (lane == 0 && o < words) dense_nib[o] = dplanes[o] = 0;
       wrong = true;
       continue;
     }
     const uint32_t len = __ldg(packed + o);
     const uint32_t blocks = (len + 31) >> 5;
     if (len != lens[i] || o + 1 + 4ull * blocks > w1) {
-      if (lane == 0) nib[o] = dense_nib[o] = dplanes[o] = 0;
+      if (lane == 0) dense_nib[o] = dplanes[o] = 0;
       wrong = true;
       continue;
     }
     if (lane == 0) {
-      nib[o] = len;
       dense_nib[o] = len;
       dplanes[o] = len;
     }
@@ -332,8 +332,6 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
       const uint64_t b = o + 1 + 4ull * k;
       const uint32_t pl[4] = {__ldg(packed + b), __ldg(packed + b + 1), __ldg(packed + b + 2),
                               __ldg(packed + b + 3)};
-      uint32_t w[4];
-      planes_to_nibbles(pl, 4, w);
       const uint32_t left = len - 32 * k;
       const uint32_t real = left >= 32 ? kFull : (1u << left) - 1u;
       uint32_t d[4] = {0u, 0u, 0u, 0u}, known = 0u;
@@ -350,7 +348,6 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
       planes_to_nibbles(d, 3, dn);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        nib[b + q] = w[q];
         dense_nib[b + q] = dn[q];
         dplanes[b + q] = d[q];
       }
@@ -372,7 +369,7 @@ static int map_bits(uint64_t map, uint32_t (&bits)[3]) {
 
 int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint32_t *lens,
                         uint32_t n, uint64_t w0, uint64_t w1, uint64_t words, uint64_t inv,
-                        uint32_t *nib, uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad,
+                        uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad,
                         cudaStream_t s) {
   if (w0 > w1 || w1 > words) return NGIA_ERR_ARG;
   if (n == 0) return NGIA_OK;
@@ -387,7 +384,7 @@ int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
   load_layouts_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
-      packed, offs, lens, n, w0, w1, words, codes, ncodes, nib, dense_nib, dplanes, bad);
+      packed, offs, lens, n, w0, w1, words, codes, ncodes, dense_nib, dplanes, bad);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

@@ -60,14 +60,21 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_d
   if (!sketch_done) {  // (else ev[8], ev[9] bracket the pipelined load and sketch)
     NGIA_CUDA(cudaEventRecord(c->ev[8], s));
     if (c->use_table && c->table_ok)
-      NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
+      NGIA_TRY(launch_sketch_table(c->packed.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
                                    c->offs.as<uint64_t>(), c->n, c->packed_words, c->ab.inv,
                                    c->sketch_table.p,
                                    c->sigs.as<uint32_t>(), c->n, s, c->side, c->ev[6],
                                    c->ev[7]));
-    else
+    else {
+      if (c->nib_stale) {  // the pieced load leaves the residue-code nibbles out
+        NGIA_TRY(launch_nibbles(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(),
+                                c->lens.as<uint32_t>(), c->n, c->packed_words,
+                                c->nib.as<uint32_t>(), c->presence.as<uint32_t>(), s));
+        c->nib_stale = false;
+      }
       NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
                                      c->sigs.as<uint32_t>(), s));
+    }
     NGIA_CUDA(cudaEventRecord(c->ev[9], s));
   }
   NGIA_TRY(bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(),
@@ -292,6 +299,7 @@ int ctx_load(ngia_ctx *c, const uint32_t *h_packed, uint64_t words, const uint64
   NGIA_TRY(launch_nibbles(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(),
                           c->lens.as<uint32_t>(), n, words, c->nib.as<uint32_t>(),
                           c->presence.as<uint32_t>(), s));
+  c->nib_stale = false;
   uint32_t present = 0;
   NGIA_CUDA(cudaMemcpyAsync(&present, c->presence.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             s));
@@ -338,6 +346,7 @@ int ctx_load_text(ngia_ctx *c, const char *h_text, uint64_t text_bytes,
                               c->lens.as<uint32_t>(), n, c->offs.as<uint64_t>(),
                               c->packed.as<uint32_t>(), c->nib.as<uint32_t>(),
                               c->presence.as<uint32_t>(), s));
+  c->nib_stale = false;
   uint32_t present = 0;
   NGIA_CUDA(cudaMemcpyAsync(&present, c->presence.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             s));
@@ -463,8 +472,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
     if (cnt) {
       const uint64_t w0 = bound(k), w1 = bound(k + 1);
       NGIA_TRY(launch_load_layouts(packed, offs + r0, c->lens.as<uint32_t>() + r0, cnt, w0, w1,
-                                   words, spec.inv,
-                                   c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(),
+                                   words, spec.inv, c->nib_dense.as<uint32_t>(),
                                    c->dplanes.as<uint32_t>(), c->presence.as<uint32_t>(),
                                    c->layout));
     }
@@ -475,7 +483,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
     const uint32_t r0 = first[k], cnt = first[k + 1] - first[k];
     NGIA_CUDA(cudaStreamWaitEvent(s, c->layout_ev[k], 0));
     if (cnt == 0) continue;
-    NGIA_TRY(launch_sketch_table(c->nib.as<uint32_t>(), c->nib_dense.as<uint32_t>(), offs + r0,
+    NGIA_TRY(launch_sketch_table(packed, c->nib_dense.as<uint32_t>(), offs + r0,
                                  cnt, words, spec.inv, c->sketch_table.p,
                                  c->sigs.as<uint32_t>() + r0, n, s, c->side, c->ev[6], nullptr));
   }
@@ -492,6 +500,7 @@ int ctx_load_sketch(ngia_ctx *c, const uint32_t *h_packed, uint64_t words,
   NGIA_CUDA(cudaMemcpyAsync(c->h_flag, c->presence.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             s));
   *sketched = true;
+  c->nib_stale = true;
   NGIA_TRY(use_alphabet(c, spec, words, n, false));
   c->n = n;
   c->sigs_valid = false;

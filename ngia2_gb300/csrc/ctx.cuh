@@ -24,6 +24,7 @@ struct ngia_ctx {
   uint64_t packed_words = 0;
   uint32_t rep_bands = 0;
   ngia::DevBuf packed, nib, offs, lens, rep, sigs;
+  bool nib_stale = false;  // `nib` not written by the last load (the pieced one)
   ngia::DevBuf staging;  // residue text of a load from text (released after it)
   ngia::DevBuf part_tmp;  // band blocks and their prefix (a graph build split over devices)
   bool sigs_valid = false;  // sigs hold all 64 bands of the loaded records

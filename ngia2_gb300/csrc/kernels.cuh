@@ -25,7 +25,7 @@ int build_sketch_table(uint64_t inv, void *table, cudaStream_t s);
 // joins later) beside the rank walk on s.  A record whose offset or length
 // word puts it past `words` (the layouts' size) is skipped, so the kernels
 // stay inside the layouts whatever the offsets hold.
-int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
+int launch_sketch_table(const uint32_t *packed, const uint32_t *dense, const uint64_t *offs,
                         uint32_t n, uint64_t words, uint64_t inv, const void *table,
                         uint32_t *sigs, uint32_t stride, cudaStream_t s, cudaStream_t side,
                         cudaEvent_t fork, cudaEvent_t join);
@@ -78,7 +78,7 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
 // (A record whose length word is not lens[i] sets *bad too.)
 int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint32_t *lens,
                         uint32_t n, uint64_t w0, uint64_t w1, uint64_t words, uint64_t inv,
-                        uint32_t *nib, uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad,
+                        uint32_t *dense_nib, uint32_t *dplanes, uint32_t *bad,
                         cudaStream_t s);
 // presence |= the codes seen (cleared first unless accumulate); a record
 // outside the region's `words`, or whose length word is not lens[i], is

@@ -334,10 +334,11 @@ sketch_rank_kernel(const uint32_t *__restrict__ dense, const uint64_t *__restric
 }
 
 // Records with fewer than kRankMinSpan signed positions: row table + hashing.
-// nib: the records' residue codes (records shorter than 8 are hashed
-// directly); dense: the same records in aligner codes 1..4.
+// packed: the records' bit planes (residue codes for the hashed bands, and
+// records shorter than 8, hashed directly); dense: the same records in
+// aligner codes 1..4 (the table's index).
 __global__ void __launch_bounds__(256)
-sketch_table_kernel(const uint32_t *__restrict__ nib, const uint32_t *__restrict__ dense,
+sketch_table_kernel(const uint32_t *__restrict__ packed, const uint32_t *__restrict__ dense,
                     const uint64_t *__restrict__ offs, uint32_t n, uint64_t words,
                     const uint4 *__restrict__ table, uint32_t *__restrict__ sigs,
                     uint32_t stride) {
@@ -346,7 +347,7 @@ sketch_table_kernel(const uint32_t *__restrict__ nib, const uint32_t *__restrict
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t o = offs[i];
     if (o >= words) continue;  // outside the layouts (flagged by their kernel)
-    const uint32_t len = __ldg(nib + o);
+    const uint32_t len = __ldg(packed + o);
     if (len >= 7 + kRankMinSpan) continue;  // the rank walk's
     if (o + 1 + 4ull * ((len + 31u) >> 5) > words) continue;
     uint32_t mn[kBands];
@@ -358,14 +359,15 @@ sketch_table_kernel(const uint32_t *__restrict__ nib, const uint32_t *__restrict
       const uint32_t pb = 7 + lane * per;
       const uint32_t pe = min(pb + per, len);
       if (pb < pe) {
-        const NibbleKmers src = NibbleKmers::make(nib + o);
+        PlaneKmers src = PlaneKmers::make(packed + o);  // rolled along the lane's run
+        src.start(pb);
         for_each_index(dense + o + 1, pb, pe, [&](uint32_t p, uint32_t idx) {
           const uint4 *row = table + (size_t)idx * (kTableBands / 4);
           uint4 v[kTableBands / 4];
 #pragma unroll
           for (int k = 0; k < kTableBands / 4; ++k) v[k] = __ldg(row + k);
           // the other bands are hashed while the row is on its way
-          const uint32_t kmer = NibbleKmers(src).at(p);
+          const uint32_t kmer = src.at(p);
           const uint32_t y = kmer ^ (kmer >> 16);
 #pragma unroll
           for (int k = kTableBands; k < kBands; ++k)
@@ -380,7 +382,9 @@ sketch_table_kernel(const uint32_t *__restrict__ nib, const uint32_t *__restrict
         });
       }
     } else if (len > 0 && lane == 0) {  // the one signed position: the whole record
-      const uint32_t kmer = NibbleKmers::make(nib + o).at(len - 1);
+      PlaneKmers src = PlaneKmers::make(packed + o);
+      src.start(len - 1);
+      const uint32_t kmer = src.at(len - 1);
       const uint32_t y = kmer ^ (kmer >> 16);
 #pragma unroll
       for (int k = 0; k < kBands; ++k) mn[k] = band_hash_tail(y ^ band_seed_fold((uint32_t)k));
@@ -440,7 +444,7 @@ static int rank_blocks_per_sm() {
   return cached;
 }
 
-int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64_t *offs,
+int launch_sketch_table(const uint32_t *packed, const uint32_t *dense, const uint64_t *offs,
                         uint32_t n, uint64_t words, uint64_t inv, const void *table,
                         uint32_t *sigs, uint32_t stride, cudaStream_t s, cudaStream_t side,
                         cudaEvent_t fork, cudaEvent_t join) {
@@ -456,7 +460,7 @@ int launch_sketch_table(const uint32_t *nib, const uint32_t *dense, const uint64
   NGIA_CUDA(cudaStreamWaitEvent(side, fork, 0));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms;
   sketch_table_kernel<<<want < cap ? want : cap, 256, 0, side>>>(
-      nib, dense, offs, n, words, reinterpret_cast<const uint4 *>(base), sigs, stride);
+      packed, dense, offs, n, words, reinterpret_cast<const uint4 *>(base), sigs, stride);
   NGIA_LAUNCHED();
   const uint32_t rank_want = ceil_div(n, kRankWarps);
   const uint32_t rank_cap = (uint32_t)(sms * rank_blocks_per_sm());

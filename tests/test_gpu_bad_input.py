@@ -174,3 +174,15 @@ def test_pieced_upload_refuses_records_outside(dna5k):
             got, st = run_host(ctx, dna5k)
             assert st["load_pipelined"] == 1
             assert np.array_equal(got, want)
+
+
+def test_hashing_sketch_after_a_pieced_load(dna5k):
+    """The pieced upload leaves the residue-code nibbles out (its sketch reads
+    the planes); the hashing sketch, which reads them, rebuilds them first."""
+    with ng.Context() as ctx:
+        want, _ = run_host(ctx, dna5k)
+        got, st = run_host(ctx, dna5k)
+        assert st["load_pipelined"] == 1 and np.array_equal(got, want)
+        ctx.use_sketch_table(False)
+        m, _ = ctx.group_align(95, 64)
+        assert np.array_equal(ctx.edges(m), want)
