@@ -298,6 +298,9 @@ int launch_nibbles(const uint32_t *packed, const uint64_t *offs, const uint32_t 
 // empty) sets *bad, and the load falls back.  Any subset of the map's codes
 // is served by the same map (it stays one-to-one on the codes present).
 // codes[k], k < ncodes: the residue codes of the map, aligner code k + 1.
+// kDense / kPlanes: which of the two layouts a launch writes (a null output
+// pointer leaves its layout out).
+template <bool kDense, bool kPlanes>
 __global__ void __launch_bounds__(256)
 load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restrict__ offs,
                     const uint32_t *__restrict__ lens, uint32_t n, uint64_t w0, uint64_t w1,
@@ -313,20 +316,26 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
     // when its offset lies in the region, left empty in every layout (the
     // sketch also bounds every record it reads by the region)
     if (o < w0 || o >= w1) {
-      if (lane == 0 && o < words) dense_nib[o] = dplanes[o] = 0;
+      if (lane == 0 && o < words) {
+        if (kDense) dense_nib[o] = 0;
+        if (kPlanes) dplanes[o] = 0;
+      }
       wrong = true;
       continue;
     }
     const uint32_t len = __ldg(packed + o);
     const uint32_t blocks = (len + 31) >> 5;
     if (len != lens[i] || o + 1 + 4ull * blocks > w1) {
-      if (lane == 0) dense_nib[o] = dplanes[o] = 0;
+      if (lane == 0) {
+        if (kDense) dense_nib[o] = 0;
+        if (kPlanes) dplanes[o] = 0;
+      }
       wrong = true;
       continue;
     }
     if (lane == 0) {
-      dense_nib[o] = len;
-      dplanes[o] = len;
+      if (kDense) dense_nib[o] = len;
+      if (kPlanes) dplanes[o] = len;
     }
     for (uint32_t k = lane; k < blocks; k += 32) {
       const uint64_t b = o + 1 + 4ull * k;
@@ -344,12 +353,15 @@ load_layouts_kernel(const uint32_t *__restrict__ packed, const uint64_t *__restr
         d[2] |= a & 4u ? m : 0u;
       }
       if (real & ~known) wrong = true;
-      uint32_t dn[4];
-      planes_to_nibbles(d, 3, dn);
+      if (kDense) {
+        uint32_t dn[4];
+        planes_to_nibbles(d, 3, dn);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        dense_nib[b + q] = dn[q];
-        dplanes[b + q] = d[q];
+        for (int q = 0; q < 4; ++q) dense_nib[b + q] = dn[q];
+      }
+      if (kPlanes) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dplanes[b + q] = d[q];
       }
     }
   }
@@ -383,8 +395,16 @@ int launch_load_layouts(const uint32_t *packed, const uint64_t *offs, const uint
   NGIA_CUDA(cudaGetDevice(&dev));
   NGIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint32_t want = ceil_div(n, 8u), cap = (uint32_t)sms * 16u;
-  load_layouts_kernel<<<want < cap ? want : cap, 256, 0, s>>>(
-      packed, offs, lens, n, w0, w1, words, codes, ncodes, dense_nib, dplanes, bad);
+  if (!dense_nib && !dplanes) return NGIA_OK;
+  if (dense_nib && dplanes)
+    load_layouts_kernel<true, true><<<want < cap ? want : cap, 256, 0, s>>>(
+        packed, offs, lens, n, w0, w1, words, codes, ncodes, dense_nib, dplanes, bad);
+  else if (dense_nib)
+    load_layouts_kernel<true, false><<<want < cap ? want : cap, 256, 0, s>>>(
+        packed, offs, lens, n, w0, w1, words, codes, ncodes, dense_nib, dplanes, bad);
+  else
+    load_layouts_kernel<false, true><<<want < cap ? want : cap, 256, 0, s>>>(
+        packed, offs, lens, n, w0, w1, words, codes, ncodes, dense_nib, dplanes, bad);
   NGIA_LAUNCHED();
   return NGIA_OK;
 }

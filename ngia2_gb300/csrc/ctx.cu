@@ -36,6 +36,17 @@ DbView db_view(const ngia_ctx *c) {
                 c->lens.as<uint32_t>()};
 }
 
+int ctx_ready_layouts(ngia_ctx *c) {
+  if (c->nib_stale && c->n) {
+    NGIA_TRY(c->presence.reserve(2 * sizeof(uint32_t)));  // word 1: scratch for the checks
+    NGIA_TRY(launch_nibbles(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(),
+                            c->lens.as<uint32_t>(), c->n, c->packed_words,
+                            c->nib.as<uint32_t>(), c->presence.as<uint32_t>() + 1, c->stream));
+    c->nib_stale = false;
+  }
+  return NGIA_OK;
+}
+
 void ctx_stage_stats(ngia_ctx *c, ngia_stats *st) {
   st->ms_sketch = ev_ms(c->ev[8], c->ev[9]);
   st->ms_bucket = ev_ms(c->ev[9], c->ev[10]);
@@ -66,12 +77,7 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_d
                                    c->sigs.as<uint32_t>(), c->n, s, c->side, c->ev[6],
                                    c->ev[7]));
     else {
-      if (c->nib_stale) {  // the pieced load leaves the residue-code nibbles out
-        NGIA_TRY(launch_nibbles(c->packed.as<uint32_t>(), c->offs.as<uint64_t>(),
-                                c->lens.as<uint32_t>(), c->n, c->packed_words,
-                                c->nib.as<uint32_t>(), c->presence.as<uint32_t>(), s));
-        c->nib_stale = false;
-      }
+      NGIA_TRY(ctx_ready_layouts(c));  // a pieced load leaves the nibbles out
       NGIA_TRY(launch_sketch_nibbles(c->nib.as<uint32_t>(), c->offs.as<uint64_t>(), c->n,
                                      c->sigs.as<uint32_t>(), s));
     }

@@ -24,7 +24,9 @@ struct ngia_ctx {
   uint64_t packed_words = 0;
   uint32_t rep_bands = 0;
   ngia::DevBuf packed, nib, offs, lens, rep, sigs;
-  bool nib_stale = false;  // `nib` not written by the last load (the pieced one)
+  // the pieced load (ngia_ctx_run_host) writes no residue-code nibbles;
+  // ctx_ready_layouts rebuilds them for the kernels that read them
+  bool nib_stale = false;
   ngia::DevBuf staging;  // residue text of a load from text (released after it)
   ngia::DevBuf part_tmp;  // band blocks and their prefix (a graph build split over devices)
   bool sigs_valid = false;  // sigs hold all 64 bands of the loaded records
@@ -57,6 +59,9 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_d
                       bool defer_stats = false);
 // ms_sketch and ms_bucket of the last ctx_sketch_bucket, once its work is done.
 void ctx_stage_stats(ngia_ctx *c, ngia_stats *st);
+// Rebuilds the residue-code nibbles a pieced load left out (on the
+// context's stream), for the kernels that read them.
+int ctx_ready_layouts(ngia_ctx *c);
 int ctx_fast_cluster(ngia_ctx *c, uint32_t identity, uint32_t bands, uint32_t *h_cluster,
                      ngia_stats *st);
 // Load from residue text (makedb): record i's h_lens[i] residues start at byte

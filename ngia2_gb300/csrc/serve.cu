@@ -381,6 +381,8 @@ static int server_init(ngia_server *s, ngia_ctx *db, const uint32_t *h_cluster,
   const uint64_t total_recs = (uint64_t)n + (uint64_t)S * Q;
   if (total_recs > 0xFFFFFFFFull) return NGIA_ERR_ARG;
   cudaStream_t st = db->stream;
+  // the database's layouts complete (a pieced load leaves the nibbles out)
+  NGIA_TRY(ctx_ready_layouts(db));
   NGIA_TRY(s->packed.reserve(total_words * 4));
   NGIA_TRY(s->nib.reserve(total_words * 4));
   if (s->recode_map) {

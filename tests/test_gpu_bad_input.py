@@ -186,3 +186,31 @@ def test_hashing_sketch_after_a_pieced_load(dna5k):
         ctx.use_sketch_table(False)
         m, _ = ctx.group_align(95, 64)
         assert np.array_equal(ctx.edges(m), want)
+
+
+def test_server_over_a_pieced_load(dna5k):
+    """A server built on a context whose database came through the pieced
+    upload (code planes deferred, residue-code nibbles left out) answers
+    exactly as one built on the plain load of the same database."""
+    p, o, l = dna5k["packed"], dna5k["offsets"], dna5k["lens"]
+    sel = np.arange(0, len(l), 50)[:64]  # database records as queries: they assign
+    recs = [p[int(o[i]):int(o[i]) + 1 + 4 * ((int(l[i]) + 31) // 32)] for i in sel]
+    q_off = np.concatenate([[0], np.cumsum([len(r) for r in recs])[:-1]]).astype(np.uint64)
+    q = (np.concatenate(recs).astype(np.uint32), q_off, l[sel].astype(np.uint32))
+    results = []
+    for pieced in (False, True):
+        with ng.Context() as ctx:
+            if pieced:
+                run_host(ctx, dna5k)
+                _, st = run_host(ctx, dna5k)
+                assert st["load_pipelined"] == 1
+            else:
+                ctx.load(p, o, l)
+                ctx.sketch_bucket(64)
+            cluster = ctx.fast_cluster(95)
+            with ng.Server(ctx, cluster, 95, slots=2) as srv:
+                res, _ = srv.wait(srv.submit(*q), len(sel))
+            results.append((cluster, res))
+    assert np.array_equal(results[0][0], results[1][0])
+    assert np.array_equal(results[0][1], results[1][1])
+    assert (results[1][1] != ng.NEW_CLUSTER).any()
