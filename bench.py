@@ -1013,11 +1013,18 @@ def run_stream(args) -> dict:
     workdir = Path(tempfile.mkdtemp(prefix="ngia_stream_"))
     packed, offs, lens = make_stream(args.stream_seqs, workdir)
     n = len(lens)
+    # the records in page-locked host memory (set up before timing, as an
+    # application holding its database for streaming would), so that chunks
+    # go to the device straight from it
+    import torch
+    t_pin = torch.empty(packed.nbytes, dtype=torch.uint8, pin_memory=True)
+    pinned = t_pin.numpy().view(packed.dtype)
+    pinned[:] = packed
+    packed = pinned
     runs = {}
     k = min(n, 1000)  # warm-up on the first records
     k_words = int(offs[k - 1]) + 1 + 4 * ((int(lens[k - 1]) + 31) // 32)
     budget = args.stream_chunk_bytes
-    import torch
     clk = ClockSampler(torch.cuda.current_device())
     for identity in STREAM_IDENTITIES:
         ng.stream_graph(packed[:k_words], offs[:k], lens[:k], identity, STREAM_BANDS, budget)
@@ -1051,6 +1058,7 @@ def run_stream(args) -> dict:
                 "packed on the device",
         "metric": "seqs/s end to end", "unit": "seqs/s", "sequences": n,
         "packed_bytes": int(packed.nbytes), "device_bytes_for_records": budget,
+        "host_records": "page-locked (allocated pinned before timing)",
         "runs": runs,
     }
 

@@ -117,25 +117,44 @@ static void parallel_copy(void *dst, const void *src, size_t bytes) {
   for (auto &t : th) t.join();
 }
 
+// page-locked host memory the device can copy from directly, over the whole
+// of [p, p + bytes)
+static bool host_pinned(const void *p, size_t bytes) {
+  const char *b = static_cast<const char *>(p);
+  for (const char *q : {b, b + (bytes ? bytes - 1 : 0)}) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    if (a.type != cudaMemoryTypeHost) return false;
+  }
+  return true;
+}
+
 // Pinned double-buffered staging of chunks into the device region's slots.
 // stage() copies a chunk's words into one of two pinned buffers (CPU) once
 // that buffer's previous copy has reached the device, then issues the
 // host-to-device copy on its own stream after the compute stream has
 // finished with the destination slot (slot_done[slot], recorded by the
 // user after the slot's last reader); the returned event marks the data on
-// the device.
+// the device.  When the caller's records are themselves page-locked, the
+// copy reads them in place and the host copy is skipped: the link alone
+// bounds the staging.
 struct Stager {
   static constexpr int kSlots = 3;
   const uint32_t *h_packed = nullptr;
+  bool direct = false;  // the caller's records are page-locked: copied from in place
   uint32_t *pinned[2] = {};
   cudaEvent_t copied_ev[2] = {}, slot_done[kSlots] = {};
   cudaStream_t copy = nullptr;
   int next = 0;
   uint64_t bytes = 0;
-  int init(const uint32_t *packed, uint64_t chunk_words) {
+  int init(const uint32_t *packed, uint64_t words, uint64_t chunk_words) {
     h_packed = packed;
+    direct = host_pinned(packed, words * 4);
     for (int k = 0; k < 2; ++k) {
-      NGIA_CUDA(cudaMallocHost(&pinned[k], chunk_words * 4));
+      if (!direct) NGIA_CUDA(cudaMallocHost(&pinned[k], chunk_words * 4));
       NGIA_CUDA(cudaEventCreateWithFlags(&copied_ev[k], cudaEventDisableTiming));
     }
     for (int k = 0; k < kSlots; ++k)
@@ -146,10 +165,14 @@ struct Stager {
   int stage(const Chunk &c, int slot, uint32_t *dst, cudaEvent_t *copied) {
     const int b = next;
     next ^= 1;
-    NGIA_CUDA(cudaEventSynchronize(copied_ev[b]));  // the pinned buffer's last copy is done
-    parallel_copy(pinned[b], h_packed + c.word_first, c.words * 4);
+    const uint32_t *src = h_packed + c.word_first;
+    if (!direct) {
+      NGIA_CUDA(cudaEventSynchronize(copied_ev[b]));  // the pinned buffer's last copy is done
+      parallel_copy(pinned[b], src, c.words * 4);
+      src = pinned[b];
+    }
     NGIA_CUDA(cudaStreamWaitEvent(copy, slot_done[slot], 0));
-    NGIA_CUDA(cudaMemcpyAsync(dst, pinned[b], c.words * 4, cudaMemcpyHostToDevice, copy));
+    NGIA_CUDA(cudaMemcpyAsync(dst, src, c.words * 4, cudaMemcpyHostToDevice, copy));
     NGIA_CUDA(cudaEventRecord(copied_ev[b], copy));
     bytes += c.words * 4;
     *copied = copied_ev[b];
@@ -233,7 +256,7 @@ static int stream_graph(StreamState &S, const uint32_t *h_packed, uint64_t words
   NGIA_CUDA(cudaStreamCreateWithFlags(&S.s, cudaStreamNonBlocking));
   cudaStream_t s = S.s;
   NGIA_TRY(S.round.init(s));
-  NGIA_TRY(S.stager.init(h_packed, chunk_words));
+  NGIA_TRY(S.stager.init(h_packed, words, chunk_words));
   NGIA_TRY(S.region_packed.reserve(3 * chunk_words * 4));
   NGIA_TRY(S.region_nib.reserve(3 * chunk_words * 4));
   NGIA_TRY(S.r_offs.reserve(2ull * max_recs * 8));

@@ -61,3 +61,20 @@ def test_stream_refuses_records_larger_than_a_chunk(cuda, built):
     packed, offs, lens = pack(s)
     with pytest.raises(ng.NgiaError):
         ng.stream_graph(packed, offs, lens, 90, 3, 36 * 10)
+
+
+def test_stream_from_page_locked_records(cuda, built):
+    """Records in page-locked host memory are copied to the device in place
+    (no host staging copy); the edges are the same as from pageable memory."""
+    import torch
+    s = synth.protein_families(8_000, 800, seed=74)
+    packed, offs, lens = pack(s)
+    chunk_bytes = 36 * (len(packed) // 5 + 2000)
+    t = torch.empty(packed.nbytes, dtype=torch.uint8, pin_memory=True)
+    pinned = t.numpy().view(np.uint32)
+    pinned[:] = packed
+    e_pin, st_pin = ng.stream_graph(pinned, offs, lens, 70, 64, chunk_bytes)
+    e_page, st_page = ng.stream_graph(packed, offs, lens, 70, 64, chunk_bytes)
+    assert st_pin["chunks"] >= 3
+    assert np.array_equal(as_triples(e_pin), as_triples(e_page))
+    assert st_pin["bytes_h2d_align"] == st_page["bytes_h2d_align"]
