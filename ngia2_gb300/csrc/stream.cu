@@ -138,9 +138,14 @@ static bool host_pinned(const void *p, size_t bytes) {
 // host-to-device copy on its own stream after the compute stream has
 // finished with the destination slot (slot_done[slot], recorded by the
 // user after the slot's last reader); the returned event marks the data on
-// the device.  When the caller's records are themselves page-locked, the
-// copy reads them in place and the host copy is skipped: the link alone
-// bounds the staging.
+// the device.  When the caller's records are themselves page-locked and span
+// at most kDirectMaxBytes, the copy reads them in place and the host copy is
+// skipped.  Measured on a GB300 host: 1.09 GB of page-locked records went
+// over at 132 GB/s in place against 62 GB/s through the staging buffers,
+// but 10.9 GB at 38-60 GB/s in place against 91 GB/s staged (the in-place
+// copies walk the whole region's pages; the staging buffers stay small).
+constexpr uint64_t kDirectMaxBytes = 4ull << 30;
+
 struct Stager {
   static constexpr int kSlots = 3;
   const uint32_t *h_packed = nullptr;
@@ -152,7 +157,7 @@ struct Stager {
   uint64_t bytes = 0;
   int init(const uint32_t *packed, uint64_t words, uint64_t chunk_words) {
     h_packed = packed;
-    direct = host_pinned(packed, words * 4);
+    direct = words * 4 <= kDirectMaxBytes && host_pinned(packed, words * 4);
     for (int k = 0; k < 2; ++k) {
       if (!direct) NGIA_CUDA(cudaMallocHost(&pinned[k], chunk_words * 4));
       NGIA_CUDA(cudaEventCreateWithFlags(&copied_ev[k], cudaEventDisableTiming));
