@@ -291,7 +291,9 @@ int ngia_pack_records(const uint8_t *h_residues, uint64_t residue_bytes,
  * rest -- signatures, rep rows, lengths, offsets, pairs, scores -- grows with
  * the record count only and stays on the device).  The records pass through
  * pinned double-buffered copies twice: once to sketch them, once per block
- * of pairs (rep chunk, target chunk) to align them.  The edges equal the
+ * of pairs (rep chunk, target chunk) to align them; records that are
+ * themselves page-locked (cudaHostAlloc'd or registered) and span at most
+ * 4 GiB are copied from in place instead.  The edges equal the
  * resident path's.  Records must be in index order (increasing offsets, not
  * overlapping); h_edges needs room for the edges (NGIA_ERR_NOMEM if cap is
  * too small).  Replaces the reference's managed-memory oversubscription
