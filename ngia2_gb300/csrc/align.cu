@@ -526,6 +526,15 @@ static int launch_group_cta_k(const RoundArgs &a, int cls, unsigned int *cursor,
 #ifndef NGIA_CTA_WARPS
 #define NGIA_CTA_WARPS 0  // 0: the classes run on one warp per pair (align_group.cuh)
 #endif
+// the first group class (index within the ladder) run block-wide when
+// NGIA_CTA_WARPS is set: 6 = the two widest, (32,8) and (32,16); 4 adds
+// (32,4) and (32,6).  On the re-laddered classes, same pairs and box: one
+// warp per pair 8.05 ms per round (autotuned), blocks of two warps from
+// (32,4) on 8.52 ms, from (32,6) on 8.65 ms.
+#ifndef NGIA_CTA_FROM
+#define NGIA_CTA_FROM 6
+#endif
+static_assert(NGIA_CTA_FROM >= 4 && NGIA_CTA_FROM <= 7, "block-wide classes are the G = 32 ones");
 constexpr int kCtaWarps = NGIA_CTA_WARPS > 0 ? NGIA_CTA_WARPS : 1;
 template <int K>
 static int launch_group_cta(const RoundArgs &a, int KC, int cls, unsigned int *cursor,
@@ -601,20 +610,20 @@ int launch_align_class(int cls, const uint32_t *packed, const uint32_t *nib,
     NGIA_GROUP_CASE(kFirstGroupClass + 1)
     NGIA_GROUP_CASE(kFirstGroupClass + 2)
     NGIA_GROUP_CASE(kFirstGroupClass + 3)
-    NGIA_GROUP_CASE(kFirstGroupClass + 4)
-    NGIA_GROUP_CASE(kFirstGroupClass + 5)
 #undef NGIA_GROUP_CASE
-    case kFirstGroupClass + 6:
-      static_assert(group_shape(kFirstGroupClass + 6).G == 32 &&
-                        group_shape(kFirstGroupClass + 7).G == 32 && kNumGroupClasses == 8,
-                    "block-wide classes: the two widest");
-      return NGIA_CTA_WARPS
-                 ? launch_group_cta<group_shape(kFirstGroupClass + 6).K>(a, ab.K, cls, cursor, s)
-                 : launch_group<32, group_shape(kFirstGroupClass + 6).K>(a, ab.K, cls, cursor, s);
-    case kFirstGroupClass + 7:
-      return NGIA_CTA_WARPS
-                 ? launch_group_cta<group_shape(kFirstGroupClass + 7).K>(a, ab.K, cls, cursor, s)
-                 : launch_group<32, group_shape(kFirstGroupClass + 7).K>(a, ab.K, cls, cursor, s);
+    // the G = 32 classes, block-wide from NGIA_CTA_FROM on when NGIA_CTA_WARPS is set
+#define NGIA_WIDE_CASE(I)                                                                   \
+  case kFirstGroupClass + I:                                                                \
+    static_assert(group_shape(kFirstGroupClass + I).G == 32, "a G = 32 class");             \
+    return NGIA_CTA_WARPS && I >= NGIA_CTA_FROM                                              \
+               ? launch_group_cta<group_shape(kFirstGroupClass + I).K>(a, ab.K, cls, cursor, s) \
+               : launch_group<32, group_shape(kFirstGroupClass + I).K>(a, ab.K, cls, cursor, s);
+    NGIA_WIDE_CASE(4)
+    NGIA_WIDE_CASE(5)
+    NGIA_WIDE_CASE(6)
+    NGIA_WIDE_CASE(7)
+#undef NGIA_WIDE_CASE
+    static_assert(kNumGroupClasses == 8, "the ladder's cases above");
     case kGeneralClass: {
       uint32_t grid = 0;
       NGIA_TRY(persistent_grid(align_general_kernel, 128, 0, kFull, &grid));
