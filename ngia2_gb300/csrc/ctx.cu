@@ -36,6 +36,45 @@ DbView db_view(const ngia_ctx *c) {
                 c->lens.as<uint32_t>()};
 }
 
+// The bucketing on the context's stream, through a cached graph when the
+// round uses graphs (captured again when the signature rows, rep rows or
+// scratch move, or n or bands change).
+static int bucket_graph(ngia_ctx *c, uint32_t bands) {
+  cudaStream_t s = c->stream;
+  if (!c->round.use_graphs)
+    return bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(), c->sort_tmp.p, s);
+  const uint64_t key_n = ((uint64_t)c->n << 8) | bands;
+  const uint64_t gen = g_alloc_gen.load();
+  if (!c->bucket_exec || c->bucket_key[0] != c->sigs.p || c->bucket_key[1] != c->rep.p ||
+      c->bucket_key[2] != c->sort_tmp.p || c->bucket_key_n != key_n ||
+      c->bucket_key_gen != gen) {
+    if (c->bucket_exec) cudaGraphExecDestroy(c->bucket_exec);
+    c->bucket_exec = nullptr;
+    NGIA_TRY(sort_prepare());  // one-time attributes, outside the capture
+    NGIA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    int rc = bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(), c->sort_tmp.p, s);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e1 = cudaStreamEndCapture(s, &graph);
+    if (rc == NGIA_OK && e1 != cudaSuccess) rc = cuda_fail(e1);
+    if (rc == NGIA_OK) {
+      const cudaError_t e2 = cudaGraphInstantiate(&c->bucket_exec, graph, 0);
+      if (e2 != cudaSuccess) rc = cuda_fail(e2);
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (rc != NGIA_OK) {
+      c->bucket_exec = nullptr;
+      return rc;
+    }
+    c->bucket_key[0] = c->sigs.p;
+    c->bucket_key[1] = c->rep.p;
+    c->bucket_key[2] = c->sort_tmp.p;
+    c->bucket_key_n = key_n;
+    c->bucket_key_gen = gen;
+  }
+  NGIA_CUDA(cudaGraphLaunch(c->bucket_exec, s));
+  return NGIA_OK;
+}
+
 int ctx_ready_layouts(ngia_ctx *c) {
   if (c->nib_stale && c->n) {
     NGIA_TRY(c->presence.reserve(2 * sizeof(uint32_t)));  // word 1: scratch for the checks
@@ -83,8 +122,7 @@ int ctx_sketch_bucket(ngia_ctx *c, uint32_t bands, ngia_stats *st, bool sketch_d
     }
     NGIA_CUDA(cudaEventRecord(c->ev[9], s));
   }
-  NGIA_TRY(bucket(c->sigs.as<uint32_t>(), c->n, bands, c->rep.as<uint32_t>(),
-                  c->sort_tmp.p, s));
+  NGIA_TRY(bucket_graph(c, bands));
   NGIA_CUDA(cudaEventRecord(c->ev[10], s));
   c->rep_bands = bands;
   c->sigs_valid = true;
@@ -594,6 +632,8 @@ void ngia_ctx_destroy(ngia_ctx *c) {
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->h_flag) cudaFreeHost(c->h_flag);
   c->h_flag = nullptr;
+  if (c->bucket_exec) cudaGraphExecDestroy(c->bucket_exec);
+  c->bucket_exec = nullptr;
   if (c->side) cudaStreamDestroy(c->side);
   if (c->copy) cudaStreamDestroy(c->copy);
   if (c->layout) cudaStreamDestroy(c->layout);

@@ -48,6 +48,12 @@ struct ngia_ctx {
   uint64_t n_edges = 0;
   // the batched aligner (scratch, side streams, plan, cached graph) on `stream`
   ngia::Round round;
+  // the bucketing's launches (partition passes, resolve) captured as one graph
+  // and replayed while its buffers, n and bands stay the same: at small n its
+  // dozen short launches cost more to issue than to run
+  cudaGraphExec_t bucket_exec = nullptr;
+  const void *bucket_key[3] = {};
+  uint64_t bucket_key_n = 0, bucket_key_gen = 0;
 };
 
 namespace ngia {

@@ -31,6 +31,9 @@ int launch_sketch_table(const uint32_t *packed, const uint32_t *dense, const uin
                         cudaEvent_t fork, cudaEvent_t join);
 
 // sort.cu
+// One-time per-device setup of the sort kernels (attributes); done by the
+// first sort, or ahead of a stream capture.
+int sort_prepare();
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs);
 int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in,
                      uint32_t *keys_out, uint32_t *vals_out, uint32_t seg_len,

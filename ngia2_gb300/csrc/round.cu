@@ -31,14 +31,18 @@ void DevBuf::release() {
 
 double ev_ms(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0.f;
-  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.0;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();  // a stage not timed is not an error of the next call
+    return 0.0;
+  }
   return ms;
 }
 
 bool Round::Key::operator==(const Key &o) const {
   return pairs == o.pairs && scores == o.scores && nib == o.nib && packed == o.packed &&
-         m == o.m && identity == o.identity && round_mode == o.round_mode &&
-         alloc_gen == o.alloc_gen && plan_gen == o.plan_gen;
+         dplanes == o.dplanes && offs == o.offs && lens == o.lens && m == o.m &&
+         identity == o.identity && round_mode == o.round_mode && ab_k == o.ab_k &&
+         ab_inv == o.ab_inv && alloc_gen == o.alloc_gen && plan_gen == o.plan_gen;
 }
 
 int Round::init(cudaStream_t s) {
@@ -139,7 +143,11 @@ int Round::launch(const DbView &db, const uint2 *pairs, uint32_t m, uint32_t ide
                   uint32_t *scores) {
   NGIA_TRY(reserve(m));
   if (!use_graphs) return enqueue(db, pairs, m, identity, scores, nullptr);
-  const Key key{pairs, scores, db.nib, db.packed, m, identity, round_mode(),
+  // everything the captured launches take by value or pointer: the database's
+  // buffers and alphabet (a new load may reuse the buffers with another
+  // alphabet, whose classes are other kernels), the pairs, the plan
+  const Key key{pairs,   scores, db.nib,   db.packed,    db.ab.dplanes, db.offs,
+                db.lens, m,      identity, round_mode(), db.ab.K,       db.ab.inv,
                 g_alloc_gen.load(), plan_gen};
   if (!exec_ || !(key == key_)) {
     if (exec_) cudaGraphExecDestroy(exec_);

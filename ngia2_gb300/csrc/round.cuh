@@ -93,10 +93,10 @@ class Round {
   bool own_stream_ = false;
   cudaGraphExec_t exec_ = nullptr;
   struct Key {
-    const void *pairs, *scores, *nib, *packed;
+    const void *pairs, *scores, *nib, *packed, *dplanes, *offs, *lens;
     uint32_t m, identity;
-    int round_mode;
-    uint64_t alloc_gen, plan_gen;
+    int round_mode, ab_k;
+    uint64_t ab_inv, alloc_gen, plan_gen;
     bool operator==(const Key &o) const;
   } key_{};
 };

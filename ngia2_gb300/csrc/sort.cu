@@ -360,6 +360,8 @@ static int scatter_smem_opt_in() {
   return NGIA_OK;
 }
 
+int sort_prepare() { return scatter_smem_opt_in(); }
+
 size_t radix_sort_scratch_bytes(uint32_t seg_len, uint32_t segs) {
   const size_t ntiles = ceil_div<size_t>(seg_len, kTile);
   const size_t n = (size_t)seg_len * segs;

@@ -189,3 +189,38 @@ def test_host_pairs_are_checked(cuda, built):
             ctx.align_pairs(np.array([[0, 2]], np.uint32), 90)
         s, _ = ctx.align_pairs(np.array([[0, 1]], np.uint32), 80)
         assert s[0] == oracle.align_pairs(packed, offs, np.array([[0, 1]], np.uint32), 80)[0]
+
+
+@pytest.mark.gpu
+def test_replayed_round_follows_a_new_database(cuda, built):
+    """The round's cached graph is keyed on the database's alphabet and
+    buffers: a four-letter nucleotide database (five-entry tables), then the
+    same sequences with a few N (eight-entry tables) loaded into the same
+    context -- the same buffers, lengths, device pairs and scores arrays; each
+    round's scores must be its own database's."""
+    from gpu_util import build_db, to_dev
+    rng = np.random.default_rng(11)
+    s = synth.dna_families(2_000, 200, seed=12)
+    order = np.argsort(-s.lens, kind="stable")
+    seqs = [s.seq(int(i)) for i in order]
+    with_n = []
+    for q in seqs:
+        b = bytearray(q)
+        for p in rng.integers(0, len(b), size=max(1, len(b) // 200)):
+            b[int(p)] = ord("N")
+        with_n.append(bytes(b))
+    a = rng.integers(0, 800, 3000)
+    b = rng.integers(0, 800, 3000)
+    pairs = np.stack([np.minimum(a, b), np.maximum(a, b)], axis=1).astype(np.uint32)
+    pairs = pairs[pairs[:, 0] != pairs[:, 1]]
+    d_pairs = to_dev(pairs)
+    import torch
+    d_scores = torch.zeros(len(pairs), dtype=torch.int32, device="cuda")
+    with ng.Context() as ctx:
+        for db in (build_db(seqs), build_db(with_n)):
+            packed, offs, lens = db
+            ctx.load(packed, offs, lens)
+            ctx.align_pairs_device(d_pairs.data_ptr(), len(pairs), 70, d_scores.data_ptr())
+            got = d_scores.cpu().numpy().view(np.uint32)
+            want = oracle.align_pairs(packed, offs, pairs, 70, oracle.ROUND_FMA)
+            assert np.array_equal(got, want)
