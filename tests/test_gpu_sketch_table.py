@@ -27,9 +27,11 @@ def random_dna(lengths, seed):
 
 @pytest.mark.parametrize("extra", [
     [b"ACGT"[: k % 4 + 1] * (k % 9) for k in range(1, 40)],   # lengths 0..8 included
-    # both sides of the rank walk's minimum span (256 signed positions = length 263),
-    # a record of one repeated 8-mer, and a long one
-    random_dna(list(range(255, 272)) + [20_000], 5) + [b"ACGTACGT" * 400],
+    # both sides of the rank walk's minimum span (512 signed positions = length
+    # 519; 256 = length 263 under the build option), a record of four 8-mers
+    # repeated (the longest walks), and long ones
+    random_dna(list(range(255, 272)) + list(range(511, 528)) + [20_000, 60_000], 5)
+    + [b"ACGTACGT" * 400],
     [b"ACGTNACGTACGT" * 5],                                    # an N: five codes, no table
 ])
 def test_table_sketch_equals_hashing(cuda, built, extra):
