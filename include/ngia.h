@@ -257,8 +257,11 @@ int ngia_ctx_autotune(ngia_ctx *ctx, const uint32_t *d_pairs, uint32_t count,
 
 /* Whether ngia_ctx_align_pairs captures its round (classification, queue
  * sort and every class launch) as a CUDA graph and replays it while the
- * pair/score addresses, count, identity and rounding stay the same (default
- * on).  Returns the previous setting (0/1), or NGIA_ERR_ARG. */
+ * pair/score addresses, count, identity, rounding, plan and the loaded
+ * database (its buffers and alphabet) stay the same, and whether the
+ * bucketing of every graph build is replayed the same way while its buffers,
+ * record count and bands stay the same (default on).  Returns the previous
+ * setting (0/1), or NGIA_ERR_ARG. */
 int ngia_ctx_use_graphs(ngia_ctx *ctx, int on);
 
 /* Same from host arrays (indices checked, NGIA_ERR_ARG when one is out of
