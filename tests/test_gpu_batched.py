@@ -224,3 +224,42 @@ def test_replayed_round_follows_a_new_database(cuda, built):
             got = d_scores.cpu().numpy().view(np.uint32)
             want = oracle.align_pairs(packed, offs, pairs, 70, oracle.ROUND_FMA)
             assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("kind,identities", [("protein", (30, 50, 90, 99)), ("dna", (50, 95))])
+def test_pairs_at_the_longest_record(cuda, built, kind, identities):
+    """Records of the format's longest read (65,534 residues; the packed file
+    drops 65,535 and above) and just below it, close and distant relatives and
+    an unrelated one, every pair: the batched round (the general kernel at low
+    identities) and the drop-in kernel both equal the oracle."""
+    from gpu_util import align_jobs_on_gpu, build_db
+    rng = np.random.default_rng(65534 if kind == "protein" else 65533)
+    alphabet = (np.asarray(synth.AMINO, np.uint8) if kind == "protein"
+                else np.frombuffer(b"ACGT", np.uint8))
+    top = 65534
+
+    def draw(n):
+        return bytes(rng.choice(alphabet, size=n))
+
+    def subst(s, rate):
+        a = np.frombuffer(s, np.uint8).copy()
+        at = rng.random(a.size) < rate
+        a[at] = rng.choice(alphabet, size=int(at.sum()))
+        return bytes(a)
+
+    root = draw(top)
+    seqs = [root, subst(root, 0.03), subst(root, 0.4)[: top - 1000], draw(top - 7)]
+    seqs.sort(key=len, reverse=True)
+    packed, offs, lens = build_db(seqs)
+    assert int(lens[0]) == top
+    pairs = np.array([(r, t) for r in range(4) for t in range(r + 1, 4)], np.uint32)
+    with ng.Context() as ctx:
+        ctx.load(packed, offs, lens)
+        for identity in identities:
+            want = oracle.align_pairs(packed, offs, pairs, identity, oracle.ROUND_FMA)
+            got, _ = ctx.align_pairs(pairs, identity)
+            assert np.array_equal(got, want), identity
+            assert np.array_equal(align_jobs_on_gpu(packed, offs, pairs, identity), want), identity
+    classes = {width_class(int(lens[r]), int(lens[t]), 30) for r, t in pairs}
+    if kind == "protein":
+        assert ng.GENERAL_CLASS in classes, sorted(classes)
