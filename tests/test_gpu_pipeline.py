@@ -145,3 +145,26 @@ def test_run_host_matches_resident_path(cuda, built, golden):
                              np.ascontiguousarray(db["offsets"]),
                              np.ascontiguousarray(db["lens"]), 70, 64, out)
         assert np.array_equal(as_triples(out[:m2]), load_edges("prot", 70, "fma"))
+
+
+def test_makedb_at_the_length_limit_is_byte_identical(cuda, built, tmp_path):
+    """Reads of 65,534 residues kept (signed over 65,527 positions, grouped
+    with their near copies), 65,535 and longer dropped: the device makedb's
+    file equals the reference's own makedb byte for byte."""
+    import oracle
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    rng = np.random.default_rng(65534)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    root = rng.choice(acgt, size=65534)
+    near = root.copy()
+    near[rng.integers(0, near.size, 40)] = rng.choice(acgt, size=40)
+    reads = [rng.choice(acgt, size=120), rng.choice(acgt, size=65535), root,
+             rng.choice(acgt, size=70000), near, rng.choice(acgt, size=65533),
+             np.zeros(0, np.uint8), rng.choice(acgt, size=3000)]
+    fa = tmp_path / "limit.fa"
+    fa.write_bytes(b"".join(b">r%d\n" % i + bytes(r) + b"\n" for i, r in enumerate(reads)))
+    mine, ref = tmp_path / "mine.packed", tmp_path / "ref.packed"
+    assert ng.makedb(fa, mine) == sum(1 for r in reads if r.size < 0xFFFF)
+    assert oracle.ref_makedb(fa, ref) == 0
+    assert mine.read_bytes() == ref.read_bytes()

@@ -84,3 +84,36 @@ def test_index_handles_wrapped_lines_and_stray_records(driver, tmp_path):
     assert name_lens == (2, 2, 2, 4, 2)
     fasta0 = struct.unpack_from("<Q", b, 4 + 16 * 5)[0]
     assert b[fasta0:] == b">a\nAAAACCGG\n>c\nACGTACGT\n>d\nTTTTTTTT\nACGT\nAC\n>b\n\n"
+
+
+def test_length_filter_matches_reference(driver, tmp_path):
+    """Reads at the format's limit: 65,534 residues kept, 65,535 and longer
+    dropped (their records absent from the index and the FASTA area), against
+    the reference's own makedb on the same file."""
+    import oracle
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    rng = np.random.default_rng(0xFFFF)
+    lengths = [120, 65535, 65534, 70000, 8, 65533, 65534, 0, 65536, 3000]
+    fa = tmp_path / "limit.fa"
+    with open(fa, "wb") as f:
+        for i, n in enumerate(lengths):
+            f.write(b">r%d\n" % i + bytes(rng.choice(np.frombuffer(b"ACGT", np.uint8), size=n))
+                    + b"\n")
+    out = tmp_path / "host.packed"
+    r = subprocess.run([str(driver), str(fa), str(out)], capture_output=True, text=True,
+                       check=True)
+    st, scanned, n = map(int, r.stdout.split())
+    assert (st, scanned) == (0, len(lengths))
+    assert n == sum(1 for x in lengths if x < 0xFFFF)
+    ref = tmp_path / "ref.packed"
+    assert oracle.ref_makedb(fa, ref) == 0  # status
+    want = ref.read_bytes()
+    got = out.read_bytes()
+    assert len(got) == len(want)
+    sig0 = 4 + 24 * n
+    fasta0 = struct.unpack_from("<Q", want, 4 + 16 * n)[0]
+    assert got[:sig0] == want[:sig0], "header differs"
+    assert got[fasta0:] == want[fasta0:], "FASTA area differs"
+    lens = struct.unpack_from(f"<{n}I", got, 4 + 4 * n)
+    assert lens == tuple(sorted((x for x in lengths if x < 0xFFFF), reverse=True))
