@@ -226,6 +226,7 @@ def test_replayed_round_follows_a_new_database(cuda, built):
             assert np.array_equal(got, want)
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("kind,identities", [("protein", (30, 50, 90, 99)), ("dna", (50, 95))])
 def test_pairs_at_the_longest_record(cuda, built, kind, identities):
     """Records of the format's longest read (65,534 residues; the packed file
