@@ -23,6 +23,9 @@ int cuda_fail(cudaError_t e);
 // Every kernel launch site calls NGIA_LAUNCHED() right after its launch: it
 // counts the launch (ngia_kernel_launches) and checks the launch error.
 void note_launch();
+// A captured graph's kernels: taken back after its capture (their launch
+// sites counted them then), added at each replay.
+void note_launches(long long delta);
 #define NGIA_LAUNCHED()               \
   do {                                \
     ::ngia::note_launch();            \

@@ -26,6 +26,9 @@ int round_mode() { return g_round_mode; }
 
 static std::atomic<unsigned long long> g_launches(0);
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(long long delta) {
+  g_launches.fetch_add((unsigned long long)delta, std::memory_order_relaxed);
+}
 
 }  // namespace ngia
 
@@ -56,10 +59,7 @@ static int bucket_graph(ngia_ctx *c, uint32_t bands) {
     cudaGraph_t graph = nullptr;
     const cudaError_t e1 = cudaStreamEndCapture(s, &graph);
     if (rc == NGIA_OK && e1 != cudaSuccess) rc = cuda_fail(e1);
-    if (rc == NGIA_OK) {
-      const cudaError_t e2 = cudaGraphInstantiate(&c->bucket_exec, graph, 0);
-      if (e2 != cudaSuccess) rc = cuda_fail(e2);
-    }
+    if (rc == NGIA_OK) rc = instantiate_counted(graph, &c->bucket_exec, &c->bucket_kernels);
     if (graph) cudaGraphDestroy(graph);
     if (rc != NGIA_OK) {
       c->bucket_exec = nullptr;
@@ -72,6 +72,7 @@ static int bucket_graph(ngia_ctx *c, uint32_t bands) {
     c->bucket_key_gen = gen;
   }
   NGIA_CUDA(cudaGraphLaunch(c->bucket_exec, s));
+  note_launches(c->bucket_kernels);
   return NGIA_OK;
 }
 

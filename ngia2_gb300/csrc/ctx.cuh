@@ -52,6 +52,7 @@ struct ngia_ctx {
   // and replayed while its buffers, n and bands stay the same: at small n its
   // dozen short launches cost more to issue than to run
   cudaGraphExec_t bucket_exec = nullptr;
+  uint32_t bucket_kernels = 0;  // kernel nodes of bucket_exec
   const void *bucket_key[3] = {};
   uint64_t bucket_key_n = 0, bucket_key_gen = 0;
 };

@@ -2,6 +2,7 @@
 #include "round.cuh"
 
 #include <cstring>
+#include <vector>
 
 namespace ngia {
 
@@ -36,6 +37,23 @@ double ev_ms(cudaEvent_t a, cudaEvent_t b) {
     return 0.0;
   }
   return ms;
+}
+
+int instantiate_counted(cudaGraph_t graph, cudaGraphExec_t *exec, uint32_t *kernels) {
+  size_t n = 0;
+  NGIA_CUDA(cudaGraphGetNodes(graph, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (n) NGIA_CUDA(cudaGraphGetNodes(graph, nodes.data(), &n));
+  uint32_t k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType t;
+    NGIA_CUDA(cudaGraphNodeGetType(nodes[i], &t));
+    if (t == cudaGraphNodeTypeKernel) ++k;
+  }
+  NGIA_CUDA(cudaGraphInstantiate(exec, graph, 0));
+  note_launches(-(long long)k);
+  *kernels = k;
+  return NGIA_OK;
 }
 
 bool Round::Key::operator==(const Key &o) const {
@@ -157,10 +175,7 @@ int Round::launch(const DbView &db, const uint2 *pairs, uint32_t m, uint32_t ide
     cudaGraph_t graph = nullptr;
     const cudaError_t e1 = cudaStreamEndCapture(stream, &graph);
     if (rc == NGIA_OK && e1 != cudaSuccess) rc = cuda_fail(e1);
-    if (rc == NGIA_OK) {
-      const cudaError_t e2 = cudaGraphInstantiate(&exec_, graph, 0);
-      if (e2 != cudaSuccess) rc = cuda_fail(e2);
-    }
+    if (rc == NGIA_OK) rc = instantiate_counted(graph, &exec_, &exec_kernels_);
     if (graph) cudaGraphDestroy(graph);
     if (rc != NGIA_OK) {
       exec_ = nullptr;
@@ -169,6 +184,7 @@ int Round::launch(const DbView &db, const uint2 *pairs, uint32_t m, uint32_t ide
     key_ = key;
   }
   NGIA_CUDA(cudaGraphLaunch(exec_, stream));
+  note_launches(exec_kernels_);
   return NGIA_OK;
 }
 

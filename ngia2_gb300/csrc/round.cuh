@@ -52,6 +52,11 @@ struct DbView {
 
 double ev_ms(cudaEvent_t a, cudaEvent_t b);
 
+// Instantiates a graph captured from a stream.  Its kernel nodes, which their
+// launch sites counted while it was captured, are taken back from the launch
+// count, and *kernels receives their number for the replays to count.
+int instantiate_counted(cudaGraph_t graph, cudaGraphExec_t *exec, uint32_t *kernels);
+
 struct RoundStats {
   unsigned long long cells, work;  // band cells, computed 32x32 blocks
   double ms_classify, ms_align;    // ms_classify is 0 for a graph replay
@@ -92,6 +97,7 @@ class Round {
   cudaEvent_t join_[kSide] = {}, fork_ = nullptr, ev_[3] = {};
   bool own_stream_ = false;
   cudaGraphExec_t exec_ = nullptr;
+  uint32_t exec_kernels_ = 0;
   struct Key {
     const void *pairs, *scores, *nib, *packed, *dplanes, *offs, *lens;
     uint32_t m, identity;

@@ -72,3 +72,40 @@ def test_small_databases_one_after_another(cuda, built):
         for name, seqs in CASES[2:]:
             check(ctx, seqs, 90)
         check(ctx, CASES[0][1], 90)
+
+
+def test_launch_count_includes_graph_replays(cuda, built):
+    """ngia_kernel_launches counts a cached graph's kernels at every replay
+    and once for the call that captures it: the bucketing inside a graph
+    build and a batched round count the same replayed, captured or launched
+    directly."""
+    s = synth.dna_families(3000, 300, seed=23)
+    packed, offs, lens = build_db(by_length([s.seq(i) for i in range(len(s))]))
+    rng = np.random.default_rng(23)
+    a, b = rng.integers(0, 1500, 4000), rng.integers(0, 1500, 4000)
+    pairs = np.stack([np.minimum(a, b), np.maximum(a, b)], axis=1).astype(np.uint32)
+    pairs = pairs[pairs[:, 0] != pairs[:, 1]]
+
+    def count(fn) -> int:
+        before = ng.kernel_launches()
+        fn()
+        return ng.kernel_launches() - before
+
+    with ng.Context() as ctx:
+        ctx.load(packed, offs, lens)
+        calls = {  # (first key, another key)
+            "graph build": (lambda: ctx.group_align(95, 64), lambda: ctx.group_align(95, 32)),
+            "round": (lambda: ctx.align_pairs(pairs, 70), lambda: ctx.align_pairs(pairs, 80)),
+        }
+        got = {}
+        for name, (first, other) in calls.items():
+            ctx.use_graphs(True)
+            first()  # captured (and the load's one-time work done)
+            got[name, "replayed"] = count(first)
+            got[name, "captured"] = count(other)
+            ctx.use_graphs(False)
+            got[name, "direct"] = count(first)
+            got[name, "direct other"] = count(other)
+    for name in calls:
+        assert got[name, "replayed"] == got[name, "direct"] > 0, got
+        assert got[name, "captured"] == got[name, "direct other"] > 0, got
