@@ -134,3 +134,50 @@ def test_cli_checks_identity_and_bands(built, golden, tmp_path):
     # README spelling: cluster -i -p -r goes to the same checks
     r = run_cli("cluster", "-i", "100", "-p", packed, "-r", str(tmp_path / "r.txt"))
     assert r.returncode == 0 and "identity should be 1-99" in r.stdout
+
+
+def _cli_essentials(out: str, prog: str) -> list[str]:
+    """The lines of a command-line run that carry its outcome: messages and
+    usage text, without dates, timers and the settings the reference echoes."""
+    import re
+    keep = []
+    for line in out.splitlines():
+        s = line.strip()
+        if (not s or "Consuming" in s or re.match(r"^[A-Z][a-z]{2} [A-Z][a-z]{2} +\d", s)
+                or re.match(r"^(use gpu|packed file|result file|fasta file|fasta|packed|"
+                            r"thread|identity|rounds|bands):", s)):
+            continue
+        keep.append(line.replace(prog, "PROG"))
+    return keep
+
+
+def test_cli_parser_quirks_match_the_reference(built, golden, tmp_path):
+    """Argument handling against the reference's own command line (its host
+    build): a later flag overrides an earlier one, the last token is never
+    read as a flag name, invalid identity or bands and a missing file print
+    the usage and exit 0 -- the same messages and exit codes."""
+    import oracle
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    ref = str(oracle.ref_cli())
+    packed = str(golden["prot"]["packed"])
+    out = str(tmp_path / "r.txt")
+    cases = [
+        ["-m", "clustering", "-p", packed, "-r", out, "-i", "95", "-i", "0"],
+        ["-m", "clustering", "-p", packed, "-r", out, "-b", "64", "-b", "65"],
+        ["-m", "clustering", "-p", packed, "-r", out, "-i", "0", "-i"],
+        ["-m", "clustering", "-i", "0", "-p", packed, "-r"],
+        ["-m", "fast", "-p", packed, "-r", out, "-i", "100"],
+        ["-m", "fast", "-p", packed, "-r", out, "-b", "0"],
+        ["-m", "clustering", "-p", str(tmp_path / "missing"), "-r", out],
+        ["-m", "makedb", "-f", str(tmp_path / "missing.fa"), "-p", out],
+        ["-p", packed, "-r", out, "-m"],
+        ["-m", "nonsense"],
+        [],
+    ]
+    for args in cases:
+        a = subprocess.run([ref, *args], capture_output=True, text=True, timeout=60)
+        b = run_cli(*args)
+        assert a.returncode == b.returncode == 0, args
+        assert _cli_essentials(a.stdout, ref) == _cli_essentials(b.stdout, str(ng.CLI_PATH)), \
+            args
