@@ -168,3 +168,23 @@ def test_makedb_at_the_length_limit_is_byte_identical(cuda, built, tmp_path):
     assert ng.makedb(fa, mine) == sum(1 for r in reads if r.size < 0xFFFF)
     assert oracle.ref_makedb(fa, ref) == 0
     assert mine.read_bytes() == ref.read_bytes()
+
+
+def test_makedb_unusual_records_byte_identical(cuda, built, tmp_path):
+    """Lower case, ambiguity and stop letters, digits, tabs and spaces in reads,
+    empty reads and reads over several lines: the device makedb's file equals
+    the reference's own makedb byte for byte (planes, signatures, rep rows)."""
+    import oracle
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    fa = tmp_path / "unusual.fa"
+    fa.write_bytes(b">a desc with spaces\nacgtNNNNacgt\nACGT\n"
+                   b">b\nMKV*LAX-UBZJOx\n"
+                   b">c\n\n\n"
+                   b">d\n" + b"ACGT" * 5 + b"\n" + b"acgu" * 3 + b"\n"
+                   b">e 123\n12345 ACGT\tTT\n"
+                   b">f\nACGTACGT\n")
+    mine, ref = tmp_path / "mine.packed", tmp_path / "ref.packed"
+    assert ng.makedb(fa, mine) == 6
+    assert oracle.ref_makedb(fa, ref) == 0
+    assert mine.read_bytes() == ref.read_bytes()

@@ -117,3 +117,31 @@ def test_length_filter_matches_reference(driver, tmp_path):
     assert got[fasta0:] == want[fasta0:], "FASTA area differs"
     lens = struct.unpack_from(f"<{n}I", got, 4 + 4 * n)
     assert lens == tuple(sorted((x for x in lengths if x < 0xFFFF), reverse=True))
+
+
+def test_unusual_records_match_reference(driver, tmp_path):
+    """Lower case, ambiguity and stop letters, digits, tabs and spaces in reads,
+    description text in names, empty reads and reads over several lines:
+    the index and the FASTA area equal the reference's own makedb."""
+    import oracle
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    fa = tmp_path / "unusual.fa"
+    fa.write_bytes(b">a desc with spaces\nacgtNNNNacgt\nACGT\n"
+                   b">b\nMKV*LAX-UBZJOx\n"
+                   b">c\n\n\n"
+                   b">d\n" + b"ACGT" * 5 + b"\n" + b"acgu" * 3 + b"\n"
+                   b">e 123\n12345 ACGT\tTT\n"
+                   b">f\nACGTACGT\n")
+    out, ref = tmp_path / "host.packed", tmp_path / "ref.packed"
+    r = subprocess.run([str(driver), str(fa), str(out)], capture_output=True, text=True,
+                       check=True)
+    st, scanned, n = map(int, r.stdout.split())
+    assert (st, scanned, n) == (0, 6, 6)
+    assert oracle.ref_makedb(fa, ref) == 0  # status
+    want, got = ref.read_bytes(), out.read_bytes()
+    assert len(got) == len(want)
+    sig0 = 4 + 24 * n
+    fasta0 = struct.unpack_from("<Q", want, 4 + 16 * n)[0]
+    assert got[:sig0] == want[:sig0], "header differs"
+    assert got[fasta0:] == want[fasta0:], "FASTA area differs"
