@@ -115,3 +115,41 @@ def test_round_modes_differ_where_expected(built):
         oracle.band_blocks(300, 300, 90, oracle.ROUND_FMA)
     # the length filter rejects Lt < Lr * t
     assert oracle.band_bounds(100, 89, 90) is None
+
+
+def test_align_matches_reference_kernel_on_random_pairs(built):
+    """The C restatement of the banded LCS against the reference's own
+    kernel_dynamic (its host build), pair by pair, on random related and
+    unrelated pairs over the whole identity range and both roundings --
+    including lengths at the FMA-sensitive multiples of 10 and 32."""
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    rng = np.random.default_rng(31337)
+    amino = np.frombuffer(b"ACDEFGHIKLMNPQRSTVWYX", np.uint8)
+    seqs, pairs = [], []
+    lengths = list(rng.integers(1, 3000, size=240)) + [10, 20, 32, 64, 320, 640, 1000, 2560]
+    for L in lengths:
+        L = int(L)
+        a = rng.choice(amino, size=L)
+        if rng.random() < 0.6:
+            b = a.copy()
+            at = rng.random(L) < rng.uniform(0.0, 0.4)
+            b[at] = rng.choice(amino, size=int(at.sum()))
+            keep = rng.random(L) >= rng.uniform(0.0, 0.05)  # deletions
+            b = b[keep] if keep.any() else b[:1]
+        else:
+            b = rng.choice(amino, size=max(1, int(L * rng.uniform(0.5, 1.0))))
+        seqs += [bytes(a), bytes(b)] if a.size >= b.size else [bytes(b), bytes(a)]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    recs = [oracle.pack_record(s) for s in seqs]
+    offs = np.concatenate([[0], np.cumsum([len(r) for r in recs])[:-1]]).astype(np.uint64)
+    packed = np.concatenate(recs).astype(np.uint32)
+    pairs = np.array(pairs, np.uint32)
+    hits = 0
+    for identity in (1, 10, 30, 50, 70, 80, 90, 95, 99):
+        for mode in (oracle.ROUND_SPLIT, oracle.ROUND_FMA):
+            want = oracle.ref_align_jobs(packed, offs, pairs, identity, mode)
+            got = oracle.align_pairs(packed, offs, pairs, identity, mode)
+            assert np.array_equal(got, want), (identity, mode, np.nonzero(got != want)[0][:5])
+            hits += int((want > 0).sum())
+    assert hits > 0
