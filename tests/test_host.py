@@ -6,6 +6,7 @@ from __future__ import annotations
 import hashlib
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -181,3 +182,78 @@ def test_cli_parser_quirks_match_the_reference(built, golden, tmp_path):
         assert a.returncode == b.returncode == 0, args
         assert _cli_essentials(a.stdout, ref) == _cli_essentials(b.stdout, str(ng.CLI_PATH)), \
             args
+
+
+def planted_graph(rng, n: int, groups: int, p_in: float, out_edges: int) -> np.ndarray:
+    """Edges (rep < tar, sorted, unique) of a graph with planted groups, as
+    the graph build emits them, weights score / 100 for scores 50..100."""
+    label = rng.integers(0, groups, n)
+    pairs = set()
+    for g in range(groups):
+        members = np.nonzero(label == g)[0]
+        for i in range(len(members)):
+            for j in range(i + 1, len(members)):
+                if rng.random() < p_in:
+                    pairs.add((int(members[i]), int(members[j])))
+    for _ in range(out_edges):
+        a, b = (int(x) for x in rng.integers(0, n, 2))
+        if a != b:
+            pairs.add((min(a, b), max(a, b)))
+    e = np.array(sorted(pairs), np.int64).reshape(-1, 2)
+    out = np.zeros(len(e), ng.EDGE_DTYPE)
+    out["rep"], out["tar"] = e[:, 0], e[:, 1]
+    out["weight"] = rng.integers(50, 101, len(e)).astype(np.float32) / np.float32(100)
+    return out
+
+
+@pytest.mark.parametrize("n,groups,p_in,out_edges", [
+    (300, 40, 0.6, 100), (2000, 150, 0.3, 3000), (5000, 60, 0.05, 20000), (4000, 4000, 0.0, 0),
+])
+def test_leiden_matches_reference_on_planted_graphs(built, n, groups, p_in, out_edges):
+    """The host Leiden against the reference's own LeidenOmp (its host build,
+    same seed, same threads) on graphs with planted groups, sparse to dense,
+    isolated nodes included, at the three resolutions the command line uses."""
+    import oracle
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    rng = np.random.default_rng(n + groups)
+    e = planted_graph(rng, n, groups, p_in, out_edges)
+    for resolution in (0.1, 0.2, 1.0):
+        for iterations in (1, 2):
+            want = oracle.ref_leiden(e["rep"].astype(np.int32), e["tar"].astype(np.int32),
+                                     e["weight"], n, resolution, 42, iterations)
+            got = ng.leiden(e, n, resolution, 42, iterations)
+            assert np.array_equal(got, want), (resolution, iterations)
+
+
+LEIDEN_THREADS_CHECK = r'''
+import sys
+sys.path[:0] = [sys.argv[1], sys.argv[1] + "/tests"]
+import numpy as np, oracle, ngia2_gb300 as ng
+from test_host import planted_graph
+e = planted_graph(np.random.default_rng(7), 3000, 100, 0.3, 5000)
+want = oracle.ref_leiden(e["rep"].astype(np.int32), e["tar"].astype(np.int32), e["weight"],
+                         3000, 0.2, 42, 1)
+got = ng.leiden(e, 3000, 0.2, 42, 1)
+import hashlib
+print(int(np.array_equal(got, want)), hashlib.sha256(want.tobytes()).hexdigest())
+'''
+
+
+def test_leiden_follows_the_reference_at_each_thread_count(built):
+    """The reference's LeidenOmp run with 1, 2 and 3 OpenMP threads: the host
+    Leiden equals it at each, and the reference's clusters do not change with
+    the thread count."""
+    import os
+    import oracle
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    seen = set()
+    for threads in (1, 2, 3):
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+        r = subprocess.run([sys.executable, "-c", LEIDEN_THREADS_CHECK, str(ROOT)], env=env,
+                           capture_output=True, text=True, timeout=300, check=True)
+        same, head = r.stdout.split()
+        assert same == "1", threads
+        seen.add(head)
+    assert len(seen) == 1
