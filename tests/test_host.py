@@ -257,3 +257,32 @@ def test_leiden_follows_the_reference_at_each_thread_count(built):
         assert same == "1", threads
         seen.add(head)
     assert len(seen) == 1
+
+
+def test_result_file_matches_reference_on_any_clustering(built, golden, tmp_path):
+    """SaveResult against the reference's own (its host build) on clusterings
+    the golden sets do not hold: all singletons, one cluster, fast-mode root
+    ids, ids numbered in an arbitrary order, and ids larger than n."""
+    import oracle
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    packed = golden["prot"]["packed"]
+    n = golden["prot"]["db"]["n"]
+    rng = np.random.default_rng(99)
+    roots = np.arange(n, dtype=np.uint32)
+    for i in range(1, n):
+        if rng.random() < 0.7:
+            roots[i] = roots[rng.integers(0, i)]
+    labels = rng.integers(0, 37, n).astype(np.uint32)
+    cases = {
+        "singletons": np.arange(n, dtype=np.uint32),
+        "one cluster": np.zeros(n, np.uint32),
+        "roots": roots,
+        "arbitrary order": rng.permutation(37).astype(np.uint32)[labels],
+        "large ids": (labels * 1_000_003 + 7).astype(np.uint32),
+    }
+    for name, cluster in cases.items():
+        mine, ref = tmp_path / "mine.txt", tmp_path / "ref.txt"
+        ng.save_result(cluster, packed, mine)
+        oracle.ref_save(cluster, packed, ref)
+        assert mine.read_bytes() == ref.read_bytes(), name
