@@ -153,3 +153,46 @@ def test_align_matches_reference_kernel_on_random_pairs(built):
             assert np.array_equal(got, want), (identity, mode, np.nonzero(got != want)[0][:5])
             hits += int((want > 0).sum())
     assert hits > 0
+
+
+def test_pack_sketch_bucket_match_reference_makedb_on_random_reads(built, tmp_path):
+    """The restated pack, sketch and grouping against the reference's own
+    makedb (its host build) on random protein and nucleotide reads of 0 to
+    4,000 residues -- lengths under 8 included -- with near copies so that
+    bands group: the planes, the seq-major signatures (makedb without its
+    grouping step) and the rep rows (with it)."""
+    import ngia2_gb300 as ng
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    rng = np.random.default_rng(2024)
+    amino = np.frombuffer(b"ACDEFGHIKLMNPQRSTVWYXBZ*", np.uint8)
+    acgt = np.frombuffer(b"ACGTN", np.uint8)
+    reads = []
+    for k in range(400):
+        letters = amino if k % 2 else acgt
+        L = int(rng.integers(0, 12)) if k % 10 == 0 else int(rng.integers(0, 4000))
+        r = rng.choice(letters, size=L)
+        reads.append(r)
+        if L and rng.random() < 0.4:  # a near copy
+            c = r.copy()
+            at = rng.random(L) < 0.02
+            c[at] = rng.choice(letters, size=int(at.sum()))
+            reads.append(c)
+    fa = tmp_path / "random.fa"
+    fa.write_bytes(b"".join(b">s%d\n" % i + bytes(r) + b"\n" for i, r in enumerate(reads)))
+    seq_major, grouped = tmp_path / "nogroup.packed", tmp_path / "group.packed"
+    assert oracle.ref_makedb(fa, seq_major, group=False) == 0
+    assert oracle.ref_makedb(fa, grouped, group=True) == 0
+    db = ng.read_packed(grouped)
+    n = db["n"]
+    assert n == len(reads)
+    order = sorted(range(n), key=lambda i: -len(reads[i]))  # stable, length descending
+    for i, o in zip(order, db["offsets"]):
+        rec = db["packed"][int(o):int(o) + 1 + ((len(reads[i]) + 31) // 32) * 4]
+        assert np.array_equal(oracle.pack_record(bytes(reads[i])), rec), i
+    sigs = oracle.sketch_all(db["packed"], db["offsets"], db["lens"])
+    raw = np.fromfile(seq_major, np.uint8)
+    ref_sigs = raw[4 + 24 * n:4 + 24 * n + 256 * n].view(np.uint32).reshape(n, 64)
+    assert np.array_equal(sigs, ref_sigs.T)
+    for b in range(64):
+        assert np.array_equal(oracle.bucket_band(sigs[b]), db["rep"][b]), b
