@@ -155,16 +155,10 @@ def test_align_matches_reference_kernel_on_random_pairs(built):
     assert hits > 0
 
 
-def test_pack_sketch_bucket_match_reference_makedb_on_random_reads(built, tmp_path):
-    """The restated pack, sketch and grouping against the reference's own
-    makedb (its host build) on random protein and nucleotide reads of 0 to
-    4,000 residues -- lengths under 8 included -- with near copies so that
-    bands group: the planes, the seq-major signatures (makedb without its
-    grouping step) and the rep rows (with it)."""
-    import ngia2_gb300 as ng
-    if not oracle.ref_available():
-        pytest.skip("the reference's host build is not available")
-    rng = np.random.default_rng(2024)
+def random_reads_fasta(tmp_path, seed: int = 2024):
+    """Random protein and nucleotide reads of 0 to 4,000 residues (every tenth
+    under 12), 40 % of them followed by a near copy (2 % substitutions)."""
+    rng = np.random.default_rng(seed)
     amino = np.frombuffer(b"ACDEFGHIKLMNPQRSTVWYXBZ*", np.uint8)
     acgt = np.frombuffer(b"ACGTN", np.uint8)
     reads = []
@@ -180,6 +174,19 @@ def test_pack_sketch_bucket_match_reference_makedb_on_random_reads(built, tmp_pa
             reads.append(c)
     fa = tmp_path / "random.fa"
     fa.write_bytes(b"".join(b">s%d\n" % i + bytes(r) + b"\n" for i, r in enumerate(reads)))
+    return reads, fa
+
+
+def test_pack_sketch_bucket_match_reference_makedb_on_random_reads(built, tmp_path):
+    """The restated pack, sketch and grouping against the reference's own
+    makedb (its host build) on random protein and nucleotide reads of 0 to
+    4,000 residues -- lengths under 8 included -- with near copies so that
+    bands group: the planes, the seq-major signatures (makedb without its
+    grouping step) and the rep rows (with it)."""
+    import ngia2_gb300 as ng
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    reads, fa = random_reads_fasta(tmp_path)
     seq_major, grouped = tmp_path / "nogroup.packed", tmp_path / "group.packed"
     assert oracle.ref_makedb(fa, seq_major, group=False) == 0
     assert oracle.ref_makedb(fa, grouped, group=True) == 0
@@ -196,3 +203,29 @@ def test_pack_sketch_bucket_match_reference_makedb_on_random_reads(built, tmp_pa
     assert np.array_equal(sigs, ref_sigs.T)
     for b in range(64):
         assert np.array_equal(oracle.bucket_band(sigs[b]), db["rep"][b]), b
+
+
+def test_graph_matches_reference_build_graph_on_random_reads(built, tmp_path):
+    """Candidate collection, scores and edge emission restated, against the
+    reference's own readData + buildGraph on the grouped random reads, at
+    identities 50 to 95, 64 and 7 bands, both roundings."""
+    import ngia2_gb300 as ng
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    _, fa = random_reads_fasta(tmp_path, seed=77)
+    packed = tmp_path / "group.packed"
+    assert oracle.ref_makedb(fa, packed, group=True) == 0
+    db = ng.read_packed(packed)
+    edges = 0
+    split, fma = oracle.ROUND_SPLIT, oracle.ROUND_FMA
+    for identity, bands, mode in ((50, 64, fma), (80, 7, split), (90, 64, split),
+                                  (90, 64, fma), (95, 64, fma), (95, 7, split)):
+        mine, _ = oracle.graph_edges(db["packed"], db["offsets"], db["lens"], db["rep"],
+                                     identity, bands, mode)
+        rep, tar, w = oracle.ref_build_graph(packed, identity, bands, 4096, mode)
+        ref = np.stack([rep.astype(np.int64), tar.astype(np.int64),
+                        np.rint(w.astype(np.float64) * 100).astype(np.int64)], axis=1)
+        ref = ref[np.lexsort((ref[:, 1], ref[:, 0]))]
+        assert np.array_equal(mine, ref), (identity, bands, mode)
+        edges += len(mine)
+    assert edges > 0
