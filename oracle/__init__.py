@@ -168,6 +168,33 @@ def graph_edges(packed, offsets, lens, rep, identity: int, bands: int,
     return e, total
 
 
+def fast_cluster(packed, offsets, rep, identity: int, bands: int,
+                 mode: int = ROUND_FMA) -> np.ndarray:
+    """Fast mode restated (FastClustering::cluster, src/fastClustering.hpp:249-352).
+    Bands in order; in band b every record i whose rep is not itself and that
+    no earlier band assigned (the list is fixed before the band's alignments)
+    is aligned against rep[b][i] with the kernel's scoring, and a hit makes
+    that rep its parent.  A record's cluster id is its root: itself when it
+    has no parent, else its parent's root (parents have lower indices)."""
+    n = rep.shape[1] if rep.ndim == 2 else 0
+    free = np.uint32(0xFFFFFFFF)
+    parent = np.full(n, free, np.uint32)
+    idx = np.arange(n, dtype=np.uint32)
+    for b in range(bands):
+        row = np.ascontiguousarray(rep[b], np.uint32)
+        tar = np.nonzero((row != idx) & (parent == free))[0]
+        if len(tar) == 0:
+            continue
+        pairs = np.stack([row[tar], tar.astype(np.uint32)], axis=1)
+        hit = align_pairs(packed, offsets, pairs, identity, mode) > 0
+        parent[tar[hit]] = row[tar[hit]]
+    root = np.empty(n, np.uint32)
+    for i in range(n):
+        p = parent[i]
+        root[i] = i if p == free else root[p]
+    return root
+
+
 # ---- the reference itself, built as a host program -------------------------------------
 def ref_available() -> bool:
     return (REF / "libngia_ref.so").exists()

@@ -229,3 +229,31 @@ def test_graph_matches_reference_build_graph_on_random_reads(built, tmp_path):
         assert np.array_equal(mine, ref), (identity, bands, mode)
         edges += len(mine)
     assert edges > 0
+
+
+@pytest.mark.parametrize("name,identity", [(s, i) for s in SETS for i in IDENTITIES[s]])
+def test_fast_cluster_matches_reference(built, golden, name, identity):
+    """The restated fast mode against the reference's own fast clusters
+    (golden fixtures from its FastClustering::cluster)."""
+    db = golden[name]["db"]
+    got = oracle.fast_cluster(db["packed"], db["offsets"], db["rep"], identity, 64)
+    assert np.array_equal(got, np.load(GOLDEN / f"{name}.fast_{identity}.npy"))
+
+
+def test_fast_cluster_matches_reference_on_random_reads(built, tmp_path):
+    """The restated fast mode against the reference's host build on the
+    grouped random reads, several identities and band counts."""
+    import ngia2_gb300 as ng
+    if not oracle.ref_available():
+        pytest.skip("the reference's host build is not available")
+    _, fa = random_reads_fasta(tmp_path, seed=5)
+    packed = tmp_path / "group.packed"
+    assert oracle.ref_makedb(fa, packed, group=True) == 0
+    db = ng.read_packed(packed)
+    merged = 0
+    for identity, bands in ((50, 64), (90, 64), (95, 9)):
+        got = oracle.fast_cluster(db["packed"], db["offsets"], db["rep"], identity, bands)
+        want = oracle.ref_fast_cluster(packed, identity, bands, db["n"])
+        assert np.array_equal(got, want), (identity, bands)
+        merged += int((got != np.arange(db["n"])).sum())
+    assert merged > 0
