@@ -286,3 +286,39 @@ def test_result_file_matches_reference_on_any_clustering(built, golden, tmp_path
         ng.save_result(cluster, packed, mine)
         oracle.ref_save(cluster, packed, ref)
         assert mine.read_bytes() == ref.read_bytes(), name
+
+
+C_CALLER = r'''
+#include <stdio.h>
+#include "ngia.h"
+int main(void) {
+  ngia_stats st;
+  (void)st;
+  printf("%s|%s|%d\n", ngia_version(), ngia_status_string(NGIA_ERR_ARG),
+         ngia_bucket(0, 0, 65, 0, 0));
+  return 0;
+}
+'''
+
+
+@pytest.mark.parametrize("compiler,flags", [("gcc", ["-std=c99", "-x", "c"]),
+                                            ("g++", ["-std=c++11", "-x", "c++"])])
+def test_header_builds_a_plain_c_and_cpp_caller(built, tmp_path, compiler, flags):
+    """include/ngia.h compiles warning-free as C99 and as C++11 (-Wall -Wextra
+    -pedantic -Werror), and a caller links libngia.so and calls it without a
+    GPU (argument checks only)."""
+    import shutil
+    cc = shutil.which(compiler)
+    if cc is None:
+        pytest.skip(f"{compiler} not available")
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    lib = ROOT / "ngia2_gb300" / "lib"
+    subprocess.run([cc, *flags, "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                    str(ROOT / "include"), str(src), "-x", "none", "-o", str(exe),
+                    "-L", str(lib), "-lngia", f"-Wl,-rpath,{lib}"],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60,
+                         check=True).stdout.strip().split("|")
+    assert out[0] and out[1] and int(out[2]) == ng.ERR_ARG
